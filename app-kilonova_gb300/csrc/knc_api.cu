@@ -1,0 +1,1240 @@
+// knc_api.cu — host runtime behind include/knc.h.
+//
+// Owns the device state of one simulation and sequences the stage kernels.
+// It restates the orchestration of src/scheme.rs:212-240 (advance: dt once,
+// then `fold` x {add_remove_blocks, RK step}), the RK driver of
+// godunov_core::runge_kutta (Shu-Osher forms, b = 1/2; 3/4 then 1/3) and the
+// State bookkeeping of src/state.rs (time and Rational64 iteration averaged
+// with the same weights as the conserved data). Geometry tables follow
+// src/mesh.rs:119-407 and are computed here once per block.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "knc_internal.h"
+
+using namespace knc;
+
+namespace {
+
+constexpr double PI_H = 3.14159265358979323846;
+constexpr double LIGHT_SPEED_H = 3e10;
+
+// ---------------------------------------------------------------- geometry --
+struct ExtentH { double r0, r1, q0, q1; };
+
+struct MeshH {
+    knc_mesh_params p;
+    double zone_dlogr() const {                                   // mesh.rs:341-346
+        return p.has_num_radial_zones ? 1.0 / (double)p.num_radial_zones : PI_H / (double)p.num_polar_zones;
+    }
+    double block_dlogr() const { return (double)p.block_size * zone_dlogr(); }
+    ExtentH extent(int32_t index) const {                         // mesh.rs:358-372
+        double q0 = 0.0, q1 = PI_H;
+        if (p.num_polar_zones == 1) { q0 = PI_H * 0.5 - zone_dlogr(); q1 = PI_H * 0.5 + zone_dlogr(); }
+        ExtentH e;
+        e.r0 = p.reference_radius * std::pow(1.0 + block_dlogr(), (double)index);
+        e.r1 = p.reference_radius * std::pow(1.0 + block_dlogr(), (double)index + 1.0);
+        e.q0 = q0;
+        e.q1 = q1;
+        return e;
+    }
+    double t_start() const { return p.has_excision_delay ? p.excision_delay : 0.0; }
+    double ies(double t) const { return p.inner_radius + std::max(t - t_start(), 0.0) * p.inner_excision_speed; }
+    double oes(double t) const { return p.outer_radius + std::max(t - t_start(), 0.0) * p.outer_excision_speed; }
+    bool moving() const { return p.inner_excision_speed > 0.0 || p.outer_excision_speed > 0.0; }
+};
+
+// SphericalPolarGrid::vertex_coordinate_signed (mesh.rs:202-210); Rust's
+// f64::log(base) is ln(x) / ln(base).
+double vertex_r(const ExtentH& e, int64_t nr, int64_t i) {
+    const double y0 = std::log(e.r0) / std::log(10.0);
+    const double y1 = std::log(e.r1) / std::log(10.0);
+    const double dy = (y1 - y0) / (double)nr;
+    return std::pow(10.0, y0 + dy * (double)i);
+}
+double vertex_q(const ExtentH& e, int64_t nq, int64_t j) {
+    const double dq = (e.q1 - e.q0) / (double)nq;
+    return e.q0 + dq * (double)j;
+}
+double cell_volume(double r0, double q0, double r1, double q1) {            // mesh.rs:119-123
+    const double dcost = -(std::cos(q1) - std::cos(q0));
+    return 2.0 * PI_H * (r1 * r1 * r1 - r0 * r0 * r0) / 3.0 * dcost;
+}
+double face_area(double r0, double q0, double r1, double q1) {              // mesh.rs:125-134
+    const double s0 = r0 * std::sin(q0);
+    const double s1 = r1 * std::sin(q1);
+    const double z0 = r0 * std::cos(q0);
+    const double z1 = r1 * std::cos(q1);
+    const double ds = s1 - s0;
+    const double dz = z1 - z0;
+    return PI_H * (s0 + s1) * std::sqrt(ds * ds + dz * dz);
+}
+
+struct GeomH {
+    int64_t nr = 0, nq = 0;
+    std::vector<double> rv, qv, ar, aq, dv, rc, qc, cot;
+    std::vector<float> ar_r, ar_q, aq_r, aq_q, dv_r, dv_q, rc32, cot32;
+};
+
+GeomH make_geometry(const MeshH& M, int32_t index, bool with_faces = true) {   // mesh.rs:246-264
+    GeomH G;
+    const ExtentH e = M.extent(index);
+    const int64_t nr = M.p.block_size, nq = M.p.num_polar_zones;
+    G.nr = nr;
+    G.nq = nq;
+    G.rv.resize(nr + 1);
+    G.qv.resize(nq + 1);
+    for (int64_t i = 0; i <= nr; ++i) G.rv[i] = vertex_r(e, nr, i);
+    for (int64_t j = 0; j <= nq; ++j) G.qv[j] = vertex_q(e, nq, j);
+    G.dv.resize(nr * nq);
+    G.rc.resize(nr);
+    G.qc.resize(nq);
+    G.cot.resize(nq);
+    for (int64_t i = 0; i < nr; ++i) {
+        G.rc[i] = std::sqrt(G.rv[i] * G.rv[i + 1]);                              // mesh.rs:157-161
+        for (int64_t j = 0; j < nq; ++j)
+            G.dv[i * nq + j] = cell_volume(G.rv[i], G.qv[j], G.rv[i + 1], G.qv[j + 1]);
+    }
+    for (int64_t j = 0; j < nq; ++j) {
+        G.qc[j] = 0.5 * (G.qv[j] + G.qv[j + 1]);
+        G.cot[j] = std::cos(G.qc[j]) / std::sin(G.qc[j]);
+    }
+    if (!with_faces) return G;
+    G.ar.resize((nr + 1) * nq);
+    G.aq.resize(nr * (nq + 1));
+    for (int64_t i = 0; i <= nr; ++i)
+        for (int64_t j = 0; j < nq; ++j) G.ar[i * nq + j] = face_area(G.rv[i], G.qv[j], G.rv[i], G.qv[j + 1]);
+    for (int64_t i = 0; i < nr; ++i)
+        for (int64_t j = 0; j <= nq; ++j)
+            G.aq[i * (nq + 1) + j] = face_area(G.rv[i], G.qv[j], G.rv[i + 1], G.qv[j]);
+    // separable FP32 factors for the mixed path
+    G.ar_r.resize(nr + 1);
+    G.aq_r.resize(nr);
+    G.dv_r.resize(nr);
+    G.rc32.resize(nr);
+    for (int64_t i = 0; i <= nr; ++i) G.ar_r[i] = (float)(G.rv[i] * G.rv[i]);
+    for (int64_t i = 0; i < nr; ++i) {
+        const double a = G.rv[i], b = G.rv[i + 1];
+        G.aq_r[i] = (float)(PI_H * (b * b - a * a));
+        G.dv_r[i] = (float)((b * b * b - a * a * a) * 2.0 * PI_H / 3.0);
+        G.rc32[i] = (float)G.rc[i];
+    }
+    G.ar_q.resize(nq);
+    G.aq_q.resize(nq + 1);
+    G.dv_q.resize(nq);
+    G.cot32.resize(nq);
+    for (int64_t j = 0; j < nq; ++j) {
+        const double s0 = std::sin(G.qv[j]), s1 = std::sin(G.qv[j + 1]);
+        const double c0 = std::cos(G.qv[j]), c1 = std::cos(G.qv[j + 1]);
+        G.ar_q[j] = (float)(PI_H * (s0 + s1) * std::sqrt((s1 - s0) * (s1 - s0) + (c1 - c0) * (c1 - c0)));
+        G.dv_q[j] = (float)(c0 - c1);
+        G.cot32[j] = (float)G.cot[j];
+    }
+    for (int64_t j = 0; j <= nq; ++j) G.aq_q[j] = (float)std::sin(G.qv[j]);
+    return G;
+}
+
+// ---------------------------------------------------------------- helpers --
+struct Rational {
+    int64_t n = 0, d = 1;
+    static int64_t gcd(int64_t a, int64_t b) {
+        if (a < 0) a = -a;
+        if (b < 0) b = -b;
+        while (b) { const int64_t t = a % b; a = b; b = t; }
+        return a ? a : 1;
+    }
+    void norm() { const int64_t g = gcd(n, d); n /= g; d /= g; if (d < 0) { n = -n; d = -d; } }
+    Rational add(const Rational& o) const { Rational r; r.n = n * o.d + o.n * d; r.d = d * o.d; r.norm(); return r; }
+    Rational mul(const Rational& o) const { Rational r; r.n = n * o.n; r.d = d * o.d; r.norm(); return r; }
+};
+
+template <class T>
+cudaError_t dalloc(T** p, size_t count) {
+    if (count == 0) { *p = nullptr; return cudaSuccess; }
+    return cudaMalloc((void**)p, count * sizeof(T));
+}
+template <class T>
+cudaError_t upload(T** p, const std::vector<T>& v, cudaStream_t s) {
+    cudaError_t e = dalloc(p, v.size());
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+}
+
+struct BlockH {
+    int32_t index = 0;
+    int64_t nr = 0, nq = 0;
+    double* buf[2] = {nullptr, nullptr};
+    void* P = nullptr;
+    double *ar = nullptr, *aq = nullptr, *dv = nullptr, *rc = nullptr, *rv = nullptr;
+    float *ar_r = nullptr, *aq_r = nullptr, *dv_r = nullptr, *rc32 = nullptr;
+    GeomH geom;   // host copy (rc, qc for error positions; dv for error values)
+};
+
+void free_block(BlockH& b) {
+    cudaFree(b.buf[0]);
+    cudaFree(b.buf[1]);
+    cudaFree(b.P);
+    cudaFree(b.ar);
+    cudaFree(b.aq);
+    cudaFree(b.dv);
+    cudaFree(b.rc);
+    cudaFree(b.rv);
+    cudaFree(b.ar_r);
+    cudaFree(b.aq_r);
+    cudaFree(b.dv_r);
+    cudaFree(b.rc32);
+    b = BlockH();
+}
+
+}  // namespace
+
+struct knc_ctx {
+    knc_hydro_params hp{};
+    MeshH mesh{};
+    knc_model_params model{};
+    bool have_model = false;
+    knc_primitive_at_fn host_fn = nullptr;
+    void* host_user = nullptr;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::map<int32_t, BlockH> blocks;
+    std::map<std::pair<int64_t, int64_t>, std::vector<BlockH>> pool;   // freed block storage by shape
+    int cur = 0;
+    // per-column tables (all blocks share the mesh's polar grid)
+    double *d_qv = nullptr, *d_qc = nullptr, *d_cot = nullptr;
+    float *d_ar_q = nullptr, *d_aq_q = nullptr, *d_dv_q = nullptr, *d_cot32 = nullptr;
+    GeomH col;   // host copy of the column tables
+    // device block table and tiles
+    DevBlock* d_table = nullptr;
+    int table_cap = 0;
+    int4* d_tiles = nullptr;
+    int tiles_cap = 0;
+    int ntiles = 0;
+    bool dirty = true;
+    std::vector<int32_t> slot_index;   // slot -> block index, current table
+    // ghost rows
+    int32_t ghost_lo = INT32_MIN, ghost_hi = INT32_MIN;
+    double* d_ghost_rc = nullptr;    // [2][2]
+    double* d_ghost_dv = nullptr;    // [2][2][nq]
+    double* d_host_prim = nullptr;   // host model values
+    size_t host_prim_cap = 0;
+    std::vector<double> ghost_rc_h, ghost_dv_h;
+    // status
+    DevStatus* d_status = nullptr;
+    DevStatus* h_status = nullptr;
+    int32_t stage_counter = 0;
+    bool failed = false;
+    // time
+    double time = 0.0;
+    Rational iteration;
+    // chosen forms
+    int32_t precision = KNC_PRECISION_FP64;
+    int32_t guess = KNC_GUESS_PLAIN;
+    int32_t batched = 0;
+    double w_split = 2.0;
+    float* d_mlp = nullptr;
+    // bookkeeping
+    int64_t launches = 0;
+    knc_error err{};
+    double* d_stage = nullptr;
+    size_t stage_cap = 0;
+};
+
+namespace {
+
+int set_msg(knc_ctx* c, int status, const char* fmt, ...) __attribute__((format(printf, 3, 4)));
+int set_msg(knc_ctx* c, int status, const char* fmt, ...) {
+    if (!c) return status;
+    std::memset(&c->err, 0, sizeof(c->err));
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(c->err.message, sizeof(c->err.message), fmt, ap);
+    va_end(ap);
+    return status;
+}
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) {                                                                   \
+            if (e_ == cudaErrorMemoryAllocation)                                                   \
+                return set_msg(c, KNC_ERR_OUT_OF_MEMORY, "%s: %s", #call, cudaGetErrorString(e_)); \
+            return set_msg(c, KNC_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));               \
+        }                                                                                          \
+    } while (0)
+
+int validate(knc_ctx* c, const knc_hydro_params* h, const knc_mesh_params* m) {
+    if (h->system != KNC_SYSTEM_RELATIVISTIC && h->system != KNC_SYSTEM_NEWTONIAN)
+        return set_msg(c, KNC_ERR_CONFIG, "unknown hydro system %d", h->system);
+    if (h->plm_theta < 1.0 || h->plm_theta > 2.0)
+        return set_msg(c, KNC_ERR_CONFIG, "plm_theta must be in the range [1, 2]");
+    if (h->cfl_number < 0.0 || h->cfl_number > 0.7)
+        return set_msg(c, KNC_ERR_CONFIG, "cfl_number must be in the range [0.0, 0.7]");
+    if (h->runge_kutta_order < 1 || h->runge_kutta_order > 3)
+        return set_msg(c, KNC_ERR_CONFIG, "runge_kutta_order must be RK1, RK2 or RK3");
+    if (h->riemann_solver != KNC_RIEMANN_HLLE && h->riemann_solver != KNC_RIEMANN_HLLC)
+        return set_msg(c, KNC_ERR_CONFIG, "unknown riemann solver");
+    if (!(h->gamma_law_index > 1.0)) return set_msg(c, KNC_ERR_CONFIG, "gamma_law_index must exceed 1");
+    if (m->reference_radius <= 0.0 || m->inner_radius < 0.0 || m->outer_radius < 0.0)
+        return set_msg(c, KNC_ERR_CONFIG, "all radii must be positive");
+    MeshH M;
+    M.p = *m;
+    if (m->reference_radius > M.oes(0.0))
+        return set_msg(c, KNC_ERR_CONFIG, "the reference radius is outside the outer excision surface");
+    if (m->has_excision_delay && m->excision_delay < 0.0)
+        return set_msg(c, KNC_ERR_CONFIG, "the excision delay time must be non-negative");
+    if (m->inner_excision_speed < 0.0 || m->outer_excision_speed < 0.0)
+        return set_msg(c, KNC_ERR_CONFIG, "the excision surface speeds must be non-negative");
+    if (m->outer_excision_speed < m->inner_excision_speed)
+        return set_msg(c, KNC_ERR_CONFIG, "outer_excision_speed < inner_excision_speed");
+    if (m->block_size < 2) return set_msg(c, KNC_ERR_CONFIG, "must have at least 2 radial zones per block");
+    if (m->num_polar_zones != 1 && m->num_polar_zones < 16)
+        return set_msg(c, KNC_ERR_CONFIG, "must have at least 16 polar zones");
+    if (m->num_polar_zones == 1 && !m->has_num_radial_zones)
+        return set_msg(c, KNC_ERR_CONFIG, "num_radial_zones is not optional when num_polar_zones=1");
+    if (m->block_size > 16383 || m->num_polar_zones > 65535)
+        return set_msg(c, KNC_ERR_CONFIG, "block shape exceeds 16383 x 65535");
+    return KNC_OK;
+}
+
+int alloc_block(knc_ctx* c, int32_t index, BlockH& b) {
+    const int64_t nr = c->mesh.p.block_size, nq = c->mesh.p.num_polar_zones;
+    auto key = std::make_pair(nr, nq);
+    auto it = c->pool.find(key);
+    b.geom = make_geometry(c->mesh, index);
+    b.index = index;
+    b.nr = nr;
+    b.nq = nq;
+    if (it != c->pool.end() && !it->second.empty()) {
+        BlockH r = it->second.back();
+        it->second.pop_back();
+        b.buf[0] = r.buf[0];
+        b.buf[1] = r.buf[1];
+        b.P = r.P;
+        b.ar = r.ar;
+        b.aq = r.aq;
+        b.dv = r.dv;
+        b.rc = r.rc;
+        b.rv = r.rv;
+        b.ar_r = r.ar_r;
+        b.aq_r = r.aq_r;
+        b.dv_r = r.dv_r;
+        b.rc32 = r.rc32;
+    } else {
+        const size_t n = (size_t)(nr * nq);
+        CK(dalloc(&b.buf[0], 5 * n));
+        CK(dalloc(&b.buf[1], 5 * n));
+        CK(cudaMalloc(&b.P, 5 * (size_t)((nr + 4) * nq) * sizeof(double)));
+        CK(dalloc(&b.ar, (size_t)((nr + 1) * nq)));
+        CK(dalloc(&b.aq, (size_t)(nr * (nq + 1))));
+        CK(dalloc(&b.dv, n));
+        CK(dalloc(&b.rc, (size_t)nr));
+        CK(dalloc(&b.rv, (size_t)nr + 1));
+        CK(dalloc(&b.ar_r, (size_t)nr + 1));
+        CK(dalloc(&b.aq_r, (size_t)nr));
+        CK(dalloc(&b.dv_r, (size_t)nr));
+        CK(dalloc(&b.rc32, (size_t)nr));
+    }
+    const GeomH& G = b.geom;
+    cudaStream_t s = c->stream;
+    CK(cudaMemcpyAsync(b.ar, G.ar.data(), G.ar.size() * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.aq, G.aq.data(), G.aq.size() * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.dv, G.dv.data(), G.dv.size() * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.rc, G.rc.data(), G.rc.size() * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.rv, G.rv.data(), G.rv.size() * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.ar_r, G.ar_r.data(), G.ar_r.size() * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.aq_r, G.aq_r.data(), G.aq_r.size() * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.dv_r, G.dv_r.data(), G.dv_r.size() * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.rc32, G.rc32.data(), G.rc32.size() * 4, cudaMemcpyHostToDevice, s));
+    // host geometry vectors are only needed for positions, volumes, ghosts
+    b.geom.ar.clear();
+    b.geom.ar.shrink_to_fit();
+    b.geom.aq.clear();
+    b.geom.aq.shrink_to_fit();
+    // zero the primitive array so halo rows of an edge block start defined
+    CK(cudaMemsetAsync(b.P, 0, 5 * (size_t)((b.nr + 4) * b.nq) * sizeof(double), s));
+    // the copies above read host vectors that live in `b`; finish them now
+    CK(cudaStreamSynchronize(s));
+    return KNC_OK;
+}
+
+void release_block(knc_ctx* c, BlockH& b) {
+    c->pool[std::make_pair(b.nr, b.nq)].push_back(b);
+    b = BlockH();
+}
+
+// Rebuild the device block table and the tile list after the block set changed.
+int rebuild_table(knc_ctx* c) {
+    if (!c->dirty) return KNC_OK;
+    const int nb = (int)c->blocks.size();
+    std::vector<DevBlock> tab(nb);
+    std::vector<int4> tiles;
+    c->slot_index.clear();
+    int slot = 0;
+    int64_t zoff = 0;
+    const BlockH* prev = nullptr;
+    std::vector<const BlockH*> order;
+    for (auto& kv : c->blocks) order.push_back(&kv.second);
+    for (int k = 0; k < nb; ++k) {
+        const BlockH& b = *order[k];
+        DevBlock& d = tab[k];
+        std::memset(&d, 0, sizeof(d));
+        d.buf[0] = b.buf[0];
+        d.buf[1] = b.buf[1];
+        d.P = b.P;
+        d.ar = b.ar;
+        d.aq = b.aq;
+        d.dv = b.dv;
+        d.rc = b.rc;
+        d.rv = b.rv;
+        d.qv = c->d_qv;
+        d.qc = c->d_qc;
+        d.cot = c->d_cot;
+        d.ar_r = b.ar_r;
+        d.ar_q = c->d_ar_q;
+        d.aq_r = b.aq_r;
+        d.aq_q = c->d_aq_q;
+        d.dv_r = b.dv_r;
+        d.dv_q = c->d_dv_q;
+        d.rc32 = b.rc32;
+        d.cot32 = c->d_cot32;
+        d.nr = (int32_t)b.nr;
+        d.nq = (int32_t)b.nq;
+        d.index = b.index;
+        if (prev && prev->index + 1 == b.index && prev->nq == b.nq) {
+            d.P_in_nbr = prev->P;
+            d.nr_in_nbr = (int32_t)prev->nr;
+            tab[k - 1].P_out_nbr = b.P;
+            tab[k - 1].nr_out_nbr = (int32_t)b.nr;
+        }
+        for (int64_t i0 = 0; i0 < b.nr; i0 += TILE_R)
+            for (int64_t j0 = 0; j0 < b.nq; j0 += TILE_Q)
+                tiles.push_back(make_int4(slot, (int)i0, (int)j0, (int)zoff));
+        c->slot_index.push_back(b.index);
+        zoff += b.nr * b.nq;
+        prev = &b;
+        ++slot;
+    }
+    if (nb > c->table_cap) {
+        cudaFree(c->d_table);
+        c->d_table = nullptr;
+        CK(dalloc(&c->d_table, (size_t)nb));
+        c->table_cap = nb;
+    }
+    if ((int)tiles.size() > c->tiles_cap) {
+        cudaFree(c->d_tiles);
+        c->d_tiles = nullptr;
+        CK(dalloc(&c->d_tiles, tiles.size()));
+        c->tiles_cap = (int)tiles.size();
+    }
+    if (nb) CK(cudaMemcpyAsync(c->d_table, tab.data(), nb * sizeof(DevBlock), cudaMemcpyHostToDevice, c->stream));
+    if (!tiles.empty())
+        CK(cudaMemcpyAsync(c->d_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->ntiles = (int)tiles.size();
+    c->dirty = false;
+    return KNC_OK;
+}
+
+// Geometry of the two ghost rows next to the mesh at each end.
+int update_ghost_geometry(knc_ctx* c) {
+    if (c->blocks.empty()) return KNC_OK;
+    const int32_t lo = c->blocks.begin()->first - 1, hi = c->blocks.rbegin()->first + 1;
+    if (lo == c->ghost_lo && hi == c->ghost_hi && c->d_ghost_rc) return KNC_OK;
+    const int64_t nq = c->mesh.p.num_polar_zones, nr = c->mesh.p.block_size;
+    const GeomH gl = make_geometry(c->mesh, lo, false), gh = make_geometry(c->mesh, hi, false);
+    c->ghost_rc_h = {gl.rc[nr - 2], gl.rc[nr - 1], gh.rc[0], gh.rc[1]};
+    c->ghost_dv_h.resize(4 * nq);
+    for (int64_t j = 0; j < nq; ++j) {
+        c->ghost_dv_h[0 * nq + j] = gl.dv[(nr - 2) * nq + j];
+        c->ghost_dv_h[1 * nq + j] = gl.dv[(nr - 1) * nq + j];
+        c->ghost_dv_h[2 * nq + j] = gh.dv[0 * nq + j];
+        c->ghost_dv_h[3 * nq + j] = gh.dv[1 * nq + j];
+    }
+    if (!c->d_ghost_rc) {
+        CK(dalloc(&c->d_ghost_rc, 4));
+        CK(dalloc(&c->d_ghost_dv, (size_t)(4 * nq)));
+    }
+    CK(cudaMemcpyAsync(c->d_ghost_rc, c->ghost_rc_h.data(), 4 * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_ghost_dv, c->ghost_dv_h.data(), 4 * nq * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->ghost_lo = lo;
+    c->ghost_hi = hi;
+    return KNC_OK;
+}
+
+int ensure_host_prim(knc_ctx* c, size_t n) {
+    if (n <= c->host_prim_cap) return KNC_OK;
+    cudaFree(c->d_host_prim);
+    c->d_host_prim = nullptr;
+    CK(dalloc(&c->d_host_prim, n));
+    c->host_prim_cap = n;
+    return KNC_OK;
+}
+
+// Host model values of the ghost rows (slow path: the model is a callback).
+int host_ghost_values(knc_ctx* c, double t) {
+    const int64_t nq = c->mesh.p.num_polar_zones;
+    std::vector<double> v(4 * nq * 5);
+    for (int k = 0; k < 4; ++k)
+        for (int64_t j = 0; j < nq; ++j) {
+            double any[4], s = 0.0;
+            c->host_fn(c->ghost_rc_h[k], c->col.qc[j], t, any, &s, c->host_user);
+            double* o = &v[((int64_t)k * nq + j) * 5];
+            o[0] = any[2];   // interpret: AnyPrimitive [u_r, u_q, rho, p] -> (rho, u_r, u_q, p)
+            o[1] = any[0];
+            o[2] = any[1];
+            o[3] = any[3];
+            o[4] = s;
+        }
+    int r = ensure_host_prim(c, v.size());
+    if (r) return r;
+    CK(cudaMemcpyAsync(c->d_host_prim, v.data(), v.size() * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return KNC_OK;
+}
+
+StageArgs base_args(knc_ctx* c) {
+    StageArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.blocks = c->d_table;
+    a.tiles = c->d_tiles;
+    a.ntiles = c->ntiles;
+    a.srhd = c->hp.system == KNC_SYSTEM_RELATIVISTIC;
+    a.hllc = c->hp.riemann_solver == KNC_RIEMANN_HLLC;
+    a.one_dimensional = c->mesh.p.num_polar_zones == 1;
+    a.guess = c->guess;
+    a.gm = c->hp.gamma_law_index;
+    a.plm_theta = c->hp.plm_theta;
+    a.cflux = a.srhd ? LIGHT_SPEED_H : 1.0;
+    a.w_split = c->w_split;
+    a.mlp = c->guess == KNC_GUESS_MLP ? c->d_mlp : nullptr;
+    a.status = c->d_status;
+    a.sel_base = -1;
+    return a;
+}
+
+bool mixed(const knc_ctx* c) { return c->precision == KNC_PRECISION_MIXED; }
+
+int launch_c2p(knc_ctx* c, const StageArgs& a) {
+    cudaError_t e = mixed(c) ? launch_c2p_mixed(a, c->stream) : launch_c2p_f64(a, c->stream);
+    ++c->launches;
+    CK(e);
+    return KNC_OK;
+}
+
+int launch_update(knc_ctx* c, const StageArgs& a) {
+    cudaError_t e = mixed(c) ? launch_update_mixed(a, c->stream) : launch_update_f64(a, c->stream);
+    ++c->launches;
+    CK(e);
+    return KNC_OK;
+}
+
+// One Euler stage U_out = avg(U_in + dt L(U_in), U_base), src/scheme.rs:16-173.
+int run_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, double bf, double t_stage,
+              double dt) {
+    int r;
+    if (c->stage_counter >= 0xffff) return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "too many stages in one call");
+    const int32_t stage = c->stage_counter++;
+    // ghost rows at the stage time
+    GhostArgs g;
+    std::memset(&g, 0, sizeof(g));
+    const BlockH& first = c->blocks.begin()->second;
+    const BlockH& last = c->blocks.rbegin()->second;
+    g.P[0] = first.P;
+    g.P[1] = last.P;
+    g.row0[0] = 0;
+    g.row0[1] = (int32_t)last.nr + 2;
+    g.nr_t[0] = (int32_t)first.nr;
+    g.nr_t[1] = (int32_t)last.nr;
+    g.nq = (int32_t)c->mesh.p.num_polar_zones;
+    g.ghost_index[0] = c->ghost_lo;
+    g.ghost_index[1] = c->ghost_hi;
+    g.rc = c->d_ghost_rc;
+    g.dv = c->d_ghost_dv;
+    g.qc = c->d_qc;
+    g.model = c->model;
+    g.time = t_stage;
+    g.srhd = c->hp.system == KNC_SYSTEM_RELATIVISTIC;
+    g.stage = stage;
+    g.gm = c->hp.gamma_law_index;
+    g.single_precision = mixed(c) ? 1 : 0;
+    g.status = c->d_status;
+    if (c->model.kind == KNC_MODEL_HOST) {
+        if ((r = host_ghost_values(c, t_stage))) return r;
+        g.host_prim = c->d_host_prim;
+    }
+    CK(launch_ghost(g, c->stream));
+    ++c->launches;
+    StageArgs a = base_args(c);
+    a.stage = stage;
+    a.sel_in = sel_in;
+    a.sel_out = sel_out;
+    a.sel_base = sel_base;
+    a.w1 = w1;
+    a.bf = bf;
+    a.dt = dt;
+    if ((r = launch_c2p(c, a))) return r;
+    if ((r = launch_update(c, a))) return r;
+    return KNC_OK;
+}
+
+// godunov_core::runge_kutta::try_advance_async restated (SSP RK1/RK2/RK3).
+int rk_step(knc_ctx* c, double dt) {
+    const int A = c->cur, B = 1 - c->cur;
+    const double t0 = c->time;
+    const Rational it0 = c->iteration;
+    Rational one;
+    one.n = 1;
+    auto avg_time = [](double t1, double tb, double bf) { return t1 * (-bf + 1.0) + tb * bf; };
+    auto avg_iter = [&](Rational i1, Rational br) {
+        Rational mbr = br;
+        mbr.n = -mbr.n;
+        return i1.mul(mbr.add(one)).add(it0.mul(br));
+    };
+    int r;
+    const int order = c->hp.runge_kutta_order;
+    if ((r = run_stage(c, A, B, -1, 1.0, 0.0, t0, dt))) return r;
+    double t1 = t0 + dt;
+    Rational i1 = it0.add(one);
+    if (order == 1) {
+        c->cur = B;
+        c->time = t1;
+        c->iteration = i1;
+        return KNC_OK;
+    }
+    if (order == 2) {
+        const double bf = 0.5;
+        if ((r = run_stage(c, B, A, A, -bf + 1.0, bf, t1, dt))) return r;
+        Rational half;
+        half.n = 1;
+        half.d = 2;
+        c->time = avg_time(t1 + dt, t0, bf);
+        c->iteration = avg_iter(i1.add(one), half);
+        return KNC_OK;
+    }
+    // RK3
+    const double b2 = 0.75;
+    if ((r = run_stage(c, B, B, A, -b2 + 1.0, b2, t1, dt))) return r;
+    Rational q34;
+    q34.n = 3;
+    q34.d = 4;
+    const double t2 = avg_time(t1 + dt, t0, b2);
+    const Rational i2 = avg_iter(i1.add(one), q34);
+    const double b3 = 1.0 / 3.0;
+    if ((r = run_stage(c, B, A, A, -b3 + 1.0, b3, t2, dt))) return r;
+    Rational q13;
+    q13.n = 1;
+    q13.d = 3;
+    c->time = avg_time(t2 + dt, t0, b3);
+    c->iteration = avg_iter(i2.add(one), q13);
+    return KNC_OK;
+}
+
+// Read the device status; on a hydro failure fill c->err from the failing zone.
+int check_status(knc_ctx* c) {
+    CK(cudaMemcpyAsync(c->h_status, c->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    const unsigned long long k = c->h_status->err_key;
+    if (k == NO_ERROR) return KNC_OK;
+    c->failed = true;
+    const uint32_t slot = (uint32_t)((k >> 34) & 0x3fffu);
+    const int32_t i = (int32_t)((k >> 20) & 0x3fffu);
+    const int32_t j = (int32_t)((k >> 4) & 0xffffu);
+    const int32_t kind = (int32_t)(k & 0xfu);
+    std::memset(&c->err, 0, sizeof(c->err));
+    c->err.kind = kind;
+    c->err.i = i;
+    c->err.j = j;
+    if (slot >= 0x3ffeu) {
+        const int end = (int)(slot - 0x3ffeu);
+        c->err.block = end ? c->ghost_hi : c->ghost_lo;
+        c->err.r = c->ghost_rc_h.empty() ? 0.0 : c->ghost_rc_h[end * 2 + i];
+        c->err.theta = c->col.qc.empty() ? 0.0 : c->col.qc[j];
+    } else if (slot < c->slot_index.size()) {
+        const int32_t index = c->slot_index[slot];
+        c->err.block = index;
+        auto it = c->blocks.find(index);
+        if (it != c->blocks.end()) {
+            const BlockH& b = it->second;
+            c->err.r = b.geom.rc[i];
+            c->err.theta = c->col.qc[j];
+            const int sel = c->h_status->err_sel;
+            double u[5];
+            const int64_t n = b.nr * b.nq, z = (int64_t)i * b.nq + j;
+            for (int q = 0; q < 5; ++q)
+                CK(cudaMemcpy(&u[q], b.buf[sel] + q * n + z, 8, cudaMemcpyDeviceToHost));
+            const double dV = b.geom.dv[z];
+            c->err.value = kind == KNC_HYDRO_NEGATIVE_ENERGY_DENSITY ? u[3] / dV : u[0] / dV;
+        }
+    }
+    static const char* names[] = {"None", "NegativeDensity", "NegativePressure", "NegativeEnergyDensity",
+                                  "RootFinderFailed"};
+    std::snprintf(c->err.message, sizeof(c->err.message),
+                  "%s(%.4e) at position (r, theta) = (%.4e, %.4f) in block %d zone (%d, %d)",
+                  names[kind <= 4 ? kind : 0], c->err.value, c->err.r, c->err.theta, c->err.block, i, j);
+    return KNC_ERR_HYDRO;
+}
+
+int reset_status(knc_ctx* c, bool keep_stats) {
+    DevStatus s;
+    if (keep_stats) {
+        CK(cudaMemcpyAsync(&s, c->d_status, sizeof(s), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    } else {
+        std::memset(&s, 0, sizeof(s));
+    }
+    s.err_key = NO_ERROR;
+    s.err_sel = 0;
+    s.dt_bits = ~0ull;
+    CK(cudaMemcpyAsync(c->d_status, &s, sizeof(s), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->stage_counter = 0;
+    return KNC_OK;
+}
+
+int init_block_from_model(knc_ctx* c, int32_t index, double t) {
+    // the new block is the last slot; run the init kernel on its tiles only
+    int r;
+    if ((r = rebuild_table(c))) return r;
+    int slot = -1;
+    for (size_t k = 0; k < c->slot_index.size(); ++k)
+        if (c->slot_index[k] == index) slot = (int)k;
+    if (slot < 0) return set_msg(c, KNC_ERR_NO_BLOCK, "block %d missing", index);
+    std::vector<int4> tiles;
+    const BlockH& b = c->blocks.at(index);
+    for (int64_t i0 = 0; i0 < b.nr; i0 += TILE_R)
+        for (int64_t j0 = 0; j0 < b.nq; j0 += TILE_Q) tiles.push_back(make_int4(slot, (int)i0, (int)j0, 0));
+    int4* d_t = nullptr;
+    CK(dalloc(&d_t, tiles.size()));
+    CK(cudaMemcpyAsync(d_t, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
+    InitArgs ia;
+    std::memset(&ia, 0, sizeof(ia));
+    ia.blocks = c->d_table;
+    ia.tiles = d_t;
+    ia.sel = c->cur;
+    ia.srhd = c->hp.system == KNC_SYSTEM_RELATIVISTIC;
+    ia.gm = c->hp.gamma_law_index;
+    ia.time = t;
+    ia.model = c->model;
+    if (c->model.kind == KNC_MODEL_HOST) {
+        const int64_t nz = b.nr * b.nq;
+        std::vector<double> v(nz * 5);
+        for (int64_t i = 0; i < b.nr; ++i)
+            for (int64_t j = 0; j < b.nq; ++j) {
+                double any[4], s = 0.0;
+                c->host_fn(b.geom.rc[i], c->col.qc[j], t, any, &s, c->host_user);
+                double* o = &v[(i * b.nq + j) * 5];
+                o[0] = any[2];
+                o[1] = any[0];
+                o[2] = any[1];
+                o[3] = any[3];
+                o[4] = s;
+            }
+        if ((r = ensure_host_prim(c, v.size()))) return r;
+        CK(cudaMemcpyAsync(c->d_host_prim, v.data(), v.size() * 8, cudaMemcpyHostToDevice, c->stream));
+        ia.host_prim = c->d_host_prim;
+    }
+    cudaError_t e = launch_init_f64(ia, (int)tiles.size(), c->stream);
+    ++c->launches;
+    cudaError_t e2 = cudaStreamSynchronize(c->stream);
+    cudaFree(d_t);
+    CK(e);
+    CK(e2);
+    return KNC_OK;
+}
+
+int insert_block(knc_ctx* c, int32_t index) {
+    auto it = c->blocks.find(index);
+    if (it != c->blocks.end()) return KNC_OK;
+    BlockH b;
+    int r = alloc_block(c, index, b);
+    if (r) return r;
+    c->blocks.emplace(index, b);
+    c->dirty = true;
+    return KNC_OK;
+}
+
+// add_remove_blocks, src/scheme.rs:179-206
+int add_remove_blocks(knc_ctx* c) {
+    if (c->blocks.empty()) return KNC_OK;
+    const int32_t inner = c->blocks.begin()->first;
+    const int32_t outer = c->blocks.rbegin()->first;
+    const bool drop = c->mesh.extent(inner).r1 < c->mesh.ies(c->time);
+    const bool add = c->mesh.extent(outer).r1 < c->mesh.oes(c->time);
+    if (!drop && !add) return KNC_OK;
+    int r;
+    // surface errors of the steps so far before the slot layout changes
+    if ((r = check_status(c))) return r;
+    if (drop) {
+        release_block(c, c->blocks.at(inner));
+        c->blocks.erase(inner);
+        c->dirty = true;
+    }
+    if (add) {
+        const int32_t nb = outer + 1;
+        if ((r = insert_block(c, nb))) return r;
+        if ((r = init_block_from_model(c, nb, c->time))) return r;
+        // initial data of an activated block is noise-free, as for ghosts
+    }
+    if ((r = rebuild_table(c))) return r;
+    if ((r = update_ghost_geometry(c))) return r;
+    return KNC_OK;
+}
+
+int check_ready(knc_ctx* c) {
+    if (c->blocks.empty()) return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "no blocks");
+    if (!c->have_model) return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "no model set (ghost blocks need one)");
+    int32_t prev = INT32_MIN;
+    for (auto& kv : c->blocks) {
+        if (prev != INT32_MIN && kv.first != prev + 1)
+            return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "block indexes are not contiguous (%d after %d)",
+                           kv.first, prev);
+        prev = kv.first;
+    }
+    if (c->failed) return set_msg(c, KNC_ERR_HYDRO, "state invalid after an earlier hydro error: %s",
+                                  c->err.message);
+    if (mixed(c) && c->hp.system != KNC_SYSTEM_RELATIVISTIC)
+        return set_msg(c, KNC_ERR_UNSUPPORTED, "the mixed-precision stage is built for relativistic hydro");
+    if (c->mesh.p.num_polar_zones == 1 && mixed(c))
+        return set_msg(c, KNC_ERR_UNSUPPORTED, "mixed precision needs num_polar_zones > 1");
+    return KNC_OK;
+}
+
+int time_step_impl(knc_ctx* c, double* dt) {
+    const bool global = c->hp.system == KNC_SYSTEM_RELATIVISTIC && !c->hp.adaptive_time_step;
+    if (global) {   // cfl * smallest_spacing(innermost) / c, state.rs:147-149
+        const ExtentH e = c->mesh.extent(c->blocks.begin()->first);
+        const int64_t nr = c->mesh.p.block_size;
+        const double spacing = vertex_r(e, nr, 1) - vertex_r(e, nr, 0);
+        *dt = c->hp.cfl_number * spacing / LIGHT_SPEED_H;
+        return KNC_OK;
+    }
+    int r;
+    if ((r = rebuild_table(c))) return r;
+    // adaptive: full c2p pass with the dl / a_max reduction
+    unsigned long long big = ~0ull;
+    CK(cudaMemcpyAsync(&c->d_status->dt_bits, &big, 8, cudaMemcpyHostToDevice, c->stream));
+    StageArgs a = base_args(c);
+    a.stage = c->stage_counter++;
+    a.sel_in = c->cur;
+    a.sel_out = c->cur;
+    a.compute_dt = 1;
+    // the reduction runs in the FP64 c2p kernel whatever the precision mode
+    CK(launch_c2p_f64(a, c->stream));
+    ++c->launches;
+    if ((r = check_status(c))) return r;
+    double dtmin;
+    std::memcpy(&dtmin, &c->h_status->dt_bits, 8);
+    *dt = dtmin * c->hp.cfl_number;
+    return KNC_OK;
+}
+
+int setup_columns(knc_ctx* c) {
+    const GeomH G = make_geometry(c->mesh, 0);
+    c->col = G;
+    cudaStream_t s = c->stream;
+    CK(upload(&c->d_qv, G.qv, s));
+    CK(upload(&c->d_qc, G.qc, s));
+    CK(upload(&c->d_cot, G.cot, s));
+    CK(upload(&c->d_ar_q, G.ar_q, s));
+    CK(upload(&c->d_aq_q, G.aq_q, s));
+    CK(upload(&c->d_dv_q, G.dv_q, s));
+    CK(upload(&c->d_cot32, G.cot32, s));
+    CK(cudaStreamSynchronize(s));
+    return KNC_OK;
+}
+
+int ensure_stage(knc_ctx* c, size_t doubles) {
+    if (doubles <= c->stage_cap) return KNC_OK;
+    cudaFree(c->d_stage);
+    c->d_stage = nullptr;
+    CK(dalloc(&c->d_stage, doubles));
+    c->stage_cap = doubles;
+    return KNC_OK;
+}
+
+int create_device_side(knc_ctx* c) {
+    int r;
+    CK(cudaGetDevice(&c->device));
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CK(dalloc(&c->d_status, 1));
+    CK(cudaMallocHost((void**)&c->h_status, sizeof(DevStatus)));
+    if ((r = setup_columns(c))) return r;
+    return reset_status(c, false);
+}
+
+}  // namespace
+
+// =========================================================================== C ABI
+extern "C" {
+
+const char* knc_status_string(int s) {
+    switch (s) {
+    case KNC_OK: return "ok";
+    case KNC_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case KNC_ERR_CONFIG: return "invalid configuration";
+    case KNC_ERR_CUDA: return "CUDA error";
+    case KNC_ERR_NO_BLOCK: return "no such block";
+    case KNC_ERR_HYDRO: return "hydro error";
+    case KNC_ERR_UNSUPPORTED: return "unsupported";
+    case KNC_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case KNC_ERR_TIMEOUT: return "timeout";
+    default: return "unknown status";
+    }
+}
+
+int knc_create(const knc_hydro_params* hydro, const knc_mesh_params* mesh, knc_ctx** out) {
+    if (!hydro || !mesh || !out) return KNC_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    knc_ctx* c = new knc_ctx();
+    int r = validate(c, hydro, mesh);
+    if (r) { delete c; return r; }
+    c->hp = *hydro;
+    c->mesh.p = *mesh;
+    c->iteration.n = 0;
+    c->iteration.d = 1;
+    r = create_device_side(c);
+    if (r) { knc_destroy(c); return r; }
+    *out = c;
+    return KNC_OK;
+}
+
+void knc_destroy(knc_ctx* c) {
+    if (!c) return;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& kv : c->blocks) free_block(kv.second);
+    for (auto& kv : c->pool)
+        for (auto& b : kv.second) free_block(b);
+    cudaFree(c->d_qv);
+    cudaFree(c->d_qc);
+    cudaFree(c->d_cot);
+    cudaFree(c->d_ar_q);
+    cudaFree(c->d_aq_q);
+    cudaFree(c->d_dv_q);
+    cudaFree(c->d_cot32);
+    cudaFree(c->d_table);
+    cudaFree(c->d_tiles);
+    cudaFree(c->d_ghost_rc);
+    cudaFree(c->d_ghost_dv);
+    cudaFree(c->d_host_prim);
+    cudaFree(c->d_status);
+    cudaFree(c->d_mlp);
+    cudaFree(c->d_stage);
+    if (c->h_status) cudaFreeHost(c->h_status);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int knc_last_error(const knc_ctx* c, knc_error* out) {
+    if (!c || !out) return KNC_ERR_INVALID_ARGUMENT;
+    *out = c->err;
+    return KNC_OK;
+}
+
+int knc_set_model(knc_ctx* c, const knc_model_params* m) {
+    if (!c || !m) return KNC_ERR_INVALID_ARGUMENT;
+    if (m->kind < KNC_MODEL_WIND || m->kind > KNC_MODEL_SPHERE)
+        return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "unknown model kind %d", m->kind);
+    c->model = *m;
+    c->have_model = true;
+    return KNC_OK;
+}
+
+int knc_set_host_model(knc_ctx* c, knc_primitive_at_fn fn, void* user) {
+    if (!c || !fn) return KNC_ERR_INVALID_ARGUMENT;
+    std::memset(&c->model, 0, sizeof(c->model));
+    c->model.kind = KNC_MODEL_HOST;
+    c->host_fn = fn;
+    c->host_user = user;
+    c->have_model = true;
+    return KNC_OK;
+}
+
+int knc_init_from_model(knc_ctx* c, double time) {
+    if (!c) return KNC_ERR_INVALID_ARGUMENT;
+    if (!c->have_model) return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "no model set");
+    int r;
+    CK(cudaStreamSynchronize(c->stream));
+    for (auto& kv : c->blocks) release_block(c, kv.second);
+    c->blocks.clear();
+    c->dirty = true;
+    std::vector<int32_t> idx;
+    for (int32_t i = 0;; ++i) {                              // Mesh::grid_blocks, mesh.rs:384-397
+        if (c->mesh.extent(i).r0 >= c->mesh.oes(time)) break;
+        idx.push_back(i);
+        if (i > 100000) return set_msg(c, KNC_ERR_CONFIG, "mesh has more than 100000 blocks");
+    }
+    c->cur = 0;
+    for (int32_t i : idx)
+        if ((r = insert_block(c, i))) return r;
+    if ((r = rebuild_table(c))) return r;
+    InitArgs ia;
+    std::memset(&ia, 0, sizeof(ia));
+    ia.blocks = c->d_table;
+    ia.tiles = c->d_tiles;
+    ia.sel = c->cur;
+    ia.srhd = c->hp.system == KNC_SYSTEM_RELATIVISTIC;
+    ia.gm = c->hp.gamma_law_index;
+    ia.time = time;
+    ia.model = c->model;
+    if (c->model.kind == KNC_MODEL_HOST) {
+        int64_t nz = 0;
+        for (auto& kv : c->blocks) nz += kv.second.nr * kv.second.nq;
+        std::vector<double> v(nz * 5);
+        int64_t off = 0;
+        for (auto& kv : c->blocks) {
+            const BlockH& b = kv.second;
+            for (int64_t i = 0; i < b.nr; ++i)
+                for (int64_t j = 0; j < b.nq; ++j) {
+                    double any[4], s = 0.0;
+                    c->host_fn(b.geom.rc[i], c->col.qc[j], time, any, &s, c->host_user);
+                    double* o = &v[(off + i * b.nq + j) * 5];
+                    o[0] = any[2];
+                    o[1] = any[0];
+                    o[2] = any[1];
+                    o[3] = any[3];
+                    o[4] = s;
+                }
+            off += b.nr * b.nq;
+        }
+        if ((r = ensure_host_prim(c, v.size()))) return r;
+        CK(cudaMemcpyAsync(c->d_host_prim, v.data(), v.size() * 8, cudaMemcpyHostToDevice, c->stream));
+        ia.host_prim = c->d_host_prim;
+    }
+    CK(launch_init_f64(ia, c->ntiles, c->stream));
+    ++c->launches;
+    CK(cudaStreamSynchronize(c->stream));
+    c->time = time;
+    c->iteration.n = 0;
+    c->iteration.d = 1;
+    c->failed = false;
+    if ((r = reset_status(c, true))) return r;
+    return update_ghost_geometry(c);
+}
+
+int knc_add_block(knc_ctx* c, int32_t index, const double* cons, const double* scalar) {
+    if (!c || !cons || !scalar) return KNC_ERR_INVALID_ARGUMENT;
+    int r;
+    if ((r = insert_block(c, index))) return r;
+    BlockH& b = c->blocks.at(index);
+    const size_t n = (size_t)(b.nr * b.nq);
+    if ((r = ensure_stage(c, 5 * n))) return r;
+    CK(cudaMemcpyAsync(c->d_stage, cons, 4 * n * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_stage + 4 * n, scalar, n * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(launch_aos_to_soa(c->d_stage, c->d_stage + 4 * n, b.buf[c->cur], b.nr, b.nq, c->stream));
+    ++c->launches;
+    CK(cudaStreamSynchronize(c->stream));
+    c->failed = false;
+    if ((r = reset_status(c, true))) return r;
+    return update_ghost_geometry(c);
+}
+
+int knc_remove_block(knc_ctx* c, int32_t index) {
+    if (!c) return KNC_ERR_INVALID_ARGUMENT;
+    auto it = c->blocks.find(index);
+    if (it == c->blocks.end()) return set_msg(c, KNC_ERR_NO_BLOCK, "no block %d", index);
+    CK(cudaStreamSynchronize(c->stream));
+    release_block(c, it->second);
+    c->blocks.erase(it);
+    c->dirty = true;
+    return c->blocks.empty() ? KNC_OK : update_ghost_geometry(c);
+}
+
+int knc_get_block(knc_ctx* c, int32_t index, double* cons, double* scalar) {
+    if (!c) return KNC_ERR_INVALID_ARGUMENT;
+    auto it = c->blocks.find(index);
+    if (it == c->blocks.end()) return set_msg(c, KNC_ERR_NO_BLOCK, "no block %d", index);
+    const BlockH& b = it->second;
+    const size_t n = (size_t)(b.nr * b.nq);
+    int r;
+    if ((r = ensure_stage(c, 5 * n))) return r;
+    CK(launch_soa_to_aos(b.buf[c->cur], c->d_stage, c->d_stage + 4 * n, b.nr, b.nq, c->stream));
+    ++c->launches;
+    if (cons) CK(cudaMemcpyAsync(cons, c->d_stage, 4 * n * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (scalar) CK(cudaMemcpyAsync(scalar, c->d_stage + 4 * n, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return KNC_OK;
+}
+
+int knc_num_blocks(const knc_ctx* c, int32_t* n) {
+    if (!c || !n) return KNC_ERR_INVALID_ARGUMENT;
+    *n = (int32_t)c->blocks.size();
+    return KNC_OK;
+}
+
+int knc_block_indexes(const knc_ctx* c, int32_t* out, int32_t capacity) {
+    if (!c || !out) return KNC_ERR_INVALID_ARGUMENT;
+    if ((int32_t)c->blocks.size() > capacity) return KNC_ERR_INVALID_ARGUMENT;
+    int32_t k = 0;
+    for (auto& kv : c->blocks) out[k++] = kv.first;
+    return KNC_OK;
+}
+
+int knc_block_shape(const knc_ctx* c, int64_t* nr, int64_t* nq) {
+    if (!c) return KNC_ERR_INVALID_ARGUMENT;
+    if (nr) *nr = c->mesh.p.block_size;
+    if (nq) *nq = c->mesh.p.num_polar_zones;
+    return KNC_OK;
+}
+
+int knc_set_state(knc_ctx* c, const double* cons, const double* scalar) {
+    if (!c || !cons || !scalar) return KNC_ERR_INVALID_ARGUMENT;
+    int64_t total = 0;
+    for (auto& kv : c->blocks) total += kv.second.nr * kv.second.nq;
+    int r;
+    if ((r = ensure_stage(c, 5 * (size_t)total))) return r;
+    CK(cudaMemcpyAsync(c->d_stage, cons, 4 * total * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_stage + 4 * total, scalar, total * 8, cudaMemcpyHostToDevice, c->stream));
+    int64_t off = 0;
+    for (auto& kv : c->blocks) {
+        BlockH& b = kv.second;
+        CK(launch_aos_to_soa(c->d_stage + 4 * off, c->d_stage + 4 * total + off, b.buf[c->cur], b.nr, b.nq,
+                             c->stream));
+        ++c->launches;
+        off += b.nr * b.nq;
+    }
+    c->failed = false;
+    return KNC_OK;
+}
+
+int knc_get_state(knc_ctx* c, double* cons, double* scalar) {
+    if (!c || !cons || !scalar) return KNC_ERR_INVALID_ARGUMENT;
+    int64_t total = 0;
+    for (auto& kv : c->blocks) total += kv.second.nr * kv.second.nq;
+    int r;
+    if ((r = ensure_stage(c, 5 * (size_t)total))) return r;
+    int64_t off = 0;
+    for (auto& kv : c->blocks) {
+        BlockH& b = kv.second;
+        CK(launch_soa_to_aos(b.buf[c->cur], c->d_stage + 4 * off, c->d_stage + 4 * total + off, b.nr, b.nq,
+                             c->stream));
+        ++c->launches;
+        off += b.nr * b.nq;
+    }
+    CK(cudaMemcpyAsync(cons, c->d_stage, 4 * total * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(scalar, c->d_stage + 4 * total, total * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return KNC_OK;
+}
+
+int knc_set_time(knc_ctx* c, double time, int64_t num, int64_t den) {
+    if (!c || den == 0) return KNC_ERR_INVALID_ARGUMENT;
+    c->time = time;
+    c->iteration.n = num;
+    c->iteration.d = den;
+    c->iteration.norm();
+    return KNC_OK;
+}
+
+int knc_get_time(const knc_ctx* c, double* time, int64_t* num, int64_t* den) {
+    if (!c) return KNC_ERR_INVALID_ARGUMENT;
+    if (time) *time = c->time;
+    if (num) *num = c->iteration.n;
+    if (den) *den = c->iteration.d;
+    return KNC_OK;
+}
+
+int knc_time_step(knc_ctx* c, double* dt) {
+    if (!c || !dt) return KNC_ERR_INVALID_ARGUMENT;
+    int r;
+    if ((r = check_ready(c))) return r;
+    if ((r = reset_status(c, true))) return r;
+    return time_step_impl(c, dt);
+}
+
+int knc_advance(knc_ctx* c, int32_t fold) {
+    if (!c || fold < 0) return KNC_ERR_INVALID_ARGUMENT;
+    int r;
+    if ((r = check_ready(c))) return r;
+    if ((r = rebuild_table(c))) return r;
+    if ((r = update_ghost_geometry(c))) return r;
+    if ((r = reset_status(c, true))) return r;
+    double dt;
+    if ((r = time_step_impl(c, &dt))) return r;
+    const int per_step = c->hp.runge_kutta_order;
+    for (int32_t k = 0; k < fold; ++k) {
+        if (c->mesh.moving())
+            if ((r = add_remove_blocks(c))) return r;
+        if (c->stage_counter + per_step >= 0xffff) {
+            if ((r = check_status(c))) return r;
+            if ((r = reset_status(c, true))) return r;
+        }
+        if ((r = rk_step(c, dt))) return r;
+    }
+    return check_status(c);
+}
+
+int knc_set_precision(knc_ctx* c, int32_t precision) {
+    if (!c) return KNC_ERR_INVALID_ARGUMENT;
+    if (precision != KNC_PRECISION_FP64 && precision != KNC_PRECISION_MIXED)
+        return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "unknown precision %d", precision);
+    c->precision = precision;
+    return KNC_OK;
+}
+
+int knc_set_c2p_guess(knc_ctx* c, int32_t guess, const float* w, size_t n) {
+    if (!c) return KNC_ERR_INVALID_ARGUMENT;
+    if (guess == KNC_GUESS_PLAIN) {
+        c->guess = guess;
+        return KNC_OK;
+    }
+    if (guess != KNC_GUESS_MLP || !w || n != (size_t)KNC_MLP_NUM_PARAMS)
+        return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "MLP guess needs %d weights", KNC_MLP_NUM_PARAMS);
+    if (!c->d_mlp) CK(dalloc(&c->d_mlp, (size_t)KNC_MLP_NUM_PARAMS));
+    CK(cudaMemcpyAsync(c->d_mlp, w, n * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->guess = guess;
+    return KNC_OK;
+}
+
+int knc_set_batched(knc_ctx* c, int32_t graph) {
+    if (!c) return KNC_ERR_INVALID_ARGUMENT;
+    c->batched = graph ? 1 : 0;
+    return KNC_OK;
+}
+
+int knc_set_mixed_w_split(knc_ctx* c, double w_split) {
+    if (!c || !(w_split >= 1.0)) return KNC_ERR_INVALID_ARGUMENT;
+    c->w_split = w_split;
+    return KNC_OK;
+}
+
+int knc_synchronize(knc_ctx* c) {
+    if (!c) return KNC_ERR_INVALID_ARGUMENT;
+    CK(cudaStreamSynchronize(c->stream));
+    return KNC_OK;
+}
+
+int knc_c2p_stats(knc_ctx* c, int64_t* zones, int64_t* it64, int64_t* it32, int64_t* fb) {
+    if (!c) return KNC_ERR_INVALID_ARGUMENT;
+    DevStatus s;
+    CK(cudaMemcpyAsync(&s, c->d_status, sizeof(s), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (zones) *zones = (int64_t)s.c2p_zones;
+    if (it64) *it64 = (int64_t)s.iters_fp64;
+    if (it32) *it32 = (int64_t)s.iters_fp32;
+    if (fb) *fb = (int64_t)s.fallbacks;
+    return KNC_OK;
+}
+
+int knc_reset_c2p_stats(knc_ctx* c) {
+    if (!c) return KNC_ERR_INVALID_ARGUMENT;
+    return reset_status(c, false);
+}
+
+int knc_launch_count(const knc_ctx* c, int64_t* launches) {
+    if (!c || !launches) return KNC_ERR_INVALID_ARGUMENT;
+    *launches = c->launches;
+    return KNC_OK;
+}
+
+}  // extern "C"

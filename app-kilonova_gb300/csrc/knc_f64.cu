@@ -1,0 +1,254 @@
+// knc_f64.cu — the plain FP64 stage (compiled with --fmad=false).
+//
+// Kernels of one RK stage on the reference's method in FP64:
+//   c2p_f64     BlockState::try_to_primitive + scalar density for every zone
+//               (src/state.rs:76-94, src/scheme.rs:32-39); also the adaptive
+//               time-step reduction of State::time_step (src/state.rs:151-160)
+//   ghost       the two ghost blocks' halo rows from the model at the stage
+//               time (src/scheme.rs:45-52 via BlockState::from_model)
+//   update      flux / source / update / RK average (knc_stage.cuh)
+//   init        State::from_model (src/state.rs:55-69, 107-115)
+// Without FMA contraction every expression rounds exactly like the CPU
+// oracle's, so this path reproduces the reference arithmetic bit for bit
+// wherever the libm-free operations (+ - * / sqrt) are all that is used.
+#include "knc_internal.h"
+#include "knc_models.cuh"
+#include "knc_physics.cuh"
+#include "knc_stage.cuh"
+
+namespace knc {
+
+// ---- c2p -------------------------------------------------------------------
+__global__ void __launch_bounds__(TILE_THREADS) c2p_f64_kernel(StageArgs a) {
+    const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
+    if (ek != NO_ERROR && (uint32_t)(ek >> 48) < (uint32_t)a.stage) return;
+    const int4 t = a.tiles[blockIdx.x];
+    const DevBlock& B = a.blocks[t.x];
+    const int i = t.y + threadIdx.x / TILE_Q;
+    const int j = t.z + threadIdx.x % TILE_Q;
+    const int nr = B.nr, nq = B.nq;
+    const bool active = i < nr && j < nq;
+    int iters = 0;
+    double dtz = 1.7976931348623157e308;
+    if (active) {
+        const int64_t n = (int64_t)nr * nq;
+        const int64_t z = (int64_t)i * nq + j;
+        const double* U = B.buf[a.sel_in];
+        const double dV = B.dv[z];
+        double u[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) u[q] = U[q * n + z] / dV;
+        const double smass = U[4 * n + z];
+        double P[4] = {0.0, 0.0, 0.0, 0.0};
+        double bad = 0.0;
+        int kind;
+        if (a.srhd) kind = srhd_c2p_newton(a.gm, u, 0.0, P, iters, bad);
+        else kind = newt_c2p(a.gm - 1.0, u, P, bad);
+        if (kind != HYDRO_NONE && kind != HYDRO_NEGATIVE_PRESSURE) {
+            atomicMin(&a.status->err_key, error_key(a.stage, t.x, i, j, kind));
+            a.status->err_sel = a.sel_in;
+        }
+        const double w = a.srhd ? sqrt(1.0 + P[1] * P[1] + P[2] * P[2]) : 1.0;
+        double v[NFIELD] = {P[0], P[1], P[2], P[3], smass / dV / w};
+        store_prim<double>(B, i, j, v);
+        if (a.compute_dt) {
+            PhysT<double> ph;
+            ph.srhd = a.srhd;
+            ph.hllc = a.hllc;
+            ph.gm = a.gm;
+            ph.gm1 = a.gm - 1.0;
+            ph.gh = a.gm / ph.gm1;
+            ph.theta = a.plm_theta;
+            const double dr = B.rv[i + 1] - B.rv[i];
+            const double dq = B.qv[j + 1] - B.qv[j];
+            const double dl = fmin(dr, dq * B.rv[i]);
+            const double amax = max_signal_speed(ph, P) * a.cflux;
+            dtz = dl / amax;
+        }
+    }
+    warp_reduce_stats(a.status, active ? 1ull : 0ull, (unsigned long long)iters, 0ull, 0ull, dtz,
+                      a.compute_dt != 0);
+}
+
+// ---- ghost rows --------------------------------------------------------------
+// blockIdx.y = 0: inner ghost block (min index - 1), its last two rows feed
+// the innermost block's rows 0, 1; blockIdx.y = 1: outer ghost block, its
+// first two rows feed the outermost block's rows nr+2, nr+3.
+__global__ void ghost_kernel(GhostArgs a) {
+    const int end = blockIdx.y;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= 2 * a.nq || a.P[end] == nullptr) return;
+    const int row = k / a.nq, j = k - row * a.nq;
+    const double r = a.rc[end * 2 + row];
+    const double q = a.qc[j];
+    const double dV = a.dv[(end * 2 + row) * a.nq + j];
+    double Pm[4];
+    double scalar;
+    if (a.host_prim) {
+        const double* hp = a.host_prim + (((int64_t)end * 2 + row) * a.nq + j) * 5;
+        Pm[0] = hp[0];
+        Pm[1] = hp[1];
+        Pm[2] = hp[2];
+        Pm[3] = hp[3];
+        scalar = hp[4];
+    } else {
+        model_eval(a.model, r, q, a.time, false, a.ghost_index[end], 0, j, Pm, scalar);
+    }
+    PhysT<double> ph;
+    ph.srhd = a.srhd;
+    ph.hllc = 0;
+    ph.gm = a.gm;
+    ph.gm1 = a.gm - 1.0;
+    ph.gh = a.gm / ph.gm1;
+    ph.theta = 1.0;
+    double U[4];
+    prim_to_cons(ph, Pm, U);
+    double Uv[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) Uv[c] = U[c] * dV;       // from_model: U dV
+    const double smass = Uv[0] * scalar;                  // lab_frame_mass * scalar
+    double u[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) u[c] = Uv[c] / dV;       // try_to_primitive: U / dV
+    double P[4] = {0.0, 0.0, 0.0, 0.0};
+    double bad = 0.0;
+    int iters = 0, kind;
+    if (a.srhd) kind = srhd_c2p_newton(a.gm, u, 0.0, P, iters, bad);
+    else kind = newt_c2p(a.gm - 1.0, u, P, bad);
+    if (kind != HYDRO_NONE && kind != HYDRO_NEGATIVE_PRESSURE) {
+        atomicMin(&a.status->err_key, error_key(a.stage, 0x3ffeu + end, row, j, kind));
+    }
+    const double w = a.srhd ? sqrt(1.0 + P[1] * P[1] + P[2] * P[2]) : 1.0;
+    const double v[NFIELD] = {P[0], P[1], P[2], P[3], smass / dV / w};
+    const int nrt = a.nr_t[end];
+    const int64_t pn = (int64_t)(nrt + 4) * a.nq;
+    const int64_t off = (int64_t)(a.row0[end] + row) * a.nq + j;
+    if (a.single_precision) {
+        float* Pd = reinterpret_cast<float*>(a.P[end]);
+#pragma unroll
+        for (int c = 0; c < NFIELD; ++c) Pd[c * pn + off] = (float)v[c];
+    } else {
+        double* Pd = reinterpret_cast<double*>(a.P[end]);
+#pragma unroll
+        for (int c = 0; c < NFIELD; ++c) Pd[c * pn + off] = v[c];
+    }
+}
+
+// ---- initial data -------------------------------------------------------------
+__global__ void __launch_bounds__(TILE_THREADS) init_kernel(InitArgs a) {
+    const int4 t = a.tiles[blockIdx.x];
+    const DevBlock& B = a.blocks[t.x];
+    const int i = t.y + threadIdx.x / TILE_Q;
+    const int j = t.z + threadIdx.x % TILE_Q;
+    const int nr = B.nr, nq = B.nq;
+    if (i >= nr || j >= nq) return;
+    const int64_t n = (int64_t)nr * nq;
+    const int64_t z = (int64_t)i * nq + j;
+    double Pm[4];
+    double scalar;
+    if (a.host_prim) {
+        // host-model values, one row of 5 per zone, blocks in slot order
+        const double* hp = a.host_prim + ((int64_t)t.w + z) * 5;
+        Pm[0] = hp[0];
+        Pm[1] = hp[1];
+        Pm[2] = hp[2];
+        Pm[3] = hp[3];
+        scalar = hp[4];
+    } else {
+        model_eval(a.model, B.rc[i], B.qc[j], a.time, true, B.index, i, j, Pm, scalar);
+    }
+    PhysT<double> ph;
+    ph.srhd = a.srhd;
+    ph.hllc = 0;
+    ph.gm = a.gm;
+    ph.gm1 = a.gm - 1.0;
+    ph.gh = a.gm / ph.gm1;
+    ph.theta = 1.0;
+    double U[4];
+    prim_to_cons(ph, Pm, U);
+    const double dV = B.dv[z];
+    double* out = B.buf[a.sel];
+    double d0 = 0.0;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const double v = U[c] * dV;
+        out[c * n + z] = v;
+        if (c == 0) d0 = v;
+    }
+    out[4 * n + z] = d0 * scalar;
+}
+
+// ---- layout transposes ---------------------------------------------------------
+__global__ void aos_to_soa_kernel(const double* __restrict__ aos, const double* __restrict__ scalar,
+                                  double* __restrict__ soa, int64_t n) {
+    const int64_t z = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (z >= n) return;
+    const double4 v = reinterpret_cast<const double4*>(aos)[z];
+    soa[z] = v.x;
+    soa[n + z] = v.y;
+    soa[2 * n + z] = v.z;
+    soa[3 * n + z] = v.w;
+    soa[4 * n + z] = scalar[z];
+}
+
+__global__ void soa_to_aos_kernel(const double* __restrict__ soa, double* __restrict__ aos,
+                                  double* __restrict__ scalar, int64_t n) {
+    const int64_t z = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (z >= n) return;
+    double4 v;
+    v.x = soa[z];
+    v.y = soa[n + z];
+    v.z = soa[2 * n + z];
+    v.w = soa[3 * n + z];
+    reinterpret_cast<double4*>(aos)[z] = v;
+    scalar[z] = soa[4 * n + z];
+}
+
+// ---- launchers ---------------------------------------------------------------
+cudaError_t launch_c2p_f64(const StageArgs& a, cudaStream_t s) {
+    if (a.ntiles <= 0) return cudaSuccess;
+    c2p_f64_kernel<<<a.ntiles, TILE_THREADS, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_update_f64(const StageArgs& a, cudaStream_t s) {
+    if (a.ntiles <= 0) return cudaSuccess;
+    static bool configured = false;
+    const size_t bytes = StageSmem<double>::bytes;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(update_kernel<double, false>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    update_kernel<double, false><<<a.ntiles, TILE_THREADS, bytes, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ghost(const GhostArgs& a, cudaStream_t s) {
+    dim3 grid((2 * a.nq + 127) / 128, 2);
+    ghost_kernel<<<grid, 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_init_f64(const InitArgs& a, int ntiles, cudaStream_t s) {
+    if (ntiles <= 0) return cudaSuccess;
+    init_kernel<<<ntiles, TILE_THREADS, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_aos_to_soa(const double* aos, const double* scalar, double* soa, int64_t nr, int64_t nq,
+                              cudaStream_t s) {
+    const int64_t n = nr * nq;
+    aos_to_soa_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(aos, scalar, soa, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_soa_to_aos(const double* soa, double* aos, double* scalar, int64_t nr, int64_t nq,
+                              cudaStream_t s) {
+    const int64_t n = nr * nq;
+    soa_to_aos_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(soa, aos, scalar, n);
+    return cudaGetLastError();
+}
+
+}  // namespace knc

@@ -1,0 +1,147 @@
+// knc_internal.h — device data layout and kernel launchers shared by the
+// host runtime (knc_api.cu) and the kernel translation units.
+//
+// HBM layout, per radial block (BlockIndex (i, 0), src/mesh.rs:12):
+//   state   buf[2]  double [5][nr][nq]     D, S_r, S_theta, tau, scalar mass
+//                                           (volume-integrated, theta fastest)
+//   prims   P       [5][nr+4][nq]          rho, u_r, u_theta, p, s (double in the
+//                                           FP64 path, float in the mixed path);
+//                                           rows 0-1 and nr+2..nr+3 hold the radial
+//                                           halo (neighbour rows or ghost rows)
+//   geometry ar [nr+1][nq], aq [nr][nq+1], dv [nr][nq] (FP64, mesh.rs formulas),
+//            rc [nr] centroid radii, rv [nr+1] vertices; per-column tables
+//            qv [nq+1], qc [nq], cot [nq]; FP32 row/column factors for the
+//            mixed path (areas and volumes separate into r- and theta-parts).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/knc.h"
+
+namespace knc {
+
+constexpr int TILE_R = 8;      // stage tile: rows (radial)
+constexpr int TILE_Q = 32;     // stage tile: columns (polar), one warp wide
+constexpr int TILE_THREADS = TILE_R * TILE_Q;
+constexpr int NFIELD = 5;
+
+struct DevBlock {
+    double* buf[2];        // [5][nr][nq] state ping/pong
+    void* P;               // [5][nr+4][nq] primitives with halo rows
+    const double* ar;      // [nr+1][nq]
+    const double* aq;      // [nr][nq+1]
+    const double* dv;      // [nr][nq]
+    const double* rc;      // [nr]
+    const double* rv;      // [nr+1]
+    const double* qv;      // [nq+1]
+    const double* qc;      // [nq]
+    const double* cot;     // [nq]
+    // mixed path geometry factors (FP32):
+    //   A_r(i,j) = ar_r[i] * ar_q[j]      ar_r = r_i^2,  ar_q = pi (s0+s1) |chord|
+    //   A_q(i,j) = aq_r[i] * aq_q[j]      aq_r = pi (r1^2 - r0^2), aq_q = sin(theta_j)
+    //   dV(i,j)  = dv_r[i] * dv_q[j]      dv_r = (r1^3 - r0^3) 2 pi / 3, dv_q = cos0 - cos1
+    const float* ar_r;     // [nr+1]
+    const float* ar_q;     // [nq]
+    const float* aq_r;     // [nr]
+    const float* aq_q;     // [nq+1]
+    const float* dv_r;     // [nr]
+    const float* dv_q;     // [nq]
+    const float* rc32;     // [nr]
+    const float* cot32;    // [nq]
+    void* P_in_nbr;        // inner neighbour's P: my rows 0,1 go to its rows nr'+2, nr'+3
+    void* P_out_nbr;       // outer neighbour's P: my rows nr-2, nr-1 go to its rows 0, 1
+    int32_t nr, nq;
+    int32_t index;         // block index i of BlockIndex (i, 0)
+    int32_t nr_in_nbr;     // rows of the inner neighbour
+    int32_t nr_out_nbr;    // rows of the outer neighbour
+    int32_t pad_;
+};
+
+// Error key: lexicographic (stage, slot, i, j) with the hydro kind in the low
+// bits; atomicMin keeps the first failure in that order.
+__host__ __device__ inline unsigned long long error_key(uint32_t stage, uint32_t slot, uint32_t i,
+                                                       uint32_t j, uint32_t kind) {
+    return ((unsigned long long)(stage & 0xffffu) << 48) | ((unsigned long long)(slot & 0x3fffu) << 34) |
+           ((unsigned long long)(i & 0x3fffu) << 20) | ((unsigned long long)(j & 0xffffu) << 4) |
+           (unsigned long long)(kind & 0xfu);
+}
+constexpr unsigned long long NO_ERROR = ~0ull;
+
+struct DevStatus {
+    unsigned long long err_key;     // NO_ERROR or error_key(...)
+    int32_t err_sel;                // state buffer the failing stage read
+    int32_t pad;
+    unsigned long long c2p_zones;
+    unsigned long long iters_fp64;
+    unsigned long long iters_fp32;
+    unsigned long long fallbacks;
+    unsigned long long dt_bits;     // min of dl/a over zones (double bits, positive)
+};
+
+struct StageArgs {
+    const DevBlock* blocks;
+    const int4* tiles;      // {slot, i0, j0, 0}
+    int32_t ntiles;
+    int32_t stage;          // stage counter for error ordering
+    int32_t sel_in, sel_out, sel_base;   // state buffer selectors; sel_base < 0: no average
+    int32_t srhd, hllc;
+    int32_t one_dimensional;
+    int32_t guess;          // KNC_GUESS_*
+    int32_t compute_dt;     // c2p pass also reduces dl / a_max
+    double gm, plm_theta;
+    double dt;
+    double w1, bf;          // out = (U + dU) w1 + U0 bf when sel_base >= 0
+    double cflux;           // LIGHT_SPEED (SRHD) or 1
+    double w_split;         // mixed path: Lorentz factor above which c2p runs in FP64
+    const float* mlp;       // packed MLP weights (device) or null
+    DevStatus* status;
+};
+
+struct GhostArgs {
+    void* P[2];             // target P of the innermost / outermost block
+    int32_t row0[2];        // first target row (0 for inner, nr+2 for outer)
+    int32_t nr_t[2];        // target block rows (row stride nr+4)
+    int32_t nq;
+    int32_t ghost_index[2];
+    const double* rc;       // [2 ends][2 rows]
+    const double* dv;       // [2 ends][2 rows][nq]
+    const double* qc;       // [nq]
+    const double* host_prim;// [2][2][nq][5] model values from a host callback, or null
+    knc_model_params model;
+    double time;
+    int32_t srhd;
+    int32_t stage;
+    double gm;
+    int32_t single_precision;   // write float P
+    DevStatus* status;
+};
+
+struct InitArgs {
+    const DevBlock* blocks;
+    const int4* tiles;
+    int32_t sel;
+    int32_t srhd;
+    double gm;
+    double time;
+    knc_model_params model;
+    const double* host_prim;     // [nzones][5] host model values (HOST model) or null
+};
+
+// ---- launchers (each returns the cudaError_t of the launch) -------------
+cudaError_t launch_init_f64(const InitArgs& a, int ntiles, cudaStream_t s);
+cudaError_t launch_c2p_f64(const StageArgs& a, cudaStream_t s);
+cudaError_t launch_update_f64(const StageArgs& a, cudaStream_t s);
+cudaError_t launch_ghost(const GhostArgs& a, cudaStream_t s);
+cudaError_t launch_c2p_mixed(const StageArgs& a, cudaStream_t s);
+cudaError_t launch_update_mixed(const StageArgs& a, cudaStream_t s);
+cudaError_t launch_aos_to_soa(const double* aos, const double* scalar, double* soa, int64_t nr, int64_t nq,
+                              cudaStream_t s);
+cudaError_t launch_soa_to_aos(const double* soa, double* aos, double* scalar, int64_t nr, int64_t nq,
+                              cudaStream_t s);
+cudaError_t launch_sample_pairs(const DevBlock* blocks, int nblocks, int sel, int stride, double gm,
+                                double* out, int64_t capacity, unsigned long long* counter, cudaStream_t s);
+cudaError_t launch_generate_pairs(double gm, double w_lo, double w_hi, double t_lo, double t_hi,
+                                  uint64_t seed, int64_t n, double* out, cudaStream_t s);
+
+}  // namespace knc

@@ -1,0 +1,388 @@
+// knc_physics.cuh — per-zone physics of the finite-volume stage, on the device.
+//
+// Replaces the arithmetic the reference reaches through its Hydrodynamics
+// trait (src/traits.rs:41-136): the adapters src/physics/relativistic_hydro.rs
+// and src/physics/newtonian_hydro.rs and, behind them, the git crates
+// hydro-srhd (srhd_2d: prim<->cons, riemann_hllc_scalar, sources, c2p),
+// hydro-euler (euler_2d) and godunov-core (piecewise_linear::plm_gradient).
+//
+// Methods: SRHD prim/cons/flux and characteristic speeds after Marti & Mueller
+// (Living Rev. Relativ. 2003), Newton pressure recovery after the same review
+// (section 6), HLLE (Harten-Lax-van Leer with Einfeldt speeds), relativistic
+// HLLC (Mignone & Bodo 2005), Newtonian HLLC (Toro ch. 10), generalised-minmod
+// slopes (van Leer 1979), spherical-polar geometric sources.
+//
+// Templated on the arithmetic type. For `double` every expression keeps one
+// fixed evaluation order; the FP64 translation unit is compiled without FMA
+// contraction so these produce the same bits as the CPU oracle.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace knc {
+
+constexpr double LIGHT_SPEED = 3e10;                   // src/physics/mod.rs:7
+constexpr double PI = 3.14159265358979323846;
+constexpr int NEWTON_ITER_MAX = 50;
+constexpr double NEWTON_TOLERANCE = 1e-12;
+constexpr double PRESSURE_FLOOR = 1e-3;                // relativistic_hydro.rs:79-81
+
+enum : int {
+    HYDRO_NONE = 0,
+    HYDRO_NEGATIVE_DENSITY = 1,
+    HYDRO_NEGATIVE_PRESSURE = 2,
+    HYDRO_NEGATIVE_ENERGY_DENSITY = 3,
+    HYDRO_ROOT_FINDER_FAILED = 4
+};
+
+template <class R>
+struct PhysT {
+    int srhd;      // 1 relativistic, 0 Newtonian
+    int hllc;      // 1 HLLC, 0 HLLE
+    R gm;          // gamma_law_index
+    R gh;          // gm / (gm - 1)
+    R gm1;         // gm - 1
+    R theta;       // plm_theta
+};
+
+template <class R> __device__ __forceinline__ R rmin(R a, R b) { return a < b ? a : b; }
+template <class R> __device__ __forceinline__ R rmax(R a, R b) { return a > b ? a : b; }
+__device__ __forceinline__ double rsqrt_(double x) { return sqrt(x); }
+__device__ __forceinline__ float rsqrt_(float x) { return sqrtf(x); }
+__device__ __forceinline__ double rabs(double x) { return fabs(x); }
+__device__ __forceinline__ float rabs(float x) { return fabsf(x); }
+
+// godunov_core::piecewise_linear::plm_gradient: generalised minmod of
+// theta (b - a), (c - a) / 2, theta (c - b).
+template <class R>
+__device__ __forceinline__ R plm_gradient(R theta, R a, R b, R c) {
+    const R x = theta * (b - a);
+    const R y = R(0.5) * (c - a);
+    const R z = theta * (c - b);
+    if (x > R(0) && y > R(0) && z > R(0)) return rmin(x, rmin(y, z));
+    if (x < R(0) && y < R(0) && z < R(0)) return rmax(x, rmax(y, z));
+    return R(0);
+}
+
+// One side of an interface: conserved state, normal flux, outer wave speeds,
+// the passive scalar's conserved density (s W) and flux (s u_n).
+template <class R>
+struct Side {
+    R U[4], F[4];
+    R lm, lp, sU, sF, vn, pre;
+};
+
+template <class R>
+__device__ __forceinline__ void srhd_side(const PhysT<R>& ph, R rho, R ur, R uq, R pre, R s, int axis,
+                                          Side<R>& S) {
+    const R uu = ur * ur + uq * uq;
+    const R w2 = R(1) + uu;
+    const R w = rsqrt_(w2);
+    const R h = R(1) + pre / rho * ph.gh;
+    const R d = rho * w;
+    const R m = d * h;
+    const R un = axis == 0 ? ur : uq;
+    const R vn = un / w;
+    S.U[0] = d;
+    S.U[1] = m * ur;
+    S.U[2] = m * uq;
+    S.U[3] = m * w - pre - d;
+    S.F[0] = S.U[0] * vn;
+    S.F[1] = axis == 0 ? S.U[1] * vn + pre : S.U[1] * vn;
+    S.F[2] = axis == 1 ? S.U[2] * vn + pre : S.U[2] * vn;
+    S.F[3] = (S.U[3] + pre) * vn;
+    const R cs2 = ph.gm * pre / (rho * h);
+    const R v2 = uu / w2;
+    const R k = R(1) - cs2;
+    const R a = vn * k;
+    const R b = rsqrt_(cs2 * (R(1) - v2) * (R(1) - v2 * cs2 - vn * vn * k));
+    const R inv = R(1) / (R(1) - v2 * cs2);
+    S.lm = (a - b) * inv;
+    S.lp = (a + b) * inv;
+    S.sU = s * w;
+    S.sF = s * un;
+    S.vn = vn;
+    S.pre = pre;
+}
+
+template <class R>
+__device__ __forceinline__ void newt_side(const PhysT<R>& ph, R rho, R vr, R vq, R pre, R s, int axis,
+                                          Side<R>& S) {
+    const R vn = axis == 0 ? vr : vq;
+    S.U[0] = rho;
+    S.U[1] = rho * vr;
+    S.U[2] = rho * vq;
+    S.U[3] = pre / ph.gm1 + R(0.5) * rho * (vr * vr + vq * vq);
+    S.F[0] = S.U[0] * vn;
+    S.F[1] = axis == 0 ? S.U[1] * vn + pre : S.U[1] * vn;
+    S.F[2] = axis == 1 ? S.U[2] * vn + pre : S.U[2] * vn;
+    S.F[3] = (S.U[3] + pre) * vn;
+    const R cs = rsqrt_(ph.gm * pre / rho);
+    S.lm = vn - cs;
+    S.lp = vn + cs;
+    S.sU = s;
+    S.sF = s * vn;
+    S.vn = vn;
+    S.pre = pre;
+}
+
+template <class R>
+__device__ __forceinline__ void make_side(const PhysT<R>& ph, const R* P, R s, int axis, Side<R>& S) {
+    if (ph.srhd) srhd_side(ph, P[0], P[1], P[2], P[3], s, axis, S);
+    else newt_side(ph, P[0], P[1], P[2], P[3], s, axis, S);
+}
+
+template <class R>
+__device__ __forceinline__ void hlle(const Side<R>& L, const Side<R>& Rr, R out[5]) {
+    const R am = rmin(L.lm, Rr.lm);
+    const R ap = rmax(L.lp, Rr.lp);
+    if (am >= R(0)) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) out[q] = L.F[q];
+        out[4] = L.sF;
+    } else if (ap <= R(0)) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) out[q] = Rr.F[q];
+        out[4] = Rr.sF;
+    } else {
+        const R inv = R(1) / (ap - am);
+        const R apam = ap * am;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            out[q] = (ap * L.F[q] - am * Rr.F[q] + apam * (Rr.U[q] - L.U[q])) * inv;
+        out[4] = (ap * L.sF - am * Rr.sF + apam * (Rr.sU - L.sU)) * inv;
+    }
+}
+
+// Relativistic HLLC, Mignone & Bodo (2005): contact speed from the HLL state
+// in the cancellation-free root form, star states with E = tau + D.
+template <class R>
+__device__ __forceinline__ void srhd_hllc(const Side<R>& L, const Side<R>& Rr, int axis, R out[5]) {
+    const R am = rmin(L.lm, Rr.lm);
+    const R ap = rmax(L.lp, Rr.lp);
+    if (am >= R(0)) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) out[q] = L.F[q];
+        out[4] = L.sF;
+        return;
+    }
+    if (ap <= R(0)) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) out[q] = Rr.F[q];
+        out[4] = Rr.sF;
+        return;
+    }
+    const int n = axis == 0 ? 1 : 2;
+    const int t = axis == 0 ? 2 : 1;
+    const R inv = R(1) / (ap - am);
+    const R apam = ap * am;
+    R Uh[4], Fh[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        Uh[q] = (ap * Rr.U[q] - am * L.U[q] - (Rr.F[q] - L.F[q])) * inv;
+        Fh[q] = (ap * L.F[q] - am * Rr.F[q] + apam * (Rr.U[q] - L.U[q])) * inv;
+    }
+    const R e_hll = Uh[3] + Uh[0];
+    const R fe_hll = Fh[3] + Fh[0];
+    const R m_hll = Uh[n];
+    const R fm_hll = Fh[n];
+    const R bq = e_hll + fm_hll;
+    const R disc = rmax(bq * bq - R(4) * fe_hll * m_hll, R(0));
+    const R lstar = R(2) * m_hll / (bq + rsqrt_(disc));
+    const R pstar = fm_hll - fe_hll * lstar;
+    const bool left = lstar >= R(0);
+    const Side<R>& K = left ? L : Rr;
+    const R lam = left ? am : ap;
+    const R fac = R(1) / (lam - lstar);
+    const R lv = lam - K.vn;
+    const R e_k = K.U[3] + K.U[0];
+    R Us[4];
+    Us[0] = K.U[0] * lv * fac;
+    Us[n] = (K.U[n] * lv + pstar - K.pre) * fac;
+    Us[t] = K.U[t] * lv * fac;
+    const R e_s = (e_k * lv + pstar * lstar - K.pre * K.vn) * fac;
+    Us[3] = e_s - Us[0];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) out[q] = K.F[q] + lam * (Us[q] - K.U[q]);
+    const R s_star = K.sU * lv * fac;
+    out[4] = K.sF + lam * (s_star - K.sU);
+}
+
+// Newtonian HLLC (Toro 3rd ed. section 10.4, contact speed eq. 10.37).
+template <class R>
+__device__ __forceinline__ void newt_hllc(const Side<R>& L, const Side<R>& Rr, int axis, R out[5]) {
+    const R am = rmin(L.lm, Rr.lm);
+    const R ap = rmax(L.lp, Rr.lp);
+    if (am >= R(0)) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) out[q] = L.F[q];
+        out[4] = L.sF;
+        return;
+    }
+    if (ap <= R(0)) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) out[q] = Rr.F[q];
+        out[4] = Rr.sF;
+        return;
+    }
+    const int n = axis == 0 ? 1 : 2;
+    const int t = axis == 0 ? 2 : 1;
+    const R ql = L.U[0] * (am - L.vn);
+    const R qr = Rr.U[0] * (ap - Rr.vn);
+    const R sstar = (Rr.pre - L.pre + L.U[n] * (am - L.vn) - Rr.U[n] * (ap - Rr.vn)) / (ql - qr);
+    const bool left = sstar >= R(0);
+    const Side<R>& K = left ? L : Rr;
+    const R lam = left ? am : ap;
+    const R rho = K.U[0];
+    const R lv = lam - K.vn;
+    const R fac = rho * lv / (lam - sstar);
+    R Us[4];
+    Us[0] = fac;
+    Us[n] = fac * sstar;
+    Us[t] = fac * (K.U[t] / rho);
+    Us[3] = fac * (K.U[3] / rho + (sstar - K.vn) * (sstar + K.pre / (rho * lv)));
+#pragma unroll
+    for (int q = 0; q < 4; ++q) out[q] = K.F[q] + lam * (Us[q] - K.U[q]);
+    const R s_star = K.sU * lv / (lam - sstar);
+    out[4] = K.sF + lam * (s_star - K.sU);
+}
+
+template <class R>
+__device__ __forceinline__ void riemann(const PhysT<R>& ph, const R* pl, const R* pr, R sl, R sr,
+                                        int axis, R out[5]) {
+    Side<R> L, Rr;
+    make_side(ph, pl, sl, axis, L);
+    make_side(ph, pr, sr, axis, Rr);
+    if (ph.hllc) {
+        if (ph.srhd) srhd_hllc(L, Rr, axis, out);
+        else newt_hllc(L, Rr, axis, out);
+    } else {
+        hlle(L, Rr, out);
+    }
+}
+
+// Geometric sources per unit volume (before LIGHT_SPEED and dV).
+template <class R>
+__device__ __forceinline__ void sources(const PhysT<R>& ph, const R* P, R r, R cot, R S[4]) {
+    const R rho = P[0], ur = P[1], uq = P[2], pre = P[3];
+    const R mass = ph.srhd ? rho * (R(1) + pre / rho * ph.gh) : rho;
+    S[0] = R(0);
+    S[1] = (R(2) * pre + mass * uq * uq) / r;
+    S[2] = (pre * cot - mass * ur * uq) / r;
+    S[3] = R(0);
+}
+
+template <class R>
+__device__ __forceinline__ void prim_to_cons(const PhysT<R>& ph, const R* P, R* U) {
+    if (ph.srhd) {
+        const R rho = P[0], ur = P[1], uq = P[2], pre = P[3];
+        const R uu = ur * ur + uq * uq;
+        const R w = rsqrt_(R(1) + uu);
+        const R h = R(1) + pre / rho * ph.gh;
+        const R d = rho * w;
+        const R m = d * h;
+        U[0] = d;
+        U[1] = m * ur;
+        U[2] = m * uq;
+        U[3] = m * w - pre - d;
+    } else {
+        const R rho = P[0], vr = P[1], vq = P[2], pre = P[3];
+        U[0] = rho;
+        U[1] = rho * vr;
+        U[2] = rho * vq;
+        U[3] = pre / ph.gm1 + R(0.5) * rho * (vr * vr + vq * vq);
+    }
+}
+
+template <class R>
+__device__ __forceinline__ R lorentz_factor(const PhysT<R>& ph, const R* P) {
+    if (!ph.srhd) return R(1);
+    return rsqrt_(R(1) + P[1] * P[1] + P[2] * P[2]);
+}
+
+// SRHD cons -> prim in the reference's Newton form (FP64, plain path):
+// Newton-Raphson on p, |f| < 1e-12 (D + tau), at most 50 iterations.
+// Returns HYDRO_* and the iteration count.
+__device__ __forceinline__ int srhd_c2p_newton(double gm, const double* U, double guess, double* P,
+                                               int& iterations, double& bad) {
+    const double m = U[0];
+    const double tau = U[3];
+    iterations = 0;
+    if (m < 0.0) { bad = m; return HYDRO_NEGATIVE_DENSITY; }
+    if (tau < 0.0) { bad = tau; return HYDRO_NEGATIVE_ENERGY_DENSITY; }
+    const double ss = U[1] * U[1] + U[2] * U[2];
+    const double tol = NEWTON_TOLERANCE * (m + tau);
+    double p = guess;
+    double w0 = 1.0;
+    bool found = false;
+    for (int n = 0; n < NEWTON_ITER_MAX; ++n) {
+        const double et = tau + p + m;
+        const double b2 = fmin(ss / et / et, 1.0 - 1e-10);
+        const double w2 = 1.0 / (1.0 - b2);
+        const double w = sqrt(w2);
+        const double e = (tau + m * (1.0 - w) + p * (1.0 - w2)) / (m * w);
+        const double d = m / w;
+        const double h = 1.0 + e + p / d;
+        const double a2 = gm * p / (d * h);
+        const double f = d * e * (gm - 1.0) - p;
+        const double g = b2 * a2 - 1.0;
+        p -= f / g;
+        iterations = n + 1;
+        if (fabs(f) < tol) { w0 = w; found = true; break; }
+    }
+    if (!found) { bad = m; return HYDRO_ROOT_FINDER_FAILED; }
+    const double et = tau + m + p;
+    P[0] = m / w0;
+    P[1] = w0 * U[1] / et;
+    P[2] = w0 * U[2] / et;
+    P[3] = p;
+    if (p < 0.0) {
+        P[3] = PRESSURE_FLOOR * P[0];
+        return HYDRO_NEGATIVE_PRESSURE;
+    }
+    return HYDRO_NONE;
+}
+
+template <class R>
+__device__ __forceinline__ int newt_c2p(R gm1, const R* U, R* P, R& bad) {
+    const R rho = U[0];
+    if (rho < R(0)) { bad = rho; return HYDRO_NEGATIVE_DENSITY; }
+    const R vr = U[1] / rho;
+    const R vq = U[2] / rho;
+    P[0] = rho;
+    P[1] = vr;
+    P[2] = vq;
+    P[3] = (U[3] - R(0.5) * rho * (vr * vr + vq * vq)) * gm1;
+    return HYDRO_NONE;
+}
+
+// Max signal speed of a primitive state (time_step, state.rs:151-160).
+template <class R>
+__device__ __forceinline__ R max_signal_speed(const PhysT<R>& ph, const R* P) {
+    if (ph.srhd) {
+        Side<R> a, b;
+        srhd_side(ph, P[0], P[1], P[2], P[3], R(0), 0, a);
+        srhd_side(ph, P[0], P[1], P[2], P[3], R(0), 1, b);
+        return rmax(rmax(rabs(a.lm), rabs(a.lp)), rmax(rabs(b.lm), rabs(b.lp)));
+    }
+    const R v = rsqrt_(P[1] * P[1] + P[2] * P[2]);
+    return v + rsqrt_(ph.gm * P[3] / P[0]);
+}
+
+// Counter-based U[0,1): splitmix64 (Steele, Lea & Flood 2014) of (seed, block, i, j).
+__device__ __host__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+__device__ __host__ __forceinline__ double uniform01(uint64_t seed, int32_t block, int64_t i, int64_t j) {
+    uint64_t k = splitmix64(seed);
+    k = splitmix64(k ^ (uint64_t)(uint32_t)block);
+    k = splitmix64(k ^ (uint64_t)i);
+    k = splitmix64(k ^ (uint64_t)j);
+    return (double)(k >> 11) * (1.0 / 9007199254740992.0);
+}
+
+}  // namespace knc

@@ -1,0 +1,275 @@
+// knc_stage.cuh — the fused flux / source / update kernel of one RK stage.
+//
+// One CTA owns a TILE_R x TILE_Q tile of one block. It stages the tile's
+// primitives plus a 2-zone halo (radial halo rows are already present in the
+// padded P array; theta halo columns come from the same block) in shared
+// memory, then:
+//   1. PLM slopes in r for rows -1..TILE_R and in theta for columns -1..TILE_Q
+//      (zero slope on the first and last column of the block,
+//      src/scheme.rs:107-110 via ndarray_ops::extend_default_2d);
+//   2. one Riemann solve per face of the tile, scaled by c (SRHD) and the face
+//      area (src/scheme.rs:90-97, 121-128; zero flux through the poles);
+//   3. per zone: geometric source x dV, dU = (S - dF_r - dF_q) dt,
+//      U1 = U + dU (src/scheme.rs:130-157), and the RK average
+//      (1 - b) U1 + b U0 fused in (src/state.rs:179-212).
+// Every face flux is computed once per tile; a zone's state is read once and
+// written once, so the output may alias the input or the RK base buffer.
+#pragma once
+
+#include "knc_internal.h"
+#include "knc_physics.cuh"
+
+namespace knc {
+
+template <class R>
+struct StageSmem {
+    static constexpr int TR = TILE_R, TQ = TILE_Q;
+    static constexpr int PR = TR + 4, PQ = TQ + 4;
+    static constexpr int NP = NFIELD * PR * PQ;
+    static constexpr int NGR = NFIELD * (TR + 2) * TQ;
+    static constexpr int NGQ = NFIELD * TR * (TQ + 2);
+    static constexpr int NFR = NFIELD * (TR + 1) * TQ;
+    static constexpr int NFQ = NFIELD * TR * (TQ + 1);
+    static constexpr size_t bytes = sizeof(R) * (size_t)(NP + NGR + NGQ + NFR + NFQ);
+};
+
+template <class R>
+__device__ __forceinline__ PhysT<R> make_phys(const StageArgs& a) {
+    PhysT<R> ph;
+    ph.srhd = a.srhd;
+    ph.hllc = a.hllc;
+    const double gm1 = a.gm - 1.0;
+    ph.gm = (R)a.gm;
+    ph.gm1 = (R)gm1;
+    ph.gh = (R)(a.gm / gm1);
+    ph.theta = (R)a.plm_theta;
+    return ph;
+}
+
+template <class R, bool MIXED>
+__global__ void __launch_bounds__(TILE_THREADS) update_kernel(StageArgs a) {
+    using S = StageSmem<R>;
+    constexpr int TR = S::TR, TQ = S::TQ, PR = S::PR, PQ = S::PQ;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* sP = reinterpret_cast<R*>(smem_raw);
+    R* sGr = sP + S::NP;
+    R* sGq = sGr + S::NGR;
+    R* sFr = sGq + S::NGQ;
+    R* sFq = sFr + S::NFR;
+
+    // A failed c2p in this or an earlier stage stops the step: keep the
+    // input state untouched so the failure can be reported from it.
+    if (*(volatile unsigned long long*)&a.status->err_key != NO_ERROR) return;
+
+    const int4 t = a.tiles[blockIdx.x];
+    const DevBlock& B = a.blocks[t.x];
+    const int nr = B.nr, nq = B.nq, i0 = t.y, j0 = t.z;
+    const int tid = threadIdx.x;
+    const R* P = reinterpret_cast<const R*>(B.P);
+    const int64_t pn = (int64_t)(nr + 4) * nq;
+    const bool one_d = a.one_dimensional != 0;
+
+    // ---- stage primitives (tile rows -2..TR+1 = padded rows i0..i0+TR+3)
+    for (int k = tid; k < PR * PQ; k += TILE_THREADS) {
+        const int rr = k / PQ, cc = k - rr * PQ;
+        const int prow = i0 + rr;
+        const int j = j0 - 2 + cc;
+        const bool ok = prow < nr + 4 && j >= 0 && j < nq;
+        const int64_t off = (int64_t)prow * nq + j;
+#pragma unroll
+        for (int q = 0; q < NFIELD; ++q) sP[(q * PR + rr) * PQ + cc] = ok ? P[q * pn + off] : R(0);
+    }
+    __syncthreads();
+
+    const PhysT<R> ph = make_phys<R>(a);
+    const R th = ph.theta;
+
+    // ---- PLM slopes
+    for (int k = tid; k < (TR + 2) * TQ; k += TILE_THREADS) {
+        const int g = k / TQ, c = k - g * TQ;
+#pragma unroll
+        for (int q = 0; q < NFIELD; ++q) {
+            const R* col = sP + (q * PR) * PQ + c + 2;
+            sGr[(q * (TR + 2) + g) * TQ + c] = plm_gradient(th, col[g * PQ], col[(g + 1) * PQ], col[(g + 2) * PQ]);
+        }
+    }
+    if (!one_d) {
+        for (int k = tid; k < TR * (TQ + 2); k += TILE_THREADS) {
+            const int r = k / (TQ + 2), c = k - r * (TQ + 2);
+            const int j = j0 - 1 + c;
+            const bool edge = j <= 0 || j >= nq - 1;
+#pragma unroll
+            for (int q = 0; q < NFIELD; ++q) {
+                const R* row = sP + (q * PR + r + 2) * PQ + c;
+                sGq[(q * TR + r) * (TQ + 2) + c] = edge ? R(0) : plm_gradient(th, row[0], row[1], row[2]);
+            }
+        }
+    }
+    __syncthreads();
+
+    const R cflux = (R)a.cflux;
+
+    // ---- radial faces i0..i0+TR (face i between zone rows i-1 and i)
+    for (int k = tid; k < (TR + 1) * TQ; k += TILE_THREADS) {
+        const int f = k / TQ, c = k - f * TQ;
+        const int i = i0 + f, j = j0 + c;
+        R out[NFIELD] = {R(0), R(0), R(0), R(0), R(0)};
+        if (i <= nr && j < nq) {
+            R pl[4], pr[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                pl[q] = sP[(q * PR + f + 1) * PQ + c + 2] + sGr[(q * (TR + 2) + f) * TQ + c] * R(0.5);
+                pr[q] = sP[(q * PR + f + 2) * PQ + c + 2] - sGr[(q * (TR + 2) + f + 1) * TQ + c] * R(0.5);
+            }
+            const R sl = sP[(4 * PR + f + 1) * PQ + c + 2] + sGr[(4 * (TR + 2) + f) * TQ + c] * R(0.5);
+            const R sr = sP[(4 * PR + f + 2) * PQ + c + 2] - sGr[(4 * (TR + 2) + f + 1) * TQ + c] * R(0.5);
+            riemann(ph, pl, pr, sl, sr, 0, out);
+            R A;
+            if (MIXED) A = (R)(B.ar_r[i] * B.ar_q[j]);
+            else A = (R)B.ar[(int64_t)i * nq + j];
+#pragma unroll
+            for (int q = 0; q < NFIELD; ++q) out[q] = out[q] * cflux * A;
+        }
+#pragma unroll
+        for (int q = 0; q < NFIELD; ++q) sFr[(q * (TR + 1) + f) * TQ + c] = out[q];
+    }
+    // ---- polar faces j0..j0+TQ (face j between zone columns j-1 and j)
+    if (!one_d) {
+        for (int k = tid; k < TR * (TQ + 1); k += TILE_THREADS) {
+            const int r = k / (TQ + 1), c = k - r * (TQ + 1);
+            const int i = i0 + r, j = j0 + c;
+            R out[NFIELD] = {R(0), R(0), R(0), R(0), R(0)};
+            if (i < nr && j > 0 && j < nq) {
+                R pl[4], pr[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    pl[q] = sP[(q * PR + r + 2) * PQ + c + 1] + sGq[(q * TR + r) * (TQ + 2) + c] * R(0.5);
+                    pr[q] = sP[(q * PR + r + 2) * PQ + c + 2] - sGq[(q * TR + r) * (TQ + 2) + c + 1] * R(0.5);
+                }
+                const R sl = sP[(4 * PR + r + 2) * PQ + c + 1] + sGq[(4 * TR + r) * (TQ + 2) + c] * R(0.5);
+                const R sr = sP[(4 * PR + r + 2) * PQ + c + 2] - sGq[(4 * TR + r) * (TQ + 2) + c + 1] * R(0.5);
+                riemann(ph, pl, pr, sl, sr, 1, out);
+                R A;
+                if (MIXED) A = (R)(B.aq_r[i] * B.aq_q[j]);
+                else A = (R)B.aq[(int64_t)i * (nq + 1) + j];
+#pragma unroll
+                for (int q = 0; q < NFIELD; ++q) out[q] = out[q] * cflux * A;
+            }
+#pragma unroll
+            for (int q = 0; q < NFIELD; ++q) sFq[(q * TR + r) * (TQ + 1) + c] = out[q];
+        }
+    }
+    __syncthreads();
+
+    // ---- sources, conserved update, RK average
+    {
+        const int r = tid / TQ, c = tid - r * TQ;
+        const int i = i0 + r, j = j0 + c;
+        if (i < nr && j < nq) {
+            const int64_t n = (int64_t)nr * nq;
+            const int64_t z = (int64_t)i * nq + j;
+            R Pc[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) Pc[q] = sP[(q * PR + r + 2) * PQ + c + 2];
+            R src[4];
+            R dV;
+            if (MIXED) {
+                sources(ph, Pc, (R)B.rc32[i], (R)B.cot32[j], src);
+                dV = (R)(B.dv_r[i] * B.dv_q[j]);
+            } else {
+                sources(ph, Pc, (R)B.rc[i], (R)B.cot[j], src);
+                dV = (R)B.dv[z];
+            }
+            const R dt = (R)a.dt;
+            const double* Uin = B.buf[a.sel_in];
+            double* Uout = B.buf[a.sel_out];
+            const double* U0 = a.sel_base >= 0 ? B.buf[a.sel_base] : nullptr;
+            double res[NFIELD];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const R sc = src[q] * cflux * dV;
+                const R fa = sFr[(q * (TR + 1) + r) * TQ + c];
+                const R fb = sFr[(q * (TR + 1) + r + 1) * TQ + c];
+                R du;
+                if (one_d) {
+                    du = (sc - (fb - fa)) * dt;
+                } else {
+                    const R fc = sFq[(q * TR + r) * (TQ + 1) + c];
+                    const R fd = sFq[(q * TR + r) * (TQ + 1) + c + 1];
+                    du = (sc - (fb - fa) - (fd - fc)) * dt;
+                }
+                res[q] = Uin[q * n + z] + (double)du;
+            }
+            {
+                const R fa = sFr[(4 * (TR + 1) + r) * TQ + c];
+                const R fb = sFr[(4 * (TR + 1) + r + 1) * TQ + c];
+                R ds;
+                if (one_d) {
+                    ds = (fb - fa) * -dt;
+                } else {
+                    const R fc = sFq[(4 * TR + r) * (TQ + 1) + c];
+                    const R fd = sFq[(4 * TR + r) * (TQ + 1) + c + 1];
+                    ds = ((fb - fa) + (fd - fc)) * -dt;
+                }
+                res[4] = Uin[4 * n + z] + (double)ds;
+            }
+            if (U0) {
+#pragma unroll
+                for (int q = 0; q < NFIELD; ++q) res[q] = res[q] * a.w1 + U0[q * n + z] * a.bf;
+            }
+#pragma unroll
+            for (int q = 0; q < NFIELD; ++q) Uout[q * n + z] = res[q];
+        }
+    }
+}
+
+// Block-wide reduction helpers (warp shuffles, then one atomic per warp).
+__device__ __forceinline__ void warp_reduce_stats(DevStatus* st, unsigned long long zones,
+                                                  unsigned long long it64, unsigned long long it32,
+                                                  unsigned long long fb, double dtz, bool want_dt) {
+    const unsigned mask = 0xffffffffu;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        zones += __shfl_down_sync(mask, zones, o);
+        it64 += __shfl_down_sync(mask, it64, o);
+        it32 += __shfl_down_sync(mask, it32, o);
+        fb += __shfl_down_sync(mask, fb, o);
+        if (want_dt) dtz = fmin(dtz, __shfl_down_sync(mask, dtz, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (zones) atomicAdd(&st->c2p_zones, zones);
+        if (it64) atomicAdd(&st->iters_fp64, it64);
+        if (it32) atomicAdd(&st->iters_fp32, it32);
+        if (fb) atomicAdd(&st->fallbacks, fb);
+        if (want_dt) atomicMin(&st->dt_bits, (unsigned long long)__double_as_longlong(dtz));
+    }
+}
+
+// Write one zone's primitive + scalar density into its padded row and, for
+// the two rows next to a block edge, into the neighbour's halo rows.
+template <class R>
+__device__ __forceinline__ void store_prim(const DevBlock& B, int i, int j, const R v[NFIELD]) {
+    const int nr = B.nr, nq = B.nq;
+    R* Pd = reinterpret_cast<R*>(B.P);
+    const int64_t pn = (int64_t)(nr + 4) * nq;
+    const int64_t off = (int64_t)(i + 2) * nq + j;
+#pragma unroll
+    for (int q = 0; q < NFIELD; ++q) Pd[q * pn + off] = v[q];
+    if (i < 2 && B.P_in_nbr) {
+        R* Q = reinterpret_cast<R*>(B.P_in_nbr);
+        const int nrn = B.nr_in_nbr;
+        const int64_t qn = (int64_t)(nrn + 4) * nq;
+        const int64_t qo = (int64_t)(nrn + 2 + i) * nq + j;
+#pragma unroll
+        for (int q = 0; q < NFIELD; ++q) Q[q * qn + qo] = v[q];
+    }
+    if (i >= nr - 2 && B.P_out_nbr) {
+        R* Q = reinterpret_cast<R*>(B.P_out_nbr);
+        const int64_t qn = (int64_t)(B.nr_out_nbr + 4) * nq;
+        const int64_t qo = (int64_t)(i - (nr - 2)) * nq + j;
+#pragma unroll
+        for (int q = 0; q < NFIELD; ++q) Q[q * qn + qo] = v[q];
+    }
+}
+
+}  // namespace knc

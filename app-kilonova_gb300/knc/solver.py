@@ -1,0 +1,206 @@
+"""Python host over the C ABI of libknc_gpu.so.
+
+`Solver` mirrors the reference's run-loop contract for the hot path:
+`advance(fold)` is scheme::advance (src/scheme.rs:212-240), `time_step()` is
+State::time_step (src/state.rs:143-162), blocks are BlockState keyed by
+BlockIndex (i, 0) (src/state.rs:27-43), and `init_from_model` is
+State::from_model over Mesh::grid_blocks (src/state.rs:107-115,
+src/mesh.rs:384-397). A failed c2p raises `HydroError` carrying the same
+fields as the reference's HydroError (src/physics/mod.rs:109-117).
+There is no CPU fallback: every call runs the CUDA library.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+
+class HydroError(abi.KncError):
+    """c2p failure at a zone: kind name, block index, zone, (r, theta), value."""
+
+
+def _raise(lib, h, status, what):
+    if status == abi.KNC_OK:
+        return
+    e = abi.Error()
+    if h:
+        lib.knc_last_error(h, C.byref(e))
+    info = dict(kind=abi.HYDRO_ERROR_NAMES.get(e.kind, str(e.kind)), block=e.block, i=e.i, j=e.j,
+                r=e.r, theta=e.theta, value=e.value)
+    msg = f"{what}: {lib.knc_status_string(status).decode()}: {e.message.decode(errors='replace')}"
+    if status == abi.KNC_ERR_HYDRO:
+        raise HydroError(status, msg, info)
+    raise abi.KncError(status, msg, info)
+
+
+class Solver:
+    """One simulation on the current CUDA device (one stream)."""
+
+    def __init__(self, hydro, mesh, precision: int = abi.KNC_PRECISION_FP64):
+        self.lib = abi.load()
+        self.hydro = hydro
+        self.mesh = mesh
+        self.hp = hydro.to_c() if hasattr(hydro, "to_c") else hydro
+        self.mp = mesh.to_c() if hasattr(mesh, "to_c") else mesh
+        h = C.c_void_p()
+        st = self.lib.knc_create(C.byref(self.hp), C.byref(self.mp), C.byref(h))
+        if st != abi.KNC_OK:
+            raise abi.KncError(st, f"knc_create: {self.lib.knc_status_string(st).decode()}")
+        self.h = h
+        self.nr = int(self.mp.block_size)
+        self.nq = int(self.mp.num_polar_zones)
+        self._host_cb = None
+        if precision != abi.KNC_PRECISION_FP64:
+            self.set_precision(precision)
+
+    # ---- lifecycle
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.knc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st, what):
+        _raise(self.lib, self.h, st, what)
+
+    # ---- configuration
+    def set_model(self, model):
+        mp = model.to_c() if hasattr(model, "to_c") else model
+        self._check(self.lib.knc_set_model(self.h, C.byref(mp)), "set_model")
+
+    def set_host_model(self, fn):
+        """fn(r, theta, t) -> ([u_r, u_theta, rho, p], scalar): the slow path."""
+        def cb(r, q, t, out, s, _user):
+            any_prim, scalar = fn(r, q, t)
+            for k in range(4):
+                out[k] = float(any_prim[k])
+            s[0] = float(scalar)
+        self._host_cb = abi.PRIMITIVE_AT_FN(cb)
+        self._check(self.lib.knc_set_host_model(self.h, self._host_cb, None), "set_host_model")
+
+    def set_precision(self, precision: int):
+        self._check(self.lib.knc_set_precision(self.h, precision), "set_precision")
+
+    def set_c2p_guess(self, guess: int, weights=None):
+        if weights is None:
+            self._check(self.lib.knc_set_c2p_guess(self.h, guess, None, 0), "set_c2p_guess")
+        else:
+            w = np.ascontiguousarray(weights, dtype=np.float32)
+            self._check(self.lib.knc_set_c2p_guess(self.h, guess, abi.fptr(w), w.size), "set_c2p_guess")
+
+    def set_batched(self, graph: bool):
+        self._check(self.lib.knc_set_batched(self.h, int(bool(graph))), "set_batched")
+
+    def set_mixed_w_split(self, w: float):
+        self._check(self.lib.knc_set_mixed_w_split(self.h, float(w)), "set_mixed_w_split")
+
+    # ---- state
+    def init_from_model(self, time: float = 0.0):
+        self._check(self.lib.knc_init_from_model(self.h, float(time)), "init_from_model")
+
+    def add_block(self, index: int, cons, scalar):
+        cons = np.ascontiguousarray(cons, dtype=np.float64)
+        scalar = np.ascontiguousarray(scalar, dtype=np.float64)
+        if cons.shape != (self.nr, self.nq, 4) or scalar.shape != (self.nr, self.nq):
+            raise ValueError(f"block arrays must be ({self.nr}, {self.nq}, 4) and ({self.nr}, {self.nq})")
+        self._check(self.lib.knc_add_block(self.h, int(index), abi.dptr(cons), abi.dptr(scalar)), "add_block")
+
+    def remove_block(self, index: int):
+        self._check(self.lib.knc_remove_block(self.h, int(index)), "remove_block")
+
+    def block_indexes(self):
+        n = C.c_int32()
+        self.lib.knc_num_blocks(self.h, C.byref(n))
+        out = (C.c_int32 * max(n.value, 1))()
+        self._check(self.lib.knc_block_indexes(self.h, out, n.value), "block_indexes")
+        return [out[k] for k in range(n.value)]
+
+    def get_block(self, index: int):
+        cons = np.empty((self.nr, self.nq, 4))
+        scalar = np.empty((self.nr, self.nq))
+        self._check(self.lib.knc_get_block(self.h, int(index), abi.dptr(cons), abi.dptr(scalar)), "get_block")
+        return cons, scalar
+
+    def state(self):
+        return {i: self.get_block(i) for i in self.block_indexes()}
+
+    def set_state(self, cons, scalar):
+        self._check(self.lib.knc_set_state(self.h, abi.dptr(cons), abi.dptr(scalar)), "set_state")
+
+    def get_state(self, cons, scalar):
+        self._check(self.lib.knc_get_state(self.h, abi.dptr(cons), abi.dptr(scalar)), "get_state")
+
+    def set_time(self, t: float, num: int = 0, den: int = 1):
+        self._check(self.lib.knc_set_time(self.h, float(t), int(num), int(den)), "set_time")
+
+    def time(self):
+        t = C.c_double()
+        n = C.c_int64()
+        d = C.c_int64()
+        self.lib.knc_get_time(self.h, C.byref(t), C.byref(n), C.byref(d))
+        return t.value, (n.value, d.value)
+
+    # ---- hot path
+    def time_step(self) -> float:
+        dt = C.c_double()
+        self._check(self.lib.knc_time_step(self.h, C.byref(dt)), "time_step")
+        return dt.value
+
+    def advance(self, fold: int = 1):
+        self._check(self.lib.knc_advance(self.h, int(fold)), "advance")
+
+    def try_advance(self, fold: int = 1) -> int:
+        return self.lib.knc_advance(self.h, int(fold))
+
+    def last_error(self) -> abi.Error:
+        e = abi.Error()
+        self.lib.knc_last_error(self.h, C.byref(e))
+        return e
+
+    def synchronize(self):
+        self._check(self.lib.knc_synchronize(self.h), "synchronize")
+
+    # ---- statistics
+    def c2p_stats(self):
+        z, a, b, f = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        self._check(self.lib.knc_c2p_stats(self.h, C.byref(z), C.byref(a), C.byref(b), C.byref(f)), "c2p_stats")
+        return dict(zones=z.value, iters_fp64=a.value, iters_fp32=b.value, fallbacks=f.value)
+
+    def reset_c2p_stats(self):
+        self._check(self.lib.knc_reset_c2p_stats(self.h), "reset_c2p_stats")
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        self.lib.knc_launch_count(self.h, C.byref(n))
+        return n.value
+
+
+def measure_fp64_peak() -> float:
+    lib = abi.load()
+    g = C.c_double()
+    st = lib.knc_measure_fp64_peak(C.byref(g))
+    if st != abi.KNC_OK:
+        raise abi.KncError(st, "knc_measure_fp64_peak failed")
+    return g.value
+
+
+def build_solver(workload, precision=abi.KNC_PRECISION_FP64):
+    """Solver for a knc.workloads.Workload with its model set and initial data."""
+    s = Solver(workload.hydro, workload.mesh, precision=precision)
+    s.set_model(workload.model)
+    s.init_from_model(0.0)
+    return s

@@ -1,0 +1,287 @@
+/*
+ * knc.h — C ABI of the GB300 finite-volume stage library (libknc_gpu.so).
+ *
+ * The library replaces the Runge–Kutta hot path of the Clemson Kilonova Code:
+ * `scheme::advance` (src/scheme.rs:212-240) together with the per-block stage
+ * `try_advance_rk` (src/scheme.rs:16-173), the state operations it relies on
+ * (src/state.rs:55-244), the block geometry (src/mesh.rs:119-407) and the
+ * per-zone physics reached through the `Hydrodynamics` trait
+ * (src/traits.rs:41-136; src/physics/relativistic_hydro.rs:42-165,
+ * src/physics/newtonian_hydro.rs:34-133).
+ *
+ * Conventions
+ *  - Every entry point returns an int status: KNC_OK (0) or a KNC_ERR_* code.
+ *    A hydro failure inside a stage (negative density, negative energy,
+ *    root-finder failure) is a value, never a crash, exactly as
+ *    `HydroError` is in the reference (src/physics/mod.rs:83-117);
+ *    `knc_last_error` returns the first failing zone with its (r, theta).
+ *  - Conserved data crossing the ABI is volume-integrated (the reference's
+ *    `BlockState.conserved` is U·dV, src/state.rs:62-63) and array-of-structs
+ *    `[nr][nq][4]` in the reference's component order (D, S_r, S_theta, tau)
+ *    for relativistic hydro and (rho, rho v_r, rho v_theta, E) for Newtonian.
+ *    The scalar mass is `[nr][nq]`.
+ *  - The device owns the live state; host buffers are only read or written
+ *    inside the call that receives them.
+ *  - One context = one CUDA stream on the current device; a context must be
+ *    driven from one host thread at a time.
+ */
+#ifndef KNC_H
+#define KNC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+    KNC_OK = 0,
+    KNC_ERR_INVALID_ARGUMENT = 1,   /* bad pointer, size, or parameter       */
+    KNC_ERR_CONFIG = 2,             /* mesh / hydro validation failed        */
+    KNC_ERR_CUDA = 3,               /* a CUDA runtime call failed            */
+    KNC_ERR_NO_BLOCK = 4,           /* block index not present               */
+    KNC_ERR_HYDRO = 5,              /* a zone failed in c2p (see last_error) */
+    KNC_ERR_UNSUPPORTED = 6,        /* combination not built                 */
+    KNC_ERR_OUT_OF_MEMORY = 7,
+    KNC_ERR_TIMEOUT = 8             /* a bounded device wait gave up         */
+};
+
+/* ---- hydro error kinds (src/physics/mod.rs:83-95) ------------------------ */
+enum {
+    KNC_HYDRO_NONE = 0,
+    KNC_HYDRO_NEGATIVE_DENSITY = 1,
+    KNC_HYDRO_NEGATIVE_PRESSURE = 2,
+    KNC_HYDRO_NEGATIVE_ENERGY_DENSITY = 3,
+    KNC_HYDRO_ROOT_FINDER_FAILED = 4
+};
+
+/* ---- enumerations of the configuration --------------------------------- */
+enum { KNC_SYSTEM_RELATIVISTIC = 0, KNC_SYSTEM_NEWTONIAN = 1 };  /* AnyHydro, src/app.rs:86-89 */
+enum { KNC_RIEMANN_HLLE = 0, KNC_RIEMANN_HLLC = 1 };             /* src/physics/mod.rs:27-30   */
+enum { KNC_PRECISION_FP64 = 0, KNC_PRECISION_MIXED = 1 };
+enum { KNC_GUESS_PLAIN = 0, KNC_GUESS_MLP = 1 };
+
+/* Initial / boundary models, evaluated on the device (src/traits.rs:145-164). */
+enum {
+    KNC_MODEL_WIND = 0,      /* cold radial wind rho ~ r^-2, u^r = const            */
+    KNC_MODEL_JET = 1,       /* wind-like ambient + W=const nozzle at the inner edge */
+    KNC_MODEL_SPHERE = 2,    /* Newtonian over-dense sphere at rest                  */
+    KNC_MODEL_HOST = 3       /* host callback (slow path, no graph capture)          */
+};
+
+/*
+ * Mirror of `RelativisticHydro` (src/physics/relativistic_hydro.rs:15-36) and
+ * `NewtonianHydro` (src/physics/newtonian_hydro.rs:15-28). Newtonian hydro
+ * ignores `adaptive_time_step` (always adaptive, newtonian_hydro.rs:79-81).
+ * `riemann_solver` = KNC_RIEMANN_HLLC for Newtonian selects a Toro HLLC flux,
+ * an extension (the reference's Newtonian adapter is HLLE only).
+ */
+typedef struct knc_hydro_params {
+    int32_t system;             /* KNC_SYSTEM_*                          */
+    int32_t runge_kutta_order;  /* 1, 2 or 3 (RungeKuttaOrder RK1..RK3)  */
+    int32_t riemann_solver;     /* KNC_RIEMANN_*                         */
+    int32_t adaptive_time_step; /* 0 / 1                                 */
+    double gamma_law_index;
+    double plm_theta;           /* [1, 2]                                */
+    double cfl_number;          /* [0, 0.7]                              */
+} knc_hydro_params;
+
+/* Mirror of `Mesh` (src/mesh.rs:84-113). Option<> fields use a has_ flag. */
+typedef struct knc_mesh_params {
+    double reference_radius;
+    double inner_radius;
+    double outer_radius;
+    double inner_excision_speed;
+    double outer_excision_speed;
+    double excision_delay;          /* used when has_excision_delay != 0 */
+    int64_t num_radial_zones;       /* per decade; used when has_num_radial_zones */
+    int64_t num_polar_zones;
+    int64_t block_size;
+    int32_t has_num_radial_zones;
+    int32_t has_excision_delay;
+} knc_mesh_params;
+
+/*
+ * Device-side model selection. Parameters by kind:
+ *  WIND  : p[0]=rho at r=1, p[1]=u^r, p[2]=p/rho, p[3]=noise amplitude
+ *  JET   : p[0]=rho at r=1, p[1]=p/rho, p[2]=noise amplitude,
+ *          p[3]=nozzle half-opening angle, p[4]=jet Lorentz factor,
+ *          p[5]=jet density / ambient density, p[6]=injection radius
+ *          (zones with r < p[6] and theta within p[3] of a pole carry the
+ *          jet; with p[6] at the inner mesh edge only the inner ghost block
+ *          does, so the jet enters through the inner boundary)
+ *  SPHERE: p[0]=rho inside, p[1]=rho outside, p[2]=sphere radius,
+ *          p[3]=pressure, p[4]=noise amplitude
+ * Noise multiplies the density by (1 + amp * U[0,1)) with U a counter-based
+ * hash of (seed, block index, i, j); it enters only the initial data, never
+ * the ghost blocks, so `primitive_at` stays a pure function of (r, theta, t).
+ */
+typedef struct knc_model_params {
+    int32_t kind;
+    int32_t reserved;
+    uint64_t seed;
+    double p[16];
+} knc_model_params;
+
+/* Host model callback: AnyPrimitive order [u_r, u_theta, rho, p]
+ * (src/physics/mod.rs:59-63) and the scalar concentration. */
+typedef void (*knc_primitive_at_fn)(double r, double theta, double t,
+                                    double out_any_primitive[4],
+                                    double* out_scalar, void* user);
+
+/* First failing zone of the last failed call (HydroError, src/physics/mod.rs:109-117). */
+typedef struct knc_error {
+    int32_t kind;        /* KNC_HYDRO_*                 */
+    int32_t block;       /* block index (i32 of BlockIndex) */
+    int32_t i, j;        /* zone within the block        */
+    double r, theta;     /* cell centroid                */
+    double value;        /* offending value              */
+    char message[256];   /* human readable, includes CUDA errors */
+} knc_error;
+
+typedef struct knc_ctx knc_ctx;
+
+/* ---- lifecycle --------------------------------------------------------- */
+
+/* Validate (Mesh::validate src/mesh.rs:273-299, RelativisticHydro::validate
+ * relativistic_hydro.rs:46-54) and create a context on the current device. */
+int knc_create(const knc_hydro_params* hydro, const knc_mesh_params* mesh,
+               knc_ctx** out);
+void knc_destroy(knc_ctx* ctx);
+const char* knc_status_string(int status);
+int knc_last_error(const knc_ctx* ctx, knc_error* out);
+
+/* ---- model and state (src/state.rs:55-69, 107-115; src/app.rs:315-330) ---- */
+
+int knc_set_model(knc_ctx* ctx, const knc_model_params* model);
+int knc_set_host_model(knc_ctx* ctx, knc_primitive_at_fn fn, void* user);
+
+/* State::from_model over Mesh::grid_blocks(time) (src/mesh.rs:384-397):
+ * replaces every block, sets time and iteration = 0. */
+int knc_init_from_model(knc_ctx* ctx, double time);
+
+/* Insert or replace one block (BlockIndex (index, 0), src/mesh.rs:12).
+ * cons_aos: [block_size][num_polar_zones][4]; scalar_mass: [..][..]. */
+int knc_add_block(knc_ctx* ctx, int32_t index, const double* cons_aos,
+                  const double* scalar_mass);
+int knc_remove_block(knc_ctx* ctx, int32_t index);
+int knc_get_block(knc_ctx* ctx, int32_t index, double* cons_aos,
+                  double* scalar_mass);
+int knc_num_blocks(const knc_ctx* ctx, int32_t* n);
+int knc_block_indexes(const knc_ctx* ctx, int32_t* out, int32_t capacity);
+int knc_block_shape(const knc_ctx* ctx, int64_t* nr, int64_t* nq);
+
+/* Whole-state copies for host-resident drivers: blocks in ascending index
+ * order, each [nr][nq][4] then [nr][nq]; sizes must match the live state. */
+int knc_set_state(knc_ctx* ctx, const double* cons_aos, const double* scalar_mass);
+int knc_get_state(knc_ctx* ctx, double* cons_aos, double* scalar_mass);
+
+/* State.time and State.iteration (Rational64 as num/den), src/state.rs:39-43 */
+int knc_set_time(knc_ctx* ctx, double time, int64_t iter_num, int64_t iter_den);
+int knc_get_time(const knc_ctx* ctx, double* time, int64_t* iter_num,
+                 int64_t* iter_den);
+
+/* ---- the hot path ------------------------------------------------------ */
+
+/* State::time_step (src/state.rs:143-162). */
+int knc_time_step(knc_ctx* ctx, double* dt);
+
+/* scheme::advance (src/scheme.rs:212-240): dt once, then `fold` times
+ * {add_remove_blocks if the excision surfaces move; one RK step}. */
+int knc_advance(knc_ctx* ctx, int32_t fold);
+
+/* Chosen forms. */
+int knc_set_precision(knc_ctx* ctx, int32_t precision);          /* KNC_PRECISION_* */
+/* weights: the packed MLP (see knc_mlp_num_params); NULL with KNC_GUESS_PLAIN. */
+int knc_set_c2p_guess(knc_ctx* ctx, int32_t guess, const float* weights,
+                      size_t n_weights);
+/* graph != 0: capture each `fold` of RK steps in a CUDA graph and replay it. */
+int knc_set_batched(knc_ctx* ctx, int32_t graph);
+/* Mixed precision: zones whose Lorentz factor estimate exceeds this recover
+ * primitives in FP64 (default 2.0); below it recovery runs in FP32. */
+int knc_set_mixed_w_split(knc_ctx* ctx, double w_split);
+
+/* Wait for all work of the context; returns the first deferred error. */
+int knc_synchronize(knc_ctx* ctx);
+
+/* ---- statistics -------------------------------------------------------- */
+
+/* Newton iterations summed over zones and c2p calls since the last reset,
+ * split by the precision they ran in. */
+int knc_c2p_stats(knc_ctx* ctx, int64_t* zones, int64_t* iters_fp64,
+                  int64_t* iters_fp32, int64_t* fallbacks);
+int knc_reset_c2p_stats(knc_ctx* ctx);
+/* Kernel launches issued by the context since creation. */
+int knc_launch_count(const knc_ctx* ctx, int64_t* launches);
+
+/* ---- learned c2p guess: MLP 3 -> 64 -> 64 -> 1 (SiLU) ------------------ */
+/*
+ * Packed float layout (offsets in floats):
+ *   W1 [64][3]   @ 0      b1 [64] @ 192
+ *   W2 [64][64]  @ 256    b2 [64] @ 4352      (row = output unit)
+ *   W3 [64]      @ 4416   b3 [1]  @ 4480
+ *   x_mean [3]   @ 4481   x_scale [3] @ 4484  (fixed input normalisation)
+ * Forward: xn = (x - x_mean) * x_scale; h1 = silu(bf16(W1) xn + b1);
+ * h2 = silu(bf16(W2) bf16(h1) + b2) with FP32 accumulation;
+ * y = bf16(W3) . h2 + b3. The target is log(p / D); the pressure guess is
+ * D * exp(y). Inputs x = (log D, |S| / (D + tau), log(tau / D)).
+ */
+#define KNC_MLP_HIDDEN 64
+#define KNC_MLP_OFF_W1 0
+#define KNC_MLP_OFF_B1 192
+#define KNC_MLP_OFF_W2 256
+#define KNC_MLP_OFF_B2 4352
+#define KNC_MLP_OFF_W3 4416
+#define KNC_MLP_OFF_B3 4480
+#define KNC_MLP_OFF_XMEAN 4481
+#define KNC_MLP_OFF_XSCALE 4484
+#define KNC_MLP_NUM_PARAMS 4487
+
+/* Number of floats in a packed weight vector (= KNC_MLP_NUM_PARAMS). */
+size_t knc_mlp_num_params(void);
+
+/* Training pairs from the solver: writes up to `capacity` rows of
+ * [D, S_r, S_theta, tau, rho, u_r, u_theta, p] (per unit volume) sampled
+ * from the live state of `ctx` (every `stride`-th zone). */
+int knc_sample_pairs(knc_ctx* ctx, int32_t stride, double* out, int64_t capacity,
+                     int64_t* written);
+
+/* Synthetic pairs over Lorentz factor [w_lo, w_hi] and p/rho [t_lo, t_hi]
+ * (log-uniform), produced on the device with the solver's prim->cons. */
+int knc_generate_pairs(double gamma_law_index, double w_lo, double w_hi,
+                       double t_lo, double t_hi, uint64_t seed, int64_t n,
+                       double* out_host);
+
+/* Train on the device: `pairs` [n][8] host rows as written above. Runs
+ * `steps` Adam steps of `batch` rows; returns the final loss. Weights in/out. */
+typedef struct knc_mlp_train_params {
+    int64_t steps;
+    int32_t batch;
+    int32_t reserved;
+    float lr;
+    float beta1, beta2, eps;
+    uint64_t seed;
+} knc_mlp_train_params;
+int knc_mlp_train(const double* pairs, int64_t n, float* weights,
+                  const knc_mlp_train_params* params, float* final_loss);
+
+/* Device forward / backward on one batch (for gradient checks): inputs x
+ * [n][3] (already normalised features), targets y [n]; outputs prediction
+ * [n], loss and the gradient of the loss wrt every packed parameter. */
+int knc_mlp_forward_backward(const float* weights, const float* x, const float* y,
+                             int32_t n, float* pred, float* loss, float* grad);
+
+/* Features of a conserved state (log D, |S|/(D+tau), log tau/D). */
+void knc_mlp_features(const double u[4], float out[3]);
+
+/* ---- utilities --------------------------------------------------------- */
+
+/* Measured FP64 FMA throughput of the current device (GFLOP/s, 2/FMA). */
+int knc_measure_fp64_peak(double* gflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KNC_H */
