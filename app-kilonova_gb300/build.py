@@ -22,6 +22,9 @@ LIB = OUT / "libknc_gpu.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+          # host-side geometry and time bookkeeping round like the CPU reference
+          # implementation on x86-64 and aarch64 alike (gcc contracts by default)
+          "-Xcompiler", "-ffp-contract=off",
           "--expt-relaxed-constexpr", f"-I{INCLUDE}"]
 PER_FILE = {
     "knc_f64.cu": ["--fmad=false"],
@@ -54,10 +57,13 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> Path:
     OUT.mkdir(exist_ok=True)
     headers = _headers()
     cc = nvcc()
+    stamp = OUT / "flags.txt"
+    flags = repr((ARCH, COMMON, PER_FILE, cc))
+    force = not stamp.exists() or stamp.read_text() != flags
     jobs = []
     for src in _sources():
         obj = OUT / (src.stem + ".o")
-        if _stale(obj, src, headers) or ptxas_info:
+        if force or _stale(obj, src, headers) or ptxas_info:
             cmd = [cc, *ARCH, *COMMON, *PER_FILE.get(src.name, []), "-c", str(src), "-o", str(obj)]
             if ptxas_info:
                 cmd.insert(1, "-Xptxas=-v")
@@ -79,6 +85,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> Path:
     if failed:
         msg = "\n".join(f"--- {s.name}\n{log}" for s, log in failed)
         raise RuntimeError("nvcc failed:\n" + msg)
+    stamp.write_text(flags)
     objs = [str(OUT / (s.stem + ".o")) for s in _sources()]
     if jobs or not LIB.exists():
         cmd = [cc, *ARCH, "-shared", "-cudart", "static", "-o", str(LIB), *objs]

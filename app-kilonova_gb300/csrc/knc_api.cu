@@ -243,6 +243,14 @@ struct knc_ctx {
     float* d_mlp = nullptr;
     // bookkeeping
     int64_t launches = 0;
+    bool profiling = false;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_events;
+    std::vector<cudaEvent_t> event_pool;
+    double prof_ms[KNC_KERNEL_KINDS] = {0, 0, 0};
+    int64_t prof_count[KNC_KERNEL_KINDS] = {0, 0, 0};
+    bool capturing = false;
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaEvent_t marks[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     knc_error err{};
     double* d_stage = nullptr;
     size_t stage_cap = 0;
@@ -502,6 +510,51 @@ int host_ghost_values(knc_ctx* c, double t) {
     return KNC_OK;
 }
 
+cudaEvent_t take_event(knc_ctx* c) {
+    if (!c->event_pool.empty()) {
+        cudaEvent_t e = c->event_pool.back();
+        c->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Brackets one launch with events when profiling (not inside graph capture).
+struct ProfScope {
+    knc_ctx* c;
+    int kind;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ProfScope(knc_ctx* c_, int kind_) : c(c_), kind(kind_) {
+        if (c->profiling && !c->capturing) {
+            e0 = take_event(c);
+            e1 = take_event(c);
+            cudaEventRecord(e0, c->stream);
+        }
+    }
+    ~ProfScope() {
+        if (e0) {
+            cudaEventRecord(e1, c->stream);
+            c->prof_events.push_back({kind, {e0, e1}});
+        }
+    }
+};
+
+// Fold finished event pairs into the per-kind sums (synchronises on them).
+void drain_profile(knc_ctx* c) {
+    for (auto& pe : c->prof_events) {
+        cudaEventSynchronize(pe.second.second);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, pe.second.first, pe.second.second);
+        c->prof_ms[pe.first] += ms;
+        c->prof_count[pe.first] += 1;
+        c->event_pool.push_back(pe.second.first);
+        c->event_pool.push_back(pe.second.second);
+    }
+    c->prof_events.clear();
+}
+
 StageArgs base_args(knc_ctx* c) {
     StageArgs a;
     std::memset(&a, 0, sizeof(a));
@@ -525,6 +578,7 @@ StageArgs base_args(knc_ctx* c) {
 bool mixed(const knc_ctx* c) { return c->precision == KNC_PRECISION_MIXED; }
 
 int launch_c2p(knc_ctx* c, const StageArgs& a) {
+    ProfScope ps(c, KNC_KERNEL_C2P);
     cudaError_t e = mixed(c) ? launch_c2p_mixed(a, c->stream) : launch_c2p_f64(a, c->stream);
     ++c->launches;
     CK(e);
@@ -532,6 +586,7 @@ int launch_c2p(knc_ctx* c, const StageArgs& a) {
 }
 
 int launch_update(knc_ctx* c, const StageArgs& a) {
+    ProfScope ps(c, KNC_KERNEL_UPDATE);
     cudaError_t e = mixed(c) ? launch_update_mixed(a, c->stream) : launch_update_f64(a, c->stream);
     ++c->launches;
     CK(e);
@@ -572,7 +627,10 @@ int run_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, doub
         if ((r = host_ghost_values(c, t_stage))) return r;
         g.host_prim = c->d_host_prim;
     }
-    CK(launch_ghost(g, c->stream));
+    {
+        ProfScope ps(c, KNC_KERNEL_GHOST);
+        CK(launch_ghost(g, c->stream));
+    }
     ++c->launches;
     StageArgs a = base_args(c);
     a.stage = stage;
@@ -722,6 +780,7 @@ int init_block_from_model(knc_ctx* c, int32_t index, double t) {
     ia.tiles = d_t;
     ia.sel = c->cur;
     ia.srhd = c->hp.system == KNC_SYSTEM_RELATIVISTIC;
+    ia.noise = 0;   // activated blocks take the model's noise-free data, like ghosts
     ia.gm = c->hp.gamma_law_index;
     ia.time = t;
     ia.model = c->model;
@@ -864,6 +923,7 @@ int ensure_stage(knc_ctx* c, size_t doubles) {
 
 int create_device_side(knc_ctx* c) {
     int r;
+    CK(configure_kernels());
     CK(cudaGetDevice(&c->device));
     CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CK(dalloc(&c->d_status, 1));
@@ -929,6 +989,11 @@ void knc_destroy(knc_ctx* c) {
     cudaFree(c->d_status);
     cudaFree(c->d_mlp);
     cudaFree(c->d_stage);
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    for (cudaEvent_t e : c->marks)
+        if (e) cudaEventDestroy(e);
+    drain_profile(c);
+    for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
     if (c->h_status) cudaFreeHost(c->h_status);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -983,6 +1048,7 @@ int knc_init_from_model(knc_ctx* c, double time) {
     ia.tiles = c->d_tiles;
     ia.sel = c->cur;
     ia.srhd = c->hp.system == KNC_SYSTEM_RELATIVISTIC;
+    ia.noise = 1;
     ia.gm = c->hp.gamma_law_index;
     ia.time = time;
     ia.model = c->model;
@@ -1153,7 +1219,7 @@ int knc_time_step(knc_ctx* c, double* dt) {
 
 int knc_advance(knc_ctx* c, int32_t fold) {
     if (!c || fold < 0) return KNC_ERR_INVALID_ARGUMENT;
-    int r;
+    int r = KNC_OK;
     if ((r = check_ready(c))) return r;
     if ((r = rebuild_table(c))) return r;
     if ((r = update_ghost_geometry(c))) return r;
@@ -1161,6 +1227,38 @@ int knc_advance(knc_ctx* c, int32_t fold) {
     double dt;
     if ((r = time_step_impl(c, &dt))) return r;
     const int per_step = c->hp.runge_kutta_order;
+    const bool graph = c->batched && !c->mesh.moving() && c->model.kind != KNC_MODEL_HOST && fold > 0 &&
+                       c->stage_counter + (int64_t)fold * per_step < 0xffff;
+    if (graph) {
+        // One CUDA graph holds the whole fold: ghost, c2p and update launches
+        // of every stage; a later fold with the same shape only updates the
+        // executable graph's parameters (times) instead of re-instantiating.
+        c->capturing = true;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        for (int32_t k = 0; k < fold && r == KNC_OK; ++k) r = rk_step(c, dt);
+        cudaGraph_t g = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(c->stream, &g);
+        c->capturing = false;
+        if (r) {
+            if (g) cudaGraphDestroy(g);
+            return r;
+        }
+        CK(ec);
+        if (c->graph_exec) {
+            cudaGraphExecUpdateResultInfo info;
+            if (cudaGraphExecUpdate(c->graph_exec, g, &info) != cudaSuccess) {
+                cudaGetLastError();
+                cudaGraphExecDestroy(c->graph_exec);
+                c->graph_exec = nullptr;
+            }
+        }
+        cudaError_t ei = cudaSuccess;
+        if (!c->graph_exec) ei = cudaGraphInstantiate(&c->graph_exec, g, 0);
+        cudaGraphDestroy(g);
+        CK(ei);
+        CK(cudaGraphLaunch(c->graph_exec, c->stream));
+        return check_status(c);
+    }
     for (int32_t k = 0; k < fold; ++k) {
         if (c->mesh.moving())
             if ((r = add_remove_blocks(c))) return r;
@@ -1171,6 +1269,38 @@ int knc_advance(knc_ctx* c, int32_t fold) {
         if ((r = rk_step(c, dt))) return r;
     }
     return check_status(c);
+}
+
+int knc_set_profiling(knc_ctx* c, int32_t on) {
+    if (!c) return KNC_ERR_INVALID_ARGUMENT;
+    drain_profile(c);
+    for (int k = 0; k < KNC_KERNEL_KINDS; ++k) {
+        c->prof_ms[k] = 0.0;
+        c->prof_count[k] = 0;
+    }
+    c->profiling = on != 0;
+    return KNC_OK;
+}
+
+int knc_kernel_times(knc_ctx* c, double* ms, int64_t* launches) {
+    if (!c) return KNC_ERR_INVALID_ARGUMENT;
+    drain_profile(c);
+    for (int k = 0; k < KNC_KERNEL_KINDS; ++k) {
+        if (ms) ms[k] = c->prof_ms[k];
+        if (launches) launches[k] = c->prof_count[k];
+    }
+    return KNC_OK;
+}
+
+int knc_host_alloc(size_t bytes, void** ptr) {
+    if (!ptr || bytes == 0) return KNC_ERR_INVALID_ARGUMENT;
+    if (cudaHostAlloc(ptr, bytes, cudaHostAllocDefault) != cudaSuccess) return KNC_ERR_OUT_OF_MEMORY;
+    return KNC_OK;
+}
+
+int knc_host_free(void* ptr) {
+    if (!ptr) return KNC_OK;
+    return cudaFreeHost(ptr) == cudaSuccess ? KNC_OK : KNC_ERR_CUDA;
 }
 
 int knc_set_precision(knc_ctx* c, int32_t precision) {
@@ -1234,6 +1364,77 @@ int knc_reset_c2p_stats(knc_ctx* c) {
 int knc_launch_count(const knc_ctx* c, int64_t* launches) {
     if (!c || !launches) return KNC_ERR_INVALID_ARGUMENT;
     *launches = c->launches;
+    return KNC_OK;
+}
+
+int knc_sample_pairs(knc_ctx* c, int32_t stride, double* out, int64_t capacity, int64_t* written) {
+    if (!c || !out || stride <= 0 || capacity <= 0) return KNC_ERR_INVALID_ARGUMENT;
+    if (c->hp.system != KNC_SYSTEM_RELATIVISTIC)
+        return set_msg(c, KNC_ERR_UNSUPPORTED, "pairs are defined for relativistic hydro");
+    if (c->blocks.empty()) return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "no blocks");
+    int r;
+    if ((r = rebuild_table(c))) return r;
+    double* d_out = nullptr;
+    unsigned long long* d_cnt = nullptr;
+    CK(dalloc(&d_out, (size_t)capacity * 8));
+    cudaError_t e = dalloc(&d_cnt, 1);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_cnt, 0, 8, c->stream);
+    if (e == cudaSuccess)
+        e = launch_sample_pairs(c->d_table, c->d_tiles, c->ntiles, c->cur, stride, c->hp.gamma_law_index, d_out,
+                                capacity, d_cnt, c->stream);
+    ++c->launches;
+    unsigned long long cnt = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&cnt, d_cnt, 8, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    const int64_t nw = std::min<int64_t>((int64_t)cnt, capacity);
+    if (e == cudaSuccess && nw > 0) e = cudaMemcpy(out, d_out, (size_t)nw * 8 * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaFree(d_out);
+    cudaFree(d_cnt);
+    CK(e);
+    if (written) *written = nw;
+    return KNC_OK;
+}
+
+int knc_mark(knc_ctx* c, int32_t slot) {
+    if (!c || slot < 0 || slot >= 8) return KNC_ERR_INVALID_ARGUMENT;
+    if (!c->marks[slot]) CK(cudaEventCreate(&c->marks[slot]));
+    CK(cudaEventRecord(c->marks[slot], c->stream));
+    return KNC_OK;
+}
+
+int knc_elapsed_ms(knc_ctx* c, int32_t a, int32_t b, double* ms) {
+    if (!c || !ms || a < 0 || a >= 8 || b < 0 || b >= 8 || !c->marks[a] || !c->marks[b])
+        return KNC_ERR_INVALID_ARGUMENT;
+    CK(cudaEventSynchronize(c->marks[b]));
+    float f = 0.f;
+    CK(cudaEventElapsedTime(&f, c->marks[a], c->marks[b]));
+    *ms = f;
+    return KNC_OK;
+}
+
+int knc_get_primitives(knc_ctx* c, int32_t index, double* prim) {
+    if (!c || !prim) return KNC_ERR_INVALID_ARGUMENT;
+    auto it = c->blocks.find(index);
+    if (it == c->blocks.end()) return set_msg(c, KNC_ERR_NO_BLOCK, "no block %d", index);
+    int r;
+    if ((r = check_ready(c))) return r;
+    if ((r = rebuild_table(c))) return r;
+    if ((r = reset_status(c, true))) return r;
+    StageArgs a = base_args(c);
+    a.mlp = nullptr;
+    a.stage = c->stage_counter++;
+    a.sel_in = c->cur;
+    a.sel_out = c->cur;
+    CK(launch_c2p_f64(a, c->stream));   // FP64 recovery, double primitives
+    ++c->launches;
+    if ((r = check_status(c))) return r;
+    const BlockH& b = it->second;
+    const size_t n = (size_t)(b.nr * b.nq);
+    if ((r = ensure_stage(c, 5 * n))) return r;
+    CK(launch_prims_to_aos(b.P, c->d_stage, b.nr, b.nq, c->stream));
+    ++c->launches;
+    CK(cudaMemcpyAsync(prim, c->d_stage, 5 * n * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     return KNC_OK;
 }
 

@@ -12,6 +12,7 @@
 // oracle's, so this path reproduces the reference arithmetic bit for bit
 // wherever the libm-free operations (+ - * / sqrt) are all that is used.
 #include "knc_internal.h"
+#include "knc_mlp.cuh"
 #include "knc_models.cuh"
 #include "knc_physics.cuh"
 #include "knc_stage.cuh"
@@ -19,31 +20,66 @@
 namespace knc {
 
 // ---- c2p -------------------------------------------------------------------
+// MLP = true: the Newton recovery starts from the learned pressure guess; the
+// plain guess p = 0 is retried when that start does not converge.
+template <bool MLP>
 __global__ void __launch_bounds__(TILE_THREADS) c2p_f64_kernel(StageArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
     if (ek != NO_ERROR && (uint32_t)(ek >> 48) < (uint32_t)a.stage) return;
-    const int4 t = a.tiles[blockIdx.x];
-    const DevBlock& B = a.blocks[t.x];
-    const int i = t.y + threadIdx.x / TILE_Q;
-    const int j = t.z + threadIdx.x % TILE_Q;
-    const int nr = B.nr, nq = B.nq;
-    const bool active = i < nr && j < nq;
-    int iters = 0;
+    MlpWeights& W = *reinterpret_cast<MlpWeights*>(smem_raw);
+    __nv_bfloat16* act = reinterpret_cast<__nv_bfloat16*>(smem_raw + sizeof(MlpWeights)) +
+                         (threadIdx.x >> 5) * MLP_ACT_ELEMS;
+    if (MLP) {
+        mlp_load(W, a.mlp);
+        __syncthreads();
+    }
+    unsigned long long zones = 0, iters_sum = 0, fbs = 0;
     double dtz = 1.7976931348623157e308;
-    if (active) {
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        const int4 t = a.tiles[tile];
+        const DevBlock& B = a.blocks[t.x];
+        const int i = t.y + threadIdx.x / TILE_Q;
+        const int j = t.z + threadIdx.x % TILE_Q;
+        const int nr = B.nr, nq = B.nq;
+        const bool active = i < nr && j < nq;
         const int64_t n = (int64_t)nr * nq;
         const int64_t z = (int64_t)i * nq + j;
-        const double* U = B.buf[a.sel_in];
-        const double dV = B.dv[z];
-        double u[4];
+        double u[4] = {1.0, 0.0, 0.0, 1.0};
+        double smass = 0.0, dV = 1.0;
+        if (active) {
+            const double* U = B.buf[a.sel_in];
+            dV = B.dv[z];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) u[q] = U[q * n + z] / dV;
-        const double smass = U[4 * n + z];
+            for (int q = 0; q < 4; ++q) u[q] = U[q * n + z] / dV;
+            smass = U[4 * n + z];
+        }
+        double guess = 0.0;
+        if (MLP && a.srhd) {
+            float x[3];
+            const bool ok = mlp_features(u[0], u[1] * u[1] + u[2] * u[2], u[3], x);
+            const float y = mlp_warp_infer(W, act, x);
+            const double g = u[0] * (double)__expf(y);
+            const double gmax = (a.gm - 1.0) * u[3];
+            guess = (ok && g > 0.0) ? fmin(g, gmax) : 0.0;
+        }
+        if (!active) continue;
         double P[4] = {0.0, 0.0, 0.0, 0.0};
         double bad = 0.0;
-        int kind;
-        if (a.srhd) kind = srhd_c2p_newton(a.gm, u, 0.0, P, iters, bad);
-        else kind = newt_c2p(a.gm - 1.0, u, P, bad);
+        int kind, iters = 0;
+        if (a.srhd) {
+            kind = srhd_c2p_newton(a.gm, u, guess, P, iters, bad);
+            if (MLP && kind == HYDRO_ROOT_FINDER_FAILED && guess != 0.0) {
+                int it2 = 0;
+                ++fbs;
+                kind = srhd_c2p_newton(a.gm, u, 0.0, P, it2, bad);
+                iters += it2;
+            }
+        } else {
+            kind = newt_c2p(a.gm - 1.0, u, P, bad);
+        }
+        ++zones;
+        iters_sum += (unsigned long long)iters;
         if (kind != HYDRO_NONE && kind != HYDRO_NEGATIVE_PRESSURE) {
             atomicMin(&a.status->err_key, error_key(a.stage, t.x, i, j, kind));
             a.status->err_sel = a.sel_in;
@@ -63,11 +99,10 @@ __global__ void __launch_bounds__(TILE_THREADS) c2p_f64_kernel(StageArgs a) {
             const double dq = B.qv[j + 1] - B.qv[j];
             const double dl = fmin(dr, dq * B.rv[i]);
             const double amax = max_signal_speed(ph, P) * a.cflux;
-            dtz = dl / amax;
+            dtz = fmin(dtz, dl / amax);
         }
     }
-    warp_reduce_stats(a.status, active ? 1ull : 0ull, (unsigned long long)iters, 0ull, 0ull, dtz,
-                      a.compute_dt != 0);
+    warp_reduce_stats(a.status, zones, iters_sum, 0ull, fbs, dtz, a.compute_dt != 0);
 }
 
 // ---- ghost rows --------------------------------------------------------------
@@ -155,7 +190,7 @@ __global__ void __launch_bounds__(TILE_THREADS) init_kernel(InitArgs a) {
         Pm[3] = hp[3];
         scalar = hp[4];
     } else {
-        model_eval(a.model, B.rc[i], B.qc[j], a.time, true, B.index, i, j, Pm, scalar);
+        model_eval(a.model, B.rc[i], B.qc[j], a.time, a.noise != 0, B.index, i, j, Pm, scalar);
     }
     PhysT<double> ph;
     ph.srhd = a.srhd;
@@ -204,25 +239,54 @@ __global__ void soa_to_aos_kernel(const double* __restrict__ soa, double* __rest
     scalar[z] = soa[4 * n + z];
 }
 
+// Interior rows of a padded double primitive array -> [nr][nq][5], with the
+// scalar density divided by rho into a concentration.
+__global__ void prims_to_aos_kernel(const double* __restrict__ P, double* __restrict__ out, int64_t nr,
+                                    int64_t nq) {
+    const int64_t z = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (z >= nr * nq) return;
+    const int64_t pn = (nr + 4) * nq;
+    const int64_t off = 2 * nq + z;
+    double v[5];
+    for (int q = 0; q < 5; ++q) v[q] = P[q * pn + off];
+    v[4] = v[4] / v[0];
+    for (int q = 0; q < 5; ++q) out[z * 5 + q] = v[q];
+}
+
 // ---- launchers ---------------------------------------------------------------
+cudaError_t launch_prims_to_aos(const void* P, double* out, int64_t nr, int64_t nq, cudaStream_t s) {
+    const int64_t n = nr * nq;
+    prims_to_aos_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(reinterpret_cast<const double*>(P), out, nr, nq);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_c2p_f64(const StageArgs& a, cudaStream_t s) {
     if (a.ntiles <= 0) return cudaSuccess;
-    c2p_f64_kernel<<<a.ntiles, TILE_THREADS, 0, s>>>(a);
+    if (a.mlp && a.srhd) {
+        const size_t bytes = sizeof(MlpWeights) + 8 * MLP_ACT_ELEMS * sizeof(__nv_bfloat16);
+        int dev = 0, sms = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int grid = a.ntiles < sms * 4 ? a.ntiles : sms * 4;
+        c2p_f64_kernel<true><<<grid, TILE_THREADS, bytes, s>>>(a);
+    } else {
+        c2p_f64_kernel<false><<<a.ntiles, TILE_THREADS, 0, s>>>(a);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_update_f64(const StageArgs& a, cudaStream_t s) {
     if (a.ntiles <= 0) return cudaSuccess;
-    static bool configured = false;
-    const size_t bytes = StageSmem<double>::bytes;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(update_kernel<double, false>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
-    update_kernel<double, false><<<a.ntiles, TILE_THREADS, bytes, s>>>(a);
+    update_kernel<double, false><<<a.ntiles, TILE_THREADS, StageSmem<double>::bytes, s>>>(a);
     return cudaGetLastError();
+}
+
+cudaError_t configure_f64() {
+    cudaError_t e = cudaFuncSetAttribute(update_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)StageSmem<double>::bytes);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(c2p_f64_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(MlpWeights) + 8 * MLP_ACT_ELEMS * sizeof(__nv_bfloat16)));
 }
 
 cudaError_t launch_ghost(const GhostArgs& a, cudaStream_t s) {

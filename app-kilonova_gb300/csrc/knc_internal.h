@@ -122,6 +122,8 @@ struct InitArgs {
     const int4* tiles;
     int32_t sel;
     int32_t srhd;
+    int32_t noise;               // seeded density noise (initial data only)
+    int32_t pad_;
     double gm;
     double time;
     knc_model_params model;
@@ -129,6 +131,8 @@ struct InitArgs {
 };
 
 // ---- launchers (each returns the cudaError_t of the launch) -------------
+// Set the kernels' shared-memory attributes once, before any launch or capture.
+cudaError_t configure_kernels();
 cudaError_t launch_init_f64(const InitArgs& a, int ntiles, cudaStream_t s);
 cudaError_t launch_c2p_f64(const StageArgs& a, cudaStream_t s);
 cudaError_t launch_update_f64(const StageArgs& a, cudaStream_t s);
@@ -137,11 +141,10 @@ cudaError_t launch_c2p_mixed(const StageArgs& a, cudaStream_t s);
 cudaError_t launch_update_mixed(const StageArgs& a, cudaStream_t s);
 cudaError_t launch_aos_to_soa(const double* aos, const double* scalar, double* soa, int64_t nr, int64_t nq,
                               cudaStream_t s);
+cudaError_t launch_prims_to_aos(const void* P, double* out, int64_t nr, int64_t nq, cudaStream_t s);
 cudaError_t launch_soa_to_aos(const double* soa, double* aos, double* scalar, int64_t nr, int64_t nq,
                               cudaStream_t s);
-cudaError_t launch_sample_pairs(const DevBlock* blocks, int nblocks, int sel, int stride, double gm,
+cudaError_t launch_sample_pairs(const DevBlock* blocks, const int4* tiles, int ntiles, int sel, int stride, double gm,
                                 double* out, int64_t capacity, unsigned long long* counter, cudaStream_t s);
-cudaError_t launch_generate_pairs(double gm, double w_lo, double w_hi, double t_lo, double t_hi,
-                                  uint64_t seed, int64_t n, double* out, cudaStream_t s);
 
 }  // namespace knc

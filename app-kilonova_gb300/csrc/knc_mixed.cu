@@ -1,0 +1,223 @@
+// knc_mixed.cu — the mixed-precision stage.
+//
+// Same method as the FP64 stage (src/scheme.rs:16-173), with the precision
+// moved per operation:
+//   FP32  reconstruction, Riemann fluxes, geometric sources, geometry factors
+//         (update_kernel<float, true>), primitive storage;
+//   FP64  the conserved state and its RK accumulation, time and excision
+//         radius (host), and the cons -> prim recovery of zones whose Lorentz
+//         factor exceeds `w_split` — converged to the reference's residual
+//         |f| < 1e-12 (D + tau).
+// Zones below `w_split` recover in FP32. Every zone first runs the Newton
+// iteration in FP32; an FP64 recovery then starts from that root and usually
+// needs one or two FP64 iterations instead of the 3-6 the plain guess takes.
+//
+// The recovery is scale-invariant (U -> k U gives p -> k p), so it runs on the
+// volume-integrated state and divides rho and p by dV afterwards: no FP64
+// divisions by the cell volume.
+#include "knc_internal.h"
+#include "knc_mlp.cuh"
+#include "knc_physics.cuh"
+#include "knc_stage.cuh"
+
+namespace knc {
+
+// Newton-Raphson on the pressure, the reference's iteration rewritten with two
+// divisions: with X = tau + m (1 - W) + p (1 - W^2) and 1 - v^2 = 1/W^2,
+// rho e = X / W^2, f = (gamma - 1) rho e - p, rho h = m / W + rho e + p and
+// f / f' = f rho h / (v^2 gamma p - rho h). Converged when |f| < tol_abs or the
+// step is below tol_rel |p| (FP32 only; tol_rel = 0 reproduces the reference's
+// criterion). Returns the root and W at the last evaluated pressure.
+template <class R>
+__device__ __forceinline__ bool newton_fast(R m, R ss, R tau, R gm, R p, R tol_abs, R tol_rel, int maxit, R& p_out,
+                                            R& w_out, int& iters) {
+    const R bmax = sizeof(R) == 8 ? R(1.0 - 1e-10) : R(1.0f - 1e-6f);
+    for (int n = 0; n < maxit; ++n) {
+        const R et = tau + p + m;
+        const R inv = R(1) / et;
+        const R b2 = rmin(ss * inv * inv, bmax);
+        const R omb = R(1) - b2;
+        const R w = sizeof(R) == 8 ? (R)rsqrt((double)omb) : (R)rsqrtf((float)omb);
+        const R w2 = w * w;
+        const R X = tau + m * (R(1) - w) + p * (R(1) - w2);
+        const R de = X * omb;
+        const R f = (gm - R(1)) * de - p;
+        const R dh = m * omb * w + de + p;
+        const R den = b2 * gm * p - dh;
+        const R step = f * dh / den;
+        p = p - step;
+        iters = n + 1;
+        if (rabs(f) < tol_abs || rabs(step) <= tol_rel * rabs(p)) {
+            p_out = p;
+            w_out = w;
+            return p == p;   // false for NaN
+        }
+    }
+    return false;
+}
+
+template <bool MLP>
+__global__ void __launch_bounds__(TILE_THREADS) c2p_mixed_kernel(StageArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
+    if (ek != NO_ERROR && (uint32_t)(ek >> 48) < (uint32_t)a.stage) return;
+    MlpWeights& W = *reinterpret_cast<MlpWeights*>(smem_raw);
+    __nv_bfloat16* act = reinterpret_cast<__nv_bfloat16*>(smem_raw + sizeof(MlpWeights)) +
+                         (threadIdx.x >> 5) * MLP_ACT_ELEMS;
+    if (MLP) {
+        mlp_load(W, a.mlp);
+        __syncthreads();
+    }
+    const double gm = a.gm;
+    const float gmf = (float)gm;
+    const float high_thr = (float)(1.0 - 1.0 / (a.w_split * a.w_split));
+    unsigned long long zones = 0, it64s = 0, it32s = 0, fbs = 0;
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        const int4 t = a.tiles[tile];
+        const DevBlock& B = a.blocks[t.x];
+        const int i = t.y + threadIdx.x / TILE_Q;
+        const int j = t.z + threadIdx.x % TILE_Q;
+        const int nr = B.nr, nq = B.nq;
+        const bool active = i < nr && j < nq;
+        const int64_t n = (int64_t)nr * nq;
+        const int64_t z = (int64_t)i * nq + j;
+        double U[5] = {1.0, 0.0, 0.0, 1.0, 0.0};
+        float dV = 1.0f;
+        if (active) {
+            const double* Ub = B.buf[a.sel_in];
+#pragma unroll
+            for (int q = 0; q < 5; ++q) U[q] = Ub[q * n + z];
+            dV = B.dv_r[i] * B.dv_q[j];
+        }
+        const double m = U[0], tau = U[3];
+        const double ss = U[1] * U[1] + U[2] * U[2];
+        int kind = HYDRO_NONE;
+        if (active && m < 0.0) kind = HYDRO_NEGATIVE_DENSITY;
+        else if (active && tau < 0.0) kind = HYDRO_NEGATIVE_ENERGY_DENSITY;
+        const float mf = (float)m, tauf = (float)tau, ssf = (float)ss;
+        const float sf = sqrtf(ssf);
+        const float x1 = __fdividef(sf, mf + tauf);
+        const bool high = active && kind == HYDRO_NONE && x1 * x1 > high_thr;
+        float guess = 0.0f;
+        if (MLP) {
+            if (__any_sync(0xffffffffu, high)) {
+                float x[3];
+                const bool ok = mlp_features(m, ss, tau, x);
+                const float y = mlp_warp_infer(W, act, x);
+                const float gsv = mf * __expf(y);
+                guess = (ok && gsv > 0.0f) ? fminf(gsv, (gmf - 1.0f) * tauf) : 0.0f;
+            }
+        }
+        float P[4] = {0.f, 0.f, 0.f, 0.f};
+        float wz = 1.0f;
+        if (active && kind == HYDRO_NONE) {
+            ++zones;
+            float p32 = 0.f, w32 = 1.f;
+            int it32 = 0;
+            const bool ok32 = newton_fast<float>(mf, ssf, tauf, gmf, guess, 1e-30f, 1e-6f, 16, p32, w32, it32);
+            it32s += (unsigned long long)it32;
+            if (!high && ok32) {
+                const float inv_dv = 1.0f / dV;
+                const float inv_et = 1.0f / (tauf + mf + p32);
+                P[0] = mf / w32 * inv_dv;
+                P[1] = w32 * (float)U[1] * inv_et;
+                P[2] = w32 * (float)U[2] * inv_et;
+                P[3] = p32 * inv_dv;
+                if (p32 < 0.f) P[3] = (float)PRESSURE_FLOOR * P[0];
+            } else {
+                const double tol = NEWTON_TOLERANCE * (m + tau);
+                double p64 = 0.0, w64 = 1.0;
+                int it64 = 0;
+                bool ok = newton_fast<double>(m, ss, tau, gm, ok32 ? (double)p32 : 0.0, tol, 0.0, NEWTON_ITER_MAX,
+                                              p64, w64, it64);
+                it64s += (unsigned long long)it64;
+                if (!ok) {
+                    // fallback: the reference's iteration from the plain guess
+                    ++fbs;
+                    const double u[4] = {m, U[1], U[2], tau};
+                    double Pd[4] = {0.0, 0.0, 0.0, 0.0};
+                    double bad;
+                    int itf = 0;
+                    const int kf = srhd_c2p_newton(gm, u, 0.0, Pd, itf, bad);
+                    it64s += (unsigned long long)itf;
+                    if (kf == HYDRO_ROOT_FINDER_FAILED) {
+                        kind = kf;
+                    } else {
+                        // Pd is the (floored) primitive of the volume-integrated state
+                        const double inv_dv = 1.0 / (double)dV;
+                        P[0] = (float)(Pd[0] * inv_dv);
+                        P[1] = (float)Pd[1];
+                        P[2] = (float)Pd[2];
+                        P[3] = (float)(Pd[3] * inv_dv);
+                    }
+                } else {
+                    const double inv_dv = 1.0 / (double)dV;
+                    const double inv_et = 1.0 / (tau + m + p64);
+                    const double rho = m / w64 * inv_dv;
+                    P[0] = (float)rho;
+                    P[1] = (float)(w64 * U[1] * inv_et);
+                    P[2] = (float)(w64 * U[2] * inv_et);
+                    P[3] = p64 < 0.0 ? (float)(PRESSURE_FLOOR * rho) : (float)(p64 * inv_dv);
+                }
+            }
+        }
+        if (active) {
+            if (kind != HYDRO_NONE) {
+                atomicMin(&a.status->err_key, error_key(a.stage, t.x, i, j, kind));
+                a.status->err_sel = a.sel_in;
+            }
+            wz = sqrtf(1.0f + P[1] * P[1] + P[2] * P[2]);
+            const float v[NFIELD] = {P[0], P[1], P[2], P[3], (float)U[4] / dV / wz};
+            store_prim<float>(B, i, j, v);
+        }
+    }
+    warp_reduce_stats(a.status, zones, it64s, it32s, fbs, 0.0, false);
+}
+
+static int g_sms = 0;
+
+static int num_sms() {
+    if (!g_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms <= 0) g_sms = 1;
+    }
+    return g_sms;
+}
+
+cudaError_t launch_c2p_mixed(const StageArgs& a, cudaStream_t s) {
+    if (a.ntiles <= 0) return cudaSuccess;
+    if (a.mlp) {
+        const size_t bytes = sizeof(MlpWeights) + 8 * MLP_ACT_ELEMS * sizeof(__nv_bfloat16);
+        const int grid = std::min(a.ntiles, num_sms() * 4);
+        c2p_mixed_kernel<true><<<grid, TILE_THREADS, bytes, s>>>(a);
+    } else {
+        c2p_mixed_kernel<false><<<a.ntiles, TILE_THREADS, 0, s>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_update_mixed(const StageArgs& a, cudaStream_t s) {
+    if (a.ntiles <= 0) return cudaSuccess;
+    update_kernel<float, true><<<a.ntiles, TILE_THREADS, StageSmem<float>::bytes, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t configure_f64();
+
+cudaError_t configure_kernels() {
+    static cudaError_t result = cudaErrorNotReady;
+    if (result == cudaSuccess) return result;
+    cudaError_t e = configure_f64();
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(update_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)StageSmem<float>::bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(c2p_mixed_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(MlpWeights) + 8 * MLP_ACT_ELEMS * sizeof(__nv_bfloat16)));
+    result = e;
+    return e;
+}
+
+}  // namespace knc

@@ -87,16 +87,29 @@ __device__ __forceinline__ void srhd_side(const PhysT<R>& ph, R rho, R ur, R uq,
     S.U[0] = d;
     S.U[1] = m * ur;
     S.U[2] = m * uq;
-    S.U[3] = m * w - pre - d;
-    S.F[0] = S.U[0] * vn;
-    S.F[1] = axis == 0 ? S.U[1] * vn + pre : S.U[1] * vn;
-    S.F[2] = axis == 1 ? S.U[2] * vn + pre : S.U[2] * vn;
-    S.F[3] = (S.U[3] + pre) * vn;
     const R cs2 = ph.gm * pre / (rho * h);
     const R v2 = uu / w2;
     const R k = R(1) - cs2;
     const R a = vn * k;
-    const R b = rsqrt_(cs2 * (R(1) - v2) * (R(1) - v2 * cs2 - vn * vn * k));
+    R b;
+    if constexpr (sizeof(R) == 4) {
+        // FP32: forms without cancellation, which the reference order has for
+        // cold gas (tau = rho h W^2 - p - rho W) and for v -> 1 (1 - v^2,
+        // 1 - v^2 cs^2 - v_n^2 (1 - cs^2)):
+        //   tau = p (gh W^2 - 1) + D u^2 / (W + 1)
+        //   1 - v^2 = 1 / W^2,   1 - v^2 cs^2 - v_n^2 (1 - cs^2) = 1/W^2 + v_t^2 (1 - cs^2)
+        S.U[3] = pre * (ph.gh * w2 - R(1)) + d * uu / (w + R(1));
+        const R ut = axis == 0 ? uq : ur;
+        const R omv2 = R(1) / w2;
+        b = rsqrt_(cs2 * omv2 * (omv2 + ut * ut * omv2 * k));
+    } else {
+        S.U[3] = m * w - pre - d;
+        b = rsqrt_(cs2 * (R(1) - v2) * (R(1) - v2 * cs2 - vn * vn * k));
+    }
+    S.F[0] = S.U[0] * vn;
+    S.F[1] = axis == 0 ? S.U[1] * vn + pre : S.U[1] * vn;
+    S.F[2] = axis == 1 ? S.U[2] * vn + pre : S.U[2] * vn;
+    S.F[3] = (S.U[3] + pre) * vn;
     const R inv = R(1) / (R(1) - v2 * cs2);
     S.lm = (a - b) * inv;
     S.lp = (a + b) * inv;

@@ -45,6 +45,11 @@ KNC_MODEL_JET = 1
 KNC_MODEL_SPHERE = 2
 KNC_MODEL_HOST = 3
 
+KNC_KERNEL_GHOST = 0
+KNC_KERNEL_C2P = 1
+KNC_KERNEL_UPDATE = 2
+KNC_KERNEL_KINDS = 3
+
 KNC_MLP_HIDDEN = 64
 KNC_MLP_OFF_W1 = 0
 KNC_MLP_OFF_B1 = 192
@@ -166,6 +171,13 @@ SIGNATURES = {
     "knc_c2p_stats": (C.c_int, [_P, _I64P, _I64P, _I64P, _I64P]),
     "knc_reset_c2p_stats": (C.c_int, [_P]),
     "knc_launch_count": (C.c_int, [_P, _I64P]),
+    "knc_set_profiling": (C.c_int, [_P, C.c_int32]),
+    "knc_kernel_times": (C.c_int, [_P, _DP, _I64P]),
+    "knc_mark": (C.c_int, [_P, C.c_int32]),
+    "knc_elapsed_ms": (C.c_int, [_P, C.c_int32, C.c_int32, _DP]),
+    "knc_get_primitives": (C.c_int, [_P, C.c_int32, _DP]),
+    "knc_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
+    "knc_host_free": (C.c_int, [C.c_void_p]),
     "knc_mlp_num_params": (C.c_size_t, []),
     "knc_sample_pairs": (C.c_int, [_P, C.c_int32, _DP, C.c_int64, _I64P]),
     "knc_generate_pairs": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_double,

@@ -144,6 +144,31 @@ class Solver:
     def get_state(self, cons, scalar):
         self._check(self.lib.knc_get_state(self.h, abi.dptr(cons), abi.dptr(scalar)), "get_state")
 
+    def get_primitives(self, index: int):
+        """(rho, u_r, u_theta, p, scalar concentration) of a block, [nr, nq, 5]."""
+        out = np.empty((self.nr, self.nq, 5))
+        self._check(self.lib.knc_get_primitives(self.h, int(index), abi.dptr(out)), "get_primitives")
+        return out
+
+    def mark(self, slot: int):
+        self._check(self.lib.knc_mark(self.h, slot), "mark")
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        ms = C.c_double()
+        self._check(self.lib.knc_elapsed_ms(self.h, a, b, C.byref(ms)), "elapsed_ms")
+        return ms.value
+
+    def set_profiling(self, on: bool):
+        self._check(self.lib.knc_set_profiling(self.h, int(bool(on))), "set_profiling")
+
+    def kernel_times(self):
+        """{kind: (total ms, launches)} for ghost / c2p / update since profiling was enabled."""
+        ms = (C.c_double * abi.KNC_KERNEL_KINDS)()
+        n = (C.c_int64 * abi.KNC_KERNEL_KINDS)()
+        self._check(self.lib.knc_kernel_times(self.h, ms, n), "kernel_times")
+        names = ["ghost", "c2p", "update"]
+        return {names[k]: (ms[k], n[k]) for k in range(abi.KNC_KERNEL_KINDS)}
+
     def set_time(self, t: float, num: int = 0, den: int = 1):
         self._check(self.lib.knc_set_time(self.h, float(t), int(num), int(den)), "set_time")
 
@@ -187,6 +212,33 @@ class Solver:
         n = C.c_int64()
         self.lib.knc_launch_count(self.h, C.byref(n))
         return n.value
+
+
+class PinnedArray:
+    """A numpy view of page-locked host memory from knc_host_alloc."""
+
+    def __init__(self, shape, dtype=np.float64):
+        self.lib = abi.load()
+        n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        p = C.c_void_p()
+        st = self.lib.knc_host_alloc(n, C.byref(p))
+        if st != abi.KNC_OK:
+            raise abi.KncError(st, "knc_host_alloc failed")
+        self.ptr = p
+        buf = (C.c_char * n).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+    def free(self):
+        if self.ptr:
+            self.array = None
+            self.lib.knc_host_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 def measure_fp64_peak() -> float:

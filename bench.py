@@ -1,0 +1,414 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 finite-volume RK stage.
+
+Workload: the relativistic wind on 4096 x 1024 zones (64 radial blocks of
+64 x 1024, r in [1, 10.0008]), gamma 4/3, PLM theta 1.5, HLLE, RK2, CFL 0.4,
+seeded synthetic initial data. A step is one full RK2 step over every zone.
+
+Reported (one JSON line from rank 0):
+  value        zone-updates/s of the mixed-precision + learned-c2p-guess +
+               graph-batched path (device-timed with CUDA events around the
+               captured graphs; inputs resident in HBM)
+  fp64         the plain FP64 path on the same workload, and the FP64 pipe
+               fraction it reaches (against the FP64 FMA rate measured here)
+  l1_density   L1 error of the comoving density of the mixed path against the
+               FP64 path after the same steps (the FP64 path equals the CPU
+               oracle to 1e-12, so this is the error against the FP64 oracle)
+  roofline     the dominant kernel of the headline path: algorithmic bytes per
+               launch / its average CUDA-event duration, against measured HBM
+  e2e          the same metric through the C ABI with host buffers: every step
+               uploads the state from pinned memory, advances, downloads it
+  cpu_baseline the CPU oracle on this host's cores, bounded sample
+`--impl reference` times the CPU implementation of the path (the C++ oracle
+port; the reference's Rust crate has no toolchain here) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "app-kilonova_gb300"))
+
+METRIC = "zone-updates/s per GB300: mixed+learned vs plain FP64 GPU at L1<1e-6; HBM %"
+UNIT = "zone-updates/s"
+# algorithmic HBM bytes per zone-update of an RK2 step: 5 FP64 fields,
+# stage 1 reads U and writes U1 (80 B), stage 2 reads U1 and U0 and writes (120 B)
+ALG_BYTES_PER_ZONE_UPDATE = 200.0
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+        pg = dist
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x: float) -> float:
+    if not pg:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(workload, blocks: int, steps: int):
+    """The CPU oracle on this host's cores: `steps` RK2 steps on `blocks` blocks."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import knc_oracle
+    knc_oracle.build()
+    threads = os.cpu_count() or 1
+    w = workload
+    o = knc_oracle.Oracle(w.hydro, w.mesh, threads=threads)
+    o.set_model(w.model)
+    o.init_from_model(0.0)
+    for i in o.block_indexes()[blocks:]:
+        o.remove_block(i)
+    zones = blocks * w.mesh.block_size * w.mesh.num_polar_zones
+    o.advance(1)     # warm caches and page in
+    t0 = time.perf_counter()
+    o.advance(steps)
+    el = time.perf_counter() - t0
+    return {"value": zones * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} RK2 steps on {blocks} of {w.num_blocks} blocks ({zones} zones) of the same "
+                      f"workload, C++ FP64 oracle, {threads} threads", "seconds": el}
+
+
+def run_reference(args):
+    rank, world, local, pg = dist_setup(args.gpus)
+    if rank != 0:
+        return 0
+    from knc import workloads
+    w = workloads.wind_large()
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import knc_oracle
+    knc_oracle.build()
+    threads = os.cpu_count() or 1
+    blocks = args.ref_blocks
+    o = knc_oracle.Oracle(w.hydro, w.mesh, threads=threads)
+    o.set_model(w.model)
+    o.init_from_model(0.0)
+    for i in o.block_indexes()[blocks:]:
+        o.remove_block(i)
+    zones = blocks * w.mesh.block_size * w.mesh.num_polar_zones
+    for _ in range(args.warmup):
+        o.advance(1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.advance(1)
+    el = time.perf_counter() - t0
+    v = zones * args.steps / el
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": f"{w.name}: wind on 4096x1024 zones, SRHD, PLM 1.5, HLLE, RK2, CFL 0.4; "
+                                   f"each step one RK2 step on {blocks} of {w.num_blocks} blocks",
+                       "zones_per_step": zones},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"one RK2 step on {blocks} blocks ({zones} zones) per step; the "
+                                       "reference's Rust path cannot build here (no cargo/rustc, physics "
+                                       "crates not vendored), so this is the C++ oracle restating it"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def l1_density(a, b) -> float:
+    num = den = 0.0
+    for i in b.block_indexes():
+        pa = a.get_primitives(i)[..., 0]
+        pb = b.get_primitives(i)[..., 0]
+        num += float(abs(pa - pb).sum())
+        den += float(abs(pb).sum())
+    return num / den
+
+
+def run_knc(args):
+    import numpy as np
+    import knc
+    from knc import abi, learned, workloads
+
+    rank, world, local, pg = dist_setup(args.gpus)
+    w = workloads.wind_large(seed=1 + rank)
+    zones = w.zones
+    hbm_peak, peak_src = load_peaks()
+
+    # ---- learned guess, trained on the device (untimed)
+    t0 = time.perf_counter()
+    pairs = learned.generate_pairs(w.hydro.gamma_law_index, args.train_pairs, seed=11)
+    probe = knc.build_solver(w)
+    probe.advance(2)
+    run_pairs = learned.sample_pairs(probe, stride=16)
+    probe.close()
+    weights, train_loss = learned.train(np.concatenate([pairs, run_pairs]), steps=args.train_steps, seed=11)
+    train_s = time.perf_counter() - t0
+
+    def make(mixed: bool, guess: bool, graph: bool):
+        s = knc.build_solver(w)
+        if mixed:
+            s.set_precision(abi.KNC_PRECISION_MIXED)
+            s.set_mixed_w_split(args.w_split)
+        if guess:
+            s.set_c2p_guess(abi.KNC_GUESS_MLP, weights)
+        s.set_batched(graph)
+        return s
+
+    def timed(s, steps, fold):
+        for _ in range(args.warmup):
+            s.advance(1)
+        s.synchronize()
+        barrier(pg)
+        l0 = s.launch_count()
+        s.mark(0)
+        done = 0
+        while done < steps:
+            f = min(fold, steps - done)
+            s.advance(f)
+            done += f
+        s.mark(1)
+        ms = s.elapsed_ms(0, 1)
+        return ms, s.launch_count() - l0
+
+    # ---- plain FP64 path
+    fp64 = make(False, False, False)
+    fp64.reset_c2p_stats()
+    ms64, _ = timed(fp64, args.steps, args.fold)
+    st64 = fp64.c2p_stats()
+    ms64 = max_over_ranks(pg, ms64)
+    v64 = zones * args.steps * world / (ms64 * 1e-3)
+    fp64_peak = knc.measure_fp64_peak()
+
+    # ---- headline: mixed + learned + graph
+    clocks = ClockSampler(local)
+    head = make(True, True, True)
+    head.reset_c2p_stats()
+    clocks.start()
+    msh, launches = timed(head, args.steps, args.fold)
+    clk = clocks.stop()
+    sth = head.c2p_stats()
+    msh = max_over_ranks(pg, msh)
+    value = zones * args.steps * world / (msh * 1e-3)
+    l1 = l1_density(head, fp64)
+
+    # ---- same path without the graph, kernels timed with events (roofline)
+    prof = make(True, True, False)
+    for _ in range(args.warmup):
+        prof.advance(1)
+    prof.set_profiling(True)
+    prof.advance(args.steps)
+    kt = prof.kernel_times()
+    prof.set_profiling(False)
+    prof.close()
+    dom = max(kt, key=lambda k: kt[k][0])
+    dom_ms = kt[dom][0] / max(kt[dom][1], 1)
+    # one launch of a stage kernel processes one stage of every zone: half of
+    # an RK2 zone-update's algorithmic bytes
+    alg_bytes = ALG_BYTES_PER_ZONE_UPDATE * zones / 2.0
+    achieved = alg_bytes / (dom_ms * 1e-3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get(dom)
+        except ValueError:
+            traffic = None
+
+    # ---- end to end through the C ABI with host buffers
+    nb = w.num_blocks
+    cons = knc.solver.PinnedArray((nb, w.mesh.block_size, w.mesh.num_polar_zones, 4))
+    scal = knc.solver.PinnedArray((nb, w.mesh.block_size, w.mesh.num_polar_zones))
+    head.get_state(cons.array, scal.array)
+    for _ in range(args.warmup):
+        head.set_state(cons.array, scal.array)
+        head.advance(1)
+        head.get_state(cons.array, scal.array)
+    barrier(pg)
+    head.mark(2)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        head.set_state(cons.array, scal.array)
+        head.advance(1)
+        head.get_state(cons.array, scal.array)
+    wall = time.perf_counter() - t0
+    head.mark(3)
+    e2e_ms = max_over_ranks(pg, max(head.elapsed_ms(2, 3), wall * 1e3))
+    e2e = zones * args.steps * world / (e2e_ms * 1e-3)
+    h2d = cons.array.nbytes + scal.array.nbytes
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(w, args.cpu_blocks, args.cpu_steps)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": msh / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 state+recovery / f32 flux",
+            "data": "synthetic",
+            "config": {"workload": f"{w.name}: relativistic wind, 4096x1024 zones in 64 blocks of 64x1024, "
+                                   "gamma 4/3, PLM theta 1.5, HLLE, RK2, CFL 0.4",
+                       "zones": zones, "path": f"mixed precision (FP64 recovery above W={args.w_split}), "
+                                               "learned c2p guess, CUDA graph per fold",
+                       "fold": args.fold, "l2": "state 168 MB per buffer > 129 MB L2 (no flush needed)",
+                       "parallelism": f"replicas x{world}"},
+            "fp64": {"value": v64, "ms_per_step": ms64 / args.steps,
+                     "newton_iters_per_zone": st64["iters_fp64"] / max(st64["zones"], 1),
+                     "fp64_peak_gflops": fp64_peak},
+            "speedup_vs_fp64": value / v64,
+            "l1_density": l1,
+            "c2p": {"fp64_iters_per_zone": sth["iters_fp64"] / max(sth["zones"], 1),
+                    "fp32_iters_per_zone": sth["iters_fp32"] / max(sth["zones"], 1),
+                    "fallbacks": sth["fallbacks"], "mlp_train_loss": train_loss, "mlp_train_s": train_s},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+                         "peak_source": peak_src, "avg_launch_ms": dom_ms,
+                         "kernel_ms": {k: v[0] / max(v[1], 1) for k, v in kt.items()}},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d},
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        if cpu:
+            line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.destroy_process_group()
+    return 0
+
+
+def run_only(args):
+    """One path alone on the workload, for profiler captures: warmup + steps."""
+    import knc
+    from knc import abi, learned, workloads
+    w = workloads.wind_large()
+    s = knc.build_solver(w)
+    if args.only == "mixed":
+        s.set_precision(abi.KNC_PRECISION_MIXED)
+        s.set_mixed_w_split(args.w_split)
+        if args.train_steps > 0:
+            pairs = learned.generate_pairs(w.hydro.gamma_law_index, args.train_pairs, seed=11)
+            weights, _ = learned.train(pairs, steps=args.train_steps, seed=11)
+            s.set_c2p_guess(abi.KNC_GUESS_MLP, weights)
+    for _ in range(args.warmup):
+        s.advance(1)
+    s.mark(0)
+    s.advance(args.steps)
+    s.mark(1)
+    ms = s.elapsed_ms(0, 1)
+    print(json.dumps({"only": args.only, "zones": w.zones, "steps": args.steps,
+                      "value": w.zones * args.steps / (ms * 1e-3), "ms_per_step": ms / args.steps}), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="knc", choices=["knc", "reference"])
+    ap.add_argument("--fold", type=int, default=10)
+    ap.add_argument("--w-split", type=float, default=2.0)
+    ap.add_argument("--train-pairs", type=int, default=2_000_000)
+    ap.add_argument("--train-steps", type=int, default=3000)
+    ap.add_argument("--cpu-blocks", type=int, default=16)
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--ref-blocks", type=int, default=8)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only", choices=["fp64", "mixed"], default=None,
+                    help="run one path alone (profiler captures)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.only:
+        return run_only(args)
+    return run_knc(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -178,6 +178,11 @@ int knc_block_shape(const knc_ctx* ctx, int64_t* nr, int64_t* nq);
 int knc_set_state(knc_ctx* ctx, const double* cons_aos, const double* scalar_mass);
 int knc_get_state(knc_ctx* ctx, double* cons_aos, double* scalar_mass);
 
+/* Primitives of one block recovered in FP64 from the live state, the data
+ * `Products::try_from_state` exports (src/products.rs:43-66): [nr][nq][5] as
+ * (rho, u_r, u_theta, p, scalar concentration). */
+int knc_get_primitives(knc_ctx* ctx, int32_t index, double* prim);
+
 /* State.time and State.iteration (Rational64 as num/den), src/state.rs:39-43 */
 int knc_set_time(knc_ctx* ctx, double time, int64_t iter_num, int64_t iter_den);
 int knc_get_time(const knc_ctx* ctx, double* time, int64_t* iter_num,
@@ -216,6 +221,23 @@ int knc_reset_c2p_stats(knc_ctx* ctx);
 /* Kernel launches issued by the context since creation. */
 int knc_launch_count(const knc_ctx* ctx, int64_t* launches);
 
+/* Per-kernel timing with CUDA events on the context's stream. While enabled,
+ * every launch is bracketed by events; knc_kernel_times returns, per kind
+ * (KNC_KERNEL_*), the summed milliseconds and launch counts since enabling.
+ * Not available while the steps run as a CUDA graph. */
+enum { KNC_KERNEL_GHOST = 0, KNC_KERNEL_C2P = 1, KNC_KERNEL_UPDATE = 2, KNC_KERNEL_KINDS = 3 };
+int knc_set_profiling(knc_ctx* ctx, int32_t on);
+int knc_kernel_times(knc_ctx* ctx, double* ms, int64_t* launches);
+
+/* Events on the context's stream: knc_mark records slot (0..7);
+ * knc_elapsed_ms waits for slot b and returns the time from slot a to b. */
+int knc_mark(knc_ctx* ctx, int32_t slot);
+int knc_elapsed_ms(knc_ctx* ctx, int32_t a, int32_t b, double* ms);
+
+/* Page-locked host buffers for host-resident drivers (cudaHostAlloc). */
+int knc_host_alloc(size_t bytes, void** ptr);
+int knc_host_free(void* ptr);
+
 /* ---- learned c2p guess: MLP 3 -> 64 -> 64 -> 1 (SiLU) ------------------ */
 /*
  * Packed float layout (offsets in floats):
@@ -226,7 +248,10 @@ int knc_launch_count(const knc_ctx* ctx, int64_t* launches);
  * Forward: xn = (x - x_mean) * x_scale; h1 = silu(bf16(W1) xn + b1);
  * h2 = silu(bf16(W2) bf16(h1) + b2) with FP32 accumulation;
  * y = bf16(W3) . h2 + b3. The target is log(p / D); the pressure guess is
- * D * exp(y). Inputs x = (log D, |S| / (D + tau), log(tau / D)).
+ * D * exp(y), clamped to (0, (gamma - 1) tau]. Inputs, all invariant under
+ * U -> k U: x = (log(tau / D), -log(1 - |S| / (D + tau)),
+ * log((tau (tau + 2 D) - S^2) / D^2)); the last is E^2 - S^2 - D^2 (E = tau + D),
+ * which keeps the pressure resolvable in cold, highly relativistic states.
  */
 #define KNC_MLP_HIDDEN 64
 #define KNC_MLP_OFF_W1 0
@@ -273,7 +298,8 @@ int knc_mlp_train(const double* pairs, int64_t n, float* weights,
 int knc_mlp_forward_backward(const float* weights, const float* x, const float* y,
                              int32_t n, float* pred, float* loss, float* grad);
 
-/* Features of a conserved state (log D, |S|/(D+tau), log tau/D). */
+/* Features of a conserved state (see the MLP layout above); zeros when the
+ * state has no usable features (the plain guess then applies). */
 void knc_mlp_features(const double u[4], float out[3]);
 
 /* ---- utilities --------------------------------------------------------- */

@@ -1222,14 +1222,15 @@ inline double sigmoid(double z) { return 1.0 / (1.0 + std::exp(-z)); }
 }  // namespace
 
 extern "C" void oracle_mlp_forward_backward(const float* w, const float* x, const float* y, int32_t n,
-                                            double* pred, double* loss, double* grad) {
+                                            int32_t round_bf16, double* pred, double* loss, double* grad) {
+    auto rnd = [round_bf16](float v) { return round_bf16 ? bf16_round(v) : v; };
     constexpr int H = KNC_MLP_HIDDEN;
     std::vector<double> g(KNC_MLP_NUM_PARAMS, 0.0);
     double W1[H][3], W2[H][H], W3[H];
     for (int u = 0; u < H; ++u) {
-        for (int k = 0; k < 3; ++k) W1[u][k] = bf16_round(w[KNC_MLP_OFF_W1 + u * 3 + k]);
-        for (int v = 0; v < H; ++v) W2[u][v] = bf16_round(w[KNC_MLP_OFF_W2 + u * H + v]);
-        W3[u] = bf16_round(w[KNC_MLP_OFF_W3 + u]);
+        for (int k = 0; k < 3; ++k) W1[u][k] = rnd(w[KNC_MLP_OFF_W1 + u * 3 + k]);
+        for (int v = 0; v < H; ++v) W2[u][v] = rnd(w[KNC_MLP_OFF_W2 + u * H + v]);
+        W3[u] = rnd(w[KNC_MLP_OFF_W3 + u]);
     }
     double L = 0.0;
     for (int32_t r = 0; r < n; ++r) {
@@ -1241,7 +1242,7 @@ extern "C" void oracle_mlp_forward_backward(const float* w, const float* x, cons
             for (int k = 0; k < 3; ++k) z += W1[u][k] * xn[k];
             z1[u] = z;
             s1[u] = sigmoid(z);
-            a1[u] = bf16_round((float)(z * s1[u]));
+            a1[u] = round_bf16 ? (double)bf16_round((float)(z * s1[u])) : z * s1[u];
         }
         double out = w[KNC_MLP_OFF_B3];
         for (int u = 0; u < H; ++u) {

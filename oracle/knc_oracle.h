@@ -75,9 +75,12 @@ int oracle_block_geometry(const knc_mesh_params* m, int32_t index, double* rv, d
 
 /* ---- learned c2p guess: CPU reference of the MLP (FP64) ---------------- */
 /* Forward + backward of the packed MLP on n rows; grad has knc_mlp_num_params
- * entries. Weights are rounded to bfloat16 first, as the device does. */
+ * entries. With round_bf16 != 0 the weights and the first hidden layer's
+ * activations are rounded to bfloat16 as the device does (gradients are
+ * straight-through); with 0 everything stays FP64, for finite differences. */
 void oracle_mlp_forward_backward(const float* weights, const float* x, const float* y,
-                                 int32_t n, double* pred, double* loss, double* grad);
+                                 int32_t n, int32_t round_bf16, double* pred, double* loss,
+                                 double* grad);
 
 #ifdef __cplusplus
 }

@@ -64,7 +64,7 @@ def load():
         "oracle_max_signal_speed": (C.c_double, [C.POINTER(abi.HydroParams), DP]),
         "oracle_block_geometry": (C.c_int, [C.POINTER(abi.MeshParams), C.c_int32, DP, DP, DP, DP, DP, DP, DP]),
         "oracle_mlp_forward_backward": (None, [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
-                                               C.c_int32, DP, DP, DP]),
+                                               C.c_int32, C.c_int32, DP, DP, DP]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -243,7 +243,7 @@ def block_geometry(mp, index):
     return out
 
 
-def mlp_forward_backward(weights, x, y):
+def mlp_forward_backward(weights, x, y, round_bf16=True):
     lib = load()
     weights = np.ascontiguousarray(weights, dtype=np.float32)
     x = np.ascontiguousarray(x, dtype=np.float32)
@@ -254,5 +254,6 @@ def mlp_forward_backward(weights, x, y):
     grad = np.empty(len(weights))
     fp = C.POINTER(C.c_float)
     lib.oracle_mlp_forward_backward(weights.ctypes.data_as(fp), x.ctypes.data_as(fp),
-                                    y.ctypes.data_as(fp), n, _d(pred), C.byref(loss), _d(grad))
+                                    y.ctypes.data_as(fp), n, int(bool(round_bf16)), _d(pred), C.byref(loss),
+                                    _d(grad))
     return pred, loss.value, grad

@@ -18,3 +18,13 @@ def oracle_lib():
     import knc_oracle
     knc_oracle.build()
     return knc_oracle.load()
+
+
+@pytest.fixture(scope="session")
+def trained_mlp():
+    """Learned c2p guess trained on the device once per session (1M solver
+    pairs over W in [1, 1000], p/rho in [1e-6, 1e2])."""
+    from knc import learned
+    pairs = learned.generate_pairs(4.0 / 3.0, 1_000_000, seed=21)
+    w, loss = learned.train(pairs, steps=3000, seed=21)
+    return w, loss

@@ -1,0 +1,97 @@
+"""The mixed-precision stage: FP32 reconstruction / flux / sources, FP64
+state accumulation and FP64 recovery above the Lorentz-factor split.
+Accuracy is reported per field against the FP64 oracle (L1 relative to the
+field's L1 norm, and max difference relative to the field's max)."""
+import numpy as np
+import pytest
+
+from helpers import field_errors, make_pair
+
+pytestmark = pytest.mark.gpu
+
+
+def l1_errors(a, b):
+    out = []
+    for q in range(5):
+        num = den = 0.0
+        for k in b:
+            x = a[k][0][..., q] if q < 4 else a[k][1]
+            y = b[k][0][..., q] if q < 4 else b[k][1]
+            num += float(np.abs(x - y).sum())
+            den += float(np.abs(y).sum())
+        out.append(num / den if den else num)
+    return out
+
+
+def _mixed_vs_oracle(workload, steps, w_split=2.0):
+    from knc import abi
+    g, o = make_pair(workload)
+    g.set_precision(abi.KNC_PRECISION_MIXED)
+    g.set_mixed_w_split(w_split)
+    g.advance(steps)
+    o.advance(steps)
+    return g, o, l1_errors(g.state(), o.state()), field_errors(g.state(), o.state())
+
+
+def test_wind_l1_density_below_1e6():
+    from knc import workloads
+    w = workloads.wind_small()
+    g, o, l1, linf = _mixed_vs_oracle(w, w.steps)
+    print("wind L1", l1, "max", linf)
+    for q in (0, 1, 3):            # D, S_r, tau (S_theta and the scalar are ~0 here)
+        assert l1[q] <= 1e-6, (q, l1)
+        assert linf[q] <= 1e-5, (q, linf)
+    assert g.time() == o.time()
+
+
+def test_jet_errors_bounded():
+    from knc import workloads
+    w = workloads.jet_small()
+    g, o, l1, linf = _mixed_vs_oracle(w, w.steps)
+    print("jet L1", l1, "max", linf)
+    assert l1[0] <= 1e-5, l1
+    assert max(linf) <= 5e-3, linf
+
+
+def test_w_split_selects_recovery_precision():
+    from knc import abi, workloads
+    w = workloads.wind_small()
+    g, _ = make_pair(w, gpu=True)
+    g.set_precision(abi.KNC_PRECISION_MIXED)
+    g.set_mixed_w_split(1.0)          # every zone recovers in FP64
+    g.reset_c2p_stats()
+    g.advance(2)
+    st = g.c2p_stats()
+    assert st["iters_fp64"] >= st["zones"]
+    g.set_mixed_w_split(1e9)          # every zone recovers in FP32
+    g.reset_c2p_stats()
+    g.advance(2)
+    st = g.c2p_stats()
+    assert st["iters_fp64"] == 0 and st["iters_fp32"] > 0
+
+
+def test_mixed_graph_equals_mixed_stream():
+    from knc import abi, workloads
+    w = workloads.wind_small()
+    a, _ = make_pair(w, gpu=True)
+    b, _ = make_pair(w, gpu=True)
+    for s in (a, b):
+        s.set_precision(abi.KNC_PRECISION_MIXED)
+    b.set_batched(True)
+    a.advance(6)
+    b.advance(3)
+    b.advance(3)
+    sa, sb = a.state(), b.state()
+    for k in sa:
+        assert np.array_equal(sa[k][0], sb[k][0]) and np.array_equal(sa[k][1], sb[k][1])
+    assert a.time() == b.time()
+
+
+def test_fp64_graph_bitwise():
+    from knc import workloads
+    w = workloads.wind_small()
+    g, o = make_pair(w)
+    g.set_batched(True)
+    g.advance(5)
+    o.advance(5)
+    assert max(field_errors(g.state(), o.state())) == 0.0

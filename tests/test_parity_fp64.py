@@ -1,7 +1,9 @@
 """FP64 GPU path vs the CPU oracle on the same seeded inputs.
 
-Tolerance: 1e-12 relative per conserved field (the plain FP64 path must match
-the CPU path to <= 1e-12 after 100 steps). Both sides compute every
+Tolerance: 1e-12 relative per conserved field, measured as the largest zone
+difference over the field's largest magnitude on the grid (S_theta passes
+through zero, so a per-zone ratio is not meaningful for it). The plain FP64
+path must match the CPU path to that level after 100 steps. Both sides compute every
 expression in the same order without FMA contraction, so differences come
 only from the libm calls in the geometry (computed once on the host for both)
 and are expected to be zero.
@@ -36,7 +38,7 @@ def test_wind_100_steps():
     from knc import workloads
     w = workloads.wind_small()
     g, o = _run(w, w.steps, fold=10)
-    errs = zone_relative_errors(g.state(), o.state())
+    errs = field_errors(g.state(), o.state())
     assert max(errs) <= TOL, errs
     assert g.time() == o.time()
 
@@ -47,7 +49,7 @@ def test_newtonian_sphere(riemann):
     w = workloads.sphere_small(riemann=riemann)
     g, o = _run(w, 20, fold=5)
     assert g.time_step() == o.time_step()
-    errs = zone_relative_errors(g.state(), o.state())
+    errs = field_errors(g.state(), o.state())
     assert max(errs) <= TOL, errs
 
 
@@ -55,7 +57,7 @@ def test_jet_small():
     from knc import workloads
     w = workloads.jet_small()
     g, o = _run(w, 50, fold=10)
-    errs = zone_relative_errors(g.state(), o.state())
+    errs = field_errors(g.state(), o.state())
     assert max(errs) <= TOL, errs
 
 
@@ -65,20 +67,40 @@ def test_rk_orders(order):
     w = workloads.wind_small()
     w.hydro.runge_kutta_order = order
     g, o = _run(w, 10, fold=5)
-    errs = zone_relative_errors(g.state(), o.state())
+    errs = field_errors(g.state(), o.state())
     assert max(errs) <= TOL, errs
     assert g.time() == o.time()
 
 
 def test_srhd_hllc_adaptive():
     from knc import workloads
-    w = workloads.jet_small()
+    w = workloads.wind_small()
     w.hydro.riemann_solver = "HLLC"
     w.hydro.adaptive_time_step = True
     g, o = _run(w, 10, fold=5)
     assert g.time_step() == o.time_step()
-    errs = zone_relative_errors(g.state(), o.state())
+    errs = field_errors(g.state(), o.state())
     assert max(errs) <= TOL, errs
+
+
+def test_jet_adaptive_fails_like_the_oracle():
+    """The adaptive step only sees interior signal speeds (src/state.rs:151-160),
+    so the W = 100 inflow through the ghost block overruns it: both paths must
+    fail in the same stage at the same zone with the same kind."""
+    import knc
+    from knc import workloads
+    w = workloads.jet_small()
+    w.hydro.adaptive_time_step = True
+    g, o = make_pair(w)
+    assert g.time_step() == o.time_step()
+    st = o.try_advance(5)
+    assert st == 5
+    eo = o.last_error()
+    with pytest.raises(knc.HydroError) as exc:
+        g.advance(5)
+    e = exc.value.error
+    assert (e["block"], e["i"], e["j"]) == (eo.block, eo.i, eo.j)
+    assert e["kind"] == knc.abi.HYDRO_ERROR_NAMES[eo.kind]
 
 
 def test_same_inputs_through_add_block():
@@ -94,7 +116,7 @@ def test_same_inputs_through_add_block():
     assert g.block_indexes() == o.block_indexes()
     g.advance(3)
     o.advance(3)
-    assert max(zone_relative_errors(g.state(), o.state())) <= TOL
+    assert max(field_errors(g.state(), o.state())) <= TOL
 
 
 def test_state_roundtrip():
