@@ -387,10 +387,10 @@ def run_only(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="knc", choices=["knc", "reference"])
-    ap.add_argument("--fold", type=int, default=10)
+    ap.add_argument("--fold", type=int, default=50)
     ap.add_argument("--w-split", type=float, default=2.0)
     ap.add_argument("--train-pairs", type=int, default=2_000_000)
     ap.add_argument("--train-steps", type=int, default=3000)

@@ -49,7 +49,11 @@ def test_learned_guess_needs_fewer_iterations(trained_mlp):
         kind_p, prim_p, a = knc_oracle.cons_to_prim(hp, u, -1.0)
         kind_l, prim_l, b = knc_oracle.cons_to_prim(hp, u, guess)
         assert kind_p == kind_l
-        assert np.allclose(prim_p, prim_l, rtol=1e-9, atol=1e-12 * (u[0] + u[3]))
+        # both stop at |f| < 1e-12 (D + tau); at Lorentz factor W that residual
+        # fixes the velocity only to about W^2 1e-12 and p to 1e-12 (D + tau)
+        w2 = 1.0 + prim_p[1] ** 2 + prim_p[2] ** 2
+        assert np.allclose(prim_p[:3], prim_l[:3], rtol=1e-11 * w2 + 1e-12, atol=0.0)
+        assert abs(prim_p[3] - prim_l[3]) <= 1e-11 * (u[0] + u[3])
         it_plain.append(a)
         it_learn.append(b)
     gain = np.mean(it_plain) - np.mean(it_learn)
@@ -72,7 +76,8 @@ def test_fp64_path_with_learned_guess(trained_mlp):
     b.reset_c2p_stats()
     a.advance(20)
     b.advance(20)
-    assert max(field_errors(a.state(), b.state())) <= 1e-9
+    # W = 100 in the nozzle: the 1e-12 residual fixes primitives to ~W^2 1e-12
+    assert max(field_errors(a.state(), b.state())) <= 1e-7
     sa, sb = a.c2p_stats(), b.c2p_stats()
     ia, ib = sa["iters_fp64"] / sa["zones"], sb["iters_fp64"] / sb["zones"]
     print(f"FP64 path iterations per zone: plain {ia:.3f} learned {ib:.3f} fallbacks {sb['fallbacks']}")
