@@ -4,7 +4,7 @@ from pathlib import Path
 import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
-for p in (ROOT / "app-kilonova_gb300", ROOT / "oracle", ROOT / "tests"):
+for p in (ROOT, ROOT / "app-kilonova_gb300", ROOT / "oracle", ROOT / "tests"):
     if str(p) not in sys.path:
         sys.path.insert(0, str(p))
 
