@@ -198,6 +198,21 @@ def run_reference(args):
     return 0
 
 
+# ncu summaries of the mixed-stage kernels on this workload (one capture each)
+PROFILE_OF = {"update": "update_kernel_mixed_wind_4096x1024.md", "c2p": "c2p_mixed_wind_4096x1024.md"}
+
+
+def profiled_traffic(kernel: str):
+    """DRAM bytes (read + write) of one launch from the committed ncu summary."""
+    f = ROOT / "profiles" / PROFILE_OF.get(kernel, "")
+    if not f.is_file():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch"):
+            return int(line.split("=")[1])
+    return None
+
+
 def l1_density(a, b) -> float:
     num = den = 0.0
     for i in b.block_indexes():
@@ -290,13 +305,7 @@ def run_knc(args):
     # an RK2 zone-update's algorithmic bytes
     alg_bytes = ALG_BYTES_PER_ZONE_UPDATE * zones / 2.0
     achieved = alg_bytes / (dom_ms * 1e-3) / 1e9
-    traffic = None
-    tf = ROOT / "profiles" / "traffic.json"
-    if tf.exists():
-        try:
-            traffic = json.loads(tf.read_text()).get(dom)
-        except ValueError:
-            traffic = None
+    traffic = profiled_traffic(dom)
 
     # ---- end to end through the C ABI with host buffers
     nb = w.num_blocks
