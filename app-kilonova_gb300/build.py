@@ -28,6 +28,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
           "--expt-relaxed-constexpr", f"-I{INCLUDE}"]
 PER_FILE = {
     "knc_f64.cu": ["--fmad=false"],
+    "knc_noalloc.cu": ["--fmad=false"],
 }
 
 

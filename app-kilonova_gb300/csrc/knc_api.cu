@@ -934,6 +934,18 @@ int create_device_side(knc_ctx* c) {
 
 }  // namespace
 
+namespace knc {
+void host_block_volumes(const knc_mesh_params& mesh, int32_t index, std::vector<double>& dv,
+                        std::vector<double>& rc, std::vector<double>& qc) {
+    MeshH M;
+    M.p = mesh;
+    GeomH G = make_geometry(M, index, false);
+    dv.swap(G.dv);
+    rc.swap(G.rc);
+    qc.swap(G.qc);
+}
+}  // namespace knc
+
 // =========================================================================== C ABI
 extern "C" {
 

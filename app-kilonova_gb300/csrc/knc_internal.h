@@ -17,6 +17,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "../../include/knc.h"
 
 namespace knc {
@@ -129,6 +131,11 @@ struct InitArgs {
     knc_model_params model;
     const double* host_prim;     // [nzones][5] host model values (HOST model) or null
 };
+
+// Host geometry of block `index` (src/mesh.rs formulas): cell volumes
+// [nr*nq], centroid radius per row [nr], centroid theta per column [nq].
+void host_block_volumes(const knc_mesh_params& mesh, int32_t index, std::vector<double>& dv,
+                        std::vector<double>& rc, std::vector<double>& qc);
 
 // ---- launchers (each returns the cudaError_t of the launch) -------------
 // Set the kernels' shared-memory attributes once, before any launch or capture.

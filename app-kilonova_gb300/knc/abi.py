@@ -60,6 +60,7 @@ KNC_MLP_OFF_B3 = 4480
 KNC_MLP_OFF_XMEAN = 4481
 KNC_MLP_OFF_XSCALE = 4484
 KNC_MLP_NUM_PARAMS = 4487
+KNC_NOALLOC_MAX_ZONES = 131072
 
 HYDRO_ERROR_NAMES = {
     KNC_HYDRO_NONE: "None",
@@ -186,6 +187,8 @@ SIGNATURES = {
     "knc_mlp_forward_backward": (C.c_int, [_FP, _FP, _FP, C.c_int32, _FP, _FP, _FP]),
     "knc_mlp_features": (None, [_DP, _FP]),
     "knc_measure_fp64_peak": (C.c_int, [_DP]),
+    "knc_recover_primitives_noalloc": (C.c_int, [C.POINTER(HydroParams), C.POINTER(MeshParams), C.c_int32,
+                                                 _P, _P, _P, _P, C.POINTER(Error)]),
 }
 
 

@@ -302,6 +302,33 @@ int knc_mlp_forward_backward(const float* weights, const float* x, const float* 
  * state has no usable features (the plain guess then applies). */
 void knc_mlp_features(const double u[4], float out[3]);
 
+/* ---- primitive recovery without device allocation ----------------------
+ * No counterpart in the reference. For callers that own all device memory
+ * themselves and cannot let a library call cudaMalloc: a host whose pool or
+ * caching allocator holds the whole GPU (a library cudaMalloc could fail or
+ * fragment it), or a time-critical loop that cannot take cudaMalloc's
+ * implicit device synchronisation. Same result as knc_get_primitives, bit
+ * for bit, from caller-owned device buffers:
+ *   d_cons   [block_size][num_polar_zones][4] volume-integrated conserved
+ *   d_scalar [block_size][num_polar_zones] scalar mass
+ *   d_prim   [block_size][num_polar_zones][5] out: rho, u_r, u_theta, p,
+ *            scalar concentration
+ * for block (block_index, 0) of `mesh`, on `stream` (a cudaStream_t; NULL
+ * for the default stream). Its only working memory is a fixed per-device
+ * array inside the library (KNC_NOALLOC_MAX_ZONES cell volumes plus a status
+ * word, 1 MiB; every GPU that loads the library holds it until the process
+ * exits). Blocks larger than KNC_NOALLOC_MAX_ZONES zones are rejected with
+ * KNC_ERR_INVALID_ARGUMENT. The first call on a device resolves that array's
+ * address; make it before any stream capture. Calls share the array, so
+ * calls whose GPU work overlaps race on it: serialise them. Returns after
+ * synchronising `stream`; a failing zone gives KNC_ERR_HYDRO with `err`
+ * (optional) filled like knc_last_error. */
+#define KNC_NOALLOC_MAX_ZONES 131072
+int knc_recover_primitives_noalloc(const knc_hydro_params* hydro, const knc_mesh_params* mesh,
+                                   int32_t block_index, const double* d_cons,
+                                   const double* d_scalar, double* d_prim, void* stream,
+                                   knc_error* err);
+
 /* ---- utilities --------------------------------------------------------- */
 
 /* Measured FP64 FMA throughput of the current device (GFLOP/s, 2/FMA). */
