@@ -15,6 +15,7 @@
 // The recovery is scale-invariant (U -> k U gives p -> k p), so it runs on the
 // volume-integrated state and divides rho and p by dV afterwards: no FP64
 // divisions by the cell volume.
+#include "knc_bits.cuh"
 #include "knc_internal.h"
 #include "knc_mlp.cuh"
 #include "knc_physics.cuh"
@@ -57,7 +58,7 @@ __device__ __forceinline__ bool newton_fast(R m, R ss, R tau, R gm, R p, R tol_a
 }
 
 template <bool MLP>
-__global__ void __launch_bounds__(TILE_THREADS) c2p_mixed_kernel(StageArgs a) {
+__global__ void __launch_bounds__(TILE_THREADS, MLP ? 2 : 3) c2p_mixed_kernel(StageArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
     if (ek != NO_ERROR && (uint32_t)(ek >> 48) < (uint32_t)a.stage) return;
@@ -90,11 +91,12 @@ __global__ void __launch_bounds__(TILE_THREADS) c2p_mixed_kernel(StageArgs a) {
             dV = B.dv_r[i] * B.dv_q[j];
         }
         const double m = U[0], tau = U[3];
-        const double ss = U[1] * U[1] + U[2] * U[2];
         int kind = HYDRO_NONE;
-        if (active && m < 0.0) kind = HYDRO_NEGATIVE_DENSITY;
-        else if (active && tau < 0.0) kind = HYDRO_NEGATIVE_ENERGY_DENSITY;
-        const float mf = (float)m, tauf = (float)tau, ssf = (float)ss;
+        if (active && is_negative(m)) kind = HYDRO_NEGATIVE_DENSITY;
+        else if (active && is_negative(tau)) kind = HYDRO_NEGATIVE_ENERGY_DENSITY;
+        // FP32 copies by integer conversion (no FP64-pipe instructions)
+        const float mf = d2f_rn(m), tauf = d2f_rn(tau), s1f = d2f_rn(U[1]), s2f = d2f_rn(U[2]);
+        const float ssf = s1f * s1f + s2f * s2f;
         const float sf = sqrtf(ssf);
         const float x1 = __fdividef(sf, mf + tauf);
         const bool high = active && kind == HYDRO_NONE && x1 * x1 > high_thr;
@@ -102,7 +104,7 @@ __global__ void __launch_bounds__(TILE_THREADS) c2p_mixed_kernel(StageArgs a) {
         if (MLP) {
             if (__any_sync(0xffffffffu, high)) {
                 float x[3];
-                const bool ok = mlp_features(m, ss, tau, x);
+                const bool ok = mlp_features(m, U[1] * U[1] + U[2] * U[2], tau, x);
                 const float y = mlp_warp_infer(W, act, x);
                 const float gsv = mf * __expf(y);
                 guess = (ok && gsv > 0.0f) ? fminf(gsv, (gmf - 1.0f) * tauf) : 0.0f;
@@ -120,11 +122,12 @@ __global__ void __launch_bounds__(TILE_THREADS) c2p_mixed_kernel(StageArgs a) {
                 const float inv_dv = 1.0f / dV;
                 const float inv_et = 1.0f / (tauf + mf + p32);
                 P[0] = mf / w32 * inv_dv;
-                P[1] = w32 * (float)U[1] * inv_et;
-                P[2] = w32 * (float)U[2] * inv_et;
+                P[1] = w32 * s1f * inv_et;
+                P[2] = w32 * s2f * inv_et;
                 P[3] = p32 * inv_dv;
                 if (p32 < 0.f) P[3] = (float)PRESSURE_FLOOR * P[0];
             } else {
+                const double ss = U[1] * U[1] + U[2] * U[2];
                 const double tol = NEWTON_TOLERANCE * (m + tau);
                 double p64 = 0.0, w64 = 1.0;
                 int it64 = 0;
@@ -167,7 +170,7 @@ __global__ void __launch_bounds__(TILE_THREADS) c2p_mixed_kernel(StageArgs a) {
                 a.status->err_sel = a.sel_in;
             }
             wz = sqrtf(1.0f + P[1] * P[1] + P[2] * P[2]);
-            const float v[NFIELD] = {P[0], P[1], P[2], P[3], (float)U[4] / dV / wz};
+            const float v[NFIELD] = {P[0], P[1], P[2], P[3], d2f_rn(U[4]) / dV / wz};
             store_prim<float>(B, i, j, v);
         }
     }

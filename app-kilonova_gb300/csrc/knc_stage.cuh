@@ -16,6 +16,7 @@
 // written once, so the output may alias the input or the RK base buffer.
 #pragma once
 
+#include "knc_bits.cuh"
 #include "knc_internal.h"
 #include "knc_physics.cuh"
 
@@ -47,7 +48,7 @@ __device__ __forceinline__ PhysT<R> make_phys(const StageArgs& a) {
 }
 
 template <class R, bool MIXED>
-__global__ void __launch_bounds__(TILE_THREADS) update_kernel(StageArgs a) {
+__global__ void __launch_bounds__(TILE_THREADS, MIXED ? 4 : 1) update_kernel(StageArgs a) {
     using S = StageSmem<R>;
     constexpr int TR = S::TR, TQ = S::TQ, PR = S::PR, PQ = S::PQ;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -68,6 +69,18 @@ __global__ void __launch_bounds__(TILE_THREADS) update_kernel(StageArgs a) {
     const R* P = reinterpret_cast<const R*>(B.P);
     const int64_t pn = (int64_t)(nr + 4) * nq;
     const bool one_d = a.one_dimensional != 0;
+    if (MIXED) {
+        // the state this thread updates at the end: start it towards L2 now
+        const int i = i0 + tid / TQ, j = j0 + tid % TQ;
+        if (i < nr && j < nq) {
+            const int64_t n = (int64_t)nr * nq, z = (int64_t)i * nq + j;
+#pragma unroll
+            for (int q = 0; q < NFIELD; ++q) {
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(B.buf[a.sel_in] + q * n + z));
+                if (a.sel_base >= 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(B.buf[a.sel_base] + q * n + z));
+            }
+        }
+    }
 
     // ---- stage primitives (tile rows -2..TR+1 = padded rows i0..i0+TR+3)
     for (int k = tid; k < PR * PQ; k += TILE_THREADS) {
@@ -198,7 +211,7 @@ __global__ void __launch_bounds__(TILE_THREADS) update_kernel(StageArgs a) {
                     const R fd = sFq[(q * TR + r) * (TQ + 1) + c + 1];
                     du = (sc - (fb - fa) - (fd - fc)) * dt;
                 }
-                res[q] = Uin[q * n + z] + (double)du;
+                res[q] = Uin[q * n + z] + (MIXED ? f2d((float)du) : (double)du);
             }
             {
                 const R fa = sFr[(4 * (TR + 1) + r) * TQ + c];
@@ -211,11 +224,17 @@ __global__ void __launch_bounds__(TILE_THREADS) update_kernel(StageArgs a) {
                     const R fd = sFq[(4 * TR + r) * (TQ + 1) + c + 1];
                     ds = ((fb - fa) + (fd - fc)) * -dt;
                 }
-                res[4] = Uin[4 * n + z] + (double)ds;
+                res[4] = Uin[4 * n + z] + (MIXED ? f2d((float)ds) : (double)ds);
             }
             if (U0) {
+                if (MIXED && a.w1 == 0.5 && a.bf == 0.5) {
+                    // RK2 average (U1 + U0) / 2 with the halving on the integer pipe
 #pragma unroll
-                for (int q = 0; q < NFIELD; ++q) res[q] = res[q] * a.w1 + U0[q * n + z] * a.bf;
+                    for (int q = 0; q < NFIELD; ++q) res[q] = half_exact(res[q] + U0[q * n + z]);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < NFIELD; ++q) res[q] = res[q] * a.w1 + U0[q * n + z] * a.bf;
+                }
             }
 #pragma unroll
             for (int q = 0; q < NFIELD; ++q) Uout[q * n + z] = res[q];

@@ -9,6 +9,7 @@
 #include <algorithm>
 
 #include "../../include/knc.h"
+#include "knc_bits.cuh"
 
 namespace {
 
@@ -29,7 +30,37 @@ __global__ void fp64_fma_kernel(double* out, double b, double c) {
     if (s == 1.2345) out[threadIdx.x] = s;   // never true; keeps the chains live
 }
 
+__global__ void conversions_kernel(const double* in, int64_t n, double* out) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const double x = in[k];
+    const float hw = __double2float_rn(x);
+    out[4 * k + 0] = (double)knc::d2f_rn(x);
+    out[4 * k + 1] = (double)hw;
+    out[4 * k + 2] = knc::f2d(hw);
+    out[4 * k + 3] = knc::half_exact(x);
+}
+
 }  // namespace
+
+extern "C" int knc_test_conversions(const double* in, int64_t n, double* out) {
+    if (!in || !out || n <= 0) return KNC_ERR_INVALID_ARGUMENT;
+    double *d_in = nullptr, *d_out = nullptr;
+    if (cudaMalloc(&d_in, n * 8) != cudaSuccess) return KNC_ERR_OUT_OF_MEMORY;
+    if (cudaMalloc(&d_out, n * 32) != cudaSuccess) {
+        cudaFree(d_in);
+        return KNC_ERR_OUT_OF_MEMORY;
+    }
+    cudaError_t e = cudaMemcpy(d_in, in, n * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        conversions_kernel<<<(unsigned)((n + 255) / 256), 256>>>(d_in, n, d_out);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, d_out, n * 32, cudaMemcpyDeviceToHost);
+    cudaFree(d_in);
+    cudaFree(d_out);
+    return e == cudaSuccess ? KNC_OK : KNC_ERR_CUDA;
+}
 
 extern "C" int knc_measure_fp64_peak(double* gflops) {
     if (!gflops) return KNC_ERR_INVALID_ARGUMENT;

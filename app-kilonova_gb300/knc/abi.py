@@ -187,6 +187,7 @@ SIGNATURES = {
     "knc_mlp_forward_backward": (C.c_int, [_FP, _FP, _FP, C.c_int32, _FP, _FP, _FP]),
     "knc_mlp_features": (None, [_DP, _FP]),
     "knc_measure_fp64_peak": (C.c_int, [_DP]),
+    "knc_test_conversions": (C.c_int, [_DP, C.c_int64, _DP]),
     "knc_recover_primitives_noalloc": (C.c_int, [C.POINTER(HydroParams), C.POINTER(MeshParams), C.c_int32,
                                                  _P, _P, _P, _P, C.POINTER(Error)]),
 }

@@ -331,6 +331,13 @@ int knc_recover_primitives_noalloc(const knc_hydro_params* hydro, const knc_mesh
 
 /* ---- utilities --------------------------------------------------------- */
 
+/* Self-test of the integer-pipe conversions the mixed stage uses: for n
+ * doubles, writes the integer-pipe double->float and float->double results
+ * and the hardware conversions (__double2float_rn, exact widening) beside
+ * them: out[4 * k + 0..3] = (integer d2f, hardware d2f, integer f2d of the
+ * hardware d2f, integer-pipe x / 2). */
+int knc_test_conversions(const double* in, int64_t n, double* out);
+
 /* Measured FP64 FMA throughput of the current device (GFLOP/s, 2/FMA). */
 int knc_measure_fp64_peak(double* gflops);
 

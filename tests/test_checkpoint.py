@@ -1,0 +1,84 @@
+"""CBOR checkpoints in the reference's App layout (src/app.rs:181-186,
+src/state.rs:27-43, src/io.rs:24-35): codec round trips, the document shape,
+and a restart that continues exactly like an uninterrupted run."""
+import struct
+
+import numpy as np
+import pytest
+
+from knc import checkpoint as ck
+from knc import config, workloads
+
+
+def test_cbor_scalars_shortest_float_width():
+    assert ck.dumps(0.0) == b"\xf9\x00\x00"
+    assert ck.dumps(1.5) == b"\xf9\x3e\x00"
+    assert ck.dumps(1e-13)[0] == 0xFB
+    assert ck.dumps(0.1)[0] == 0xFB
+    assert ck.dumps(100000.5)[0] == 0xFA         # exact in f32, beyond f16
+    for v in [0, 1, 23, 24, 255, 256, 65535, 65536, 2 ** 40, -1, -25, "RK2", None, True, False]:
+        assert ck.loads(ck.dumps(v)) == v
+
+
+def test_cbor_structures():
+    doc = {"a": [1, 2.5, "x"], (3, 0): {"v": 1}, "b": None, "arr": ck.F64Array(np.arange(6.0).reshape(3, 2))}
+    back = ck.loads(ck.dumps(doc))
+    assert back["a"] == [1, 2.5, "x"] and back[(3, 0)] == {"v": 1} and back["b"] is None
+    assert np.array_equal(back["arr"], np.arange(6.0).reshape(3, 2))
+
+
+def test_app_document_shape():
+    w = workloads.wind_small()
+    blocks = {0: (np.ones((2, 3, 4)), np.zeros((2, 3)))}
+    ctl = config.Control(start_time=0.0, final_time=1.0, checkpoint_interval=0.1, fold=10)
+    doc = ck.loads(ck.dumps(ck.app_document(blocks, 0.5, (7, 2), w.hydro, "wind", {"rho0": 1.0}, w.mesh, ctl)))
+    assert list(doc) == ["state", "tasks", "config", "version"]
+    st = doc["state"]["Relativistic"]
+    assert list(st) == ["time", "iteration", "solution"]
+    assert st["iteration"] == [7, 2]
+    bs = st["solution"][(0, 0)]
+    assert bs["conserved"]["v"] == 1 and bs["conserved"]["dim"] == [2, 3]
+    assert bs["conserved"]["data"].shape == (6, 4)
+    assert doc["config"]["hydro"]["relativistic"]["runge_kutta_order"] == "RK2"
+    assert list(doc["tasks"]) == ["write_checkpoint", "write_products", "iteration_message", "report_progress"]
+    assert list(doc["config"]["mesh"])[:3] == ["reference_radius", "inner_radius", "outer_radius"]
+
+
+def test_checkpoint_file_round_trip(tmp_path, oracle_lib):
+    import knc_oracle
+    w = workloads.wind_small()
+    o = knc_oracle.Oracle(w.hydro, w.mesh, threads=4)
+    o.set_model(w.model)
+    o.init_from_model(0.0)
+    o.advance(3)
+    ctl = config.Control(start_time=0.0, final_time=1e-9, checkpoint_interval=1e-10, fold=3)
+    t, it = o.time()
+    path = tmp_path / "chkpt.0000.cbor"
+    path.write_bytes(ck.dumps(ck.app_document(o.state(), t, it, w.hydro, "wind", {"rho0": 1.0, "ur": 1.0},
+                                              w.mesh, ctl)))
+    c = ck.read_checkpoint(path)
+    assert c.time == t and c.iteration == it and c.kind == "Relativistic"
+    for i, (cons, scal) in o.state().items():
+        assert np.array_equal(c.blocks[i][0], cons) and np.array_equal(c.blocks[i][1], scal)
+    assert c.mesh == w.mesh and c.hydro == w.hydro and c.control == ctl
+    assert c.model_name == "wind" and c.model_params["ur"] == 1.0
+
+
+@pytest.mark.gpu
+def test_restart_continues_exactly(tmp_path):
+    import knc
+    w = workloads.wind_small()
+    ctl = config.Control(start_time=0.0, final_time=1e-9, checkpoint_interval=1e-10, fold=3)
+    a = knc.build_solver(w)
+    a.advance(4)
+    path = tmp_path / "chkpt.cbor"
+    ck.write_checkpoint(path, a, w.hydro, "wind", {}, w.mesh, ctl)
+    a.advance(4)
+    b = knc.Solver(w.hydro, w.mesh)
+    b.set_model(w.model)
+    ck.read_checkpoint(path).restore(b)
+    b.advance(4)
+    assert a.time() == b.time()
+    sa, sb = a.state(), b.state()
+    for i in sa:
+        assert np.array_equal(sa[i][0], sb[i][0]) and np.array_equal(sa[i][1], sb[i][1])
