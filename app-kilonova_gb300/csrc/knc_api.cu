@@ -81,10 +81,17 @@ double face_area(double r0, double q0, double r1, double q1) {              // m
 struct GeomH {
     int64_t nr = 0, nq = 0;
     std::vector<double> rv, qv, ar, aq, dv, rc, qc, cot;
-    std::vector<float> ar_r, ar_q, aq_r, aq_q, dv_r, dv_q, rc32, cot32;
+    std::vector<float2> ar_r, ar_q, aq_r, aq_q, dv_r, dv_q;
+    std::vector<float> dv_r32, rc32, cot32;
 };
 
-GeomH make_geometry(const MeshH& M, int32_t index, bool with_faces = true) {   // mesh.rs:246-264
+// x as an unevaluated pair of floats hi + lo (|lo| <= ulp(hi) / 2).
+float2 split_df(double x) {
+    const float hi = (float)x;
+    return make_float2(hi, (float)(x - (double)hi));
+}
+
+GeomH make_geometry(const MeshH& M, int32_t index, bool with_faces = true, double cflux = 1.0) {   // mesh.rs:246-264
     GeomH G;
     const ExtentH e = M.extent(index);
     const int64_t nr = M.p.block_size, nq = M.p.num_polar_zones;
@@ -115,16 +122,19 @@ GeomH make_geometry(const MeshH& M, int32_t index, bool with_faces = true) {   /
     for (int64_t i = 0; i < nr; ++i)
         for (int64_t j = 0; j <= nq; ++j)
             G.aq[i * (nq + 1) + j] = face_area(G.rv[i], G.qv[j], G.rv[i + 1], G.qv[j]);
-    // separable FP32 factors for the mixed path
+    // separable factors for the mixed path (double-float pairs, c folded in)
     G.ar_r.resize(nr + 1);
     G.aq_r.resize(nr);
     G.dv_r.resize(nr);
+    G.dv_r32.resize(nr);
     G.rc32.resize(nr);
-    for (int64_t i = 0; i <= nr; ++i) G.ar_r[i] = (float)(G.rv[i] * G.rv[i]);
+    for (int64_t i = 0; i <= nr; ++i) G.ar_r[i] = split_df(cflux * (G.rv[i] * G.rv[i]));
     for (int64_t i = 0; i < nr; ++i) {
         const double a = G.rv[i], b = G.rv[i + 1];
-        G.aq_r[i] = (float)(PI_H * (b * b - a * a));
-        G.dv_r[i] = (float)((b * b * b - a * a * a) * 2.0 * PI_H / 3.0);
+        G.aq_r[i] = split_df(cflux * (PI_H * (b * b - a * a)));
+        const double v = (b * b * b - a * a * a) * 2.0 * PI_H / 3.0;
+        G.dv_r[i] = split_df(cflux * v);
+        G.dv_r32[i] = (float)v;
         G.rc32[i] = (float)G.rc[i];
     }
     G.ar_q.resize(nq);
@@ -134,11 +144,11 @@ GeomH make_geometry(const MeshH& M, int32_t index, bool with_faces = true) {   /
     for (int64_t j = 0; j < nq; ++j) {
         const double s0 = std::sin(G.qv[j]), s1 = std::sin(G.qv[j + 1]);
         const double c0 = std::cos(G.qv[j]), c1 = std::cos(G.qv[j + 1]);
-        G.ar_q[j] = (float)(PI_H * (s0 + s1) * std::sqrt((s1 - s0) * (s1 - s0) + (c1 - c0) * (c1 - c0)));
-        G.dv_q[j] = (float)(c0 - c1);
+        G.ar_q[j] = split_df(PI_H * (s0 + s1) * std::sqrt((s1 - s0) * (s1 - s0) + (c1 - c0) * (c1 - c0)));
+        G.dv_q[j] = split_df(c0 - c1);
         G.cot32[j] = (float)G.cot[j];
     }
-    for (int64_t j = 0; j <= nq; ++j) G.aq_q[j] = (float)std::sin(G.qv[j]);
+    for (int64_t j = 0; j <= nq; ++j) G.aq_q[j] = split_df(std::sin(G.qv[j]));
     return G;
 }
 
@@ -174,7 +184,8 @@ struct BlockH {
     double* buf[2] = {nullptr, nullptr};
     void* P = nullptr;
     double *ar = nullptr, *aq = nullptr, *dv = nullptr, *rc = nullptr, *rv = nullptr;
-    float *ar_r = nullptr, *aq_r = nullptr, *dv_r = nullptr, *rc32 = nullptr;
+    float2 *ar_r = nullptr, *aq_r = nullptr, *dv_r = nullptr;
+    float *dv_r32 = nullptr, *rc32 = nullptr;
     GeomH geom;   // host copy (rc, qc for error positions; dv for error values)
 };
 
@@ -190,6 +201,7 @@ void free_block(BlockH& b) {
     cudaFree(b.ar_r);
     cudaFree(b.aq_r);
     cudaFree(b.dv_r);
+    cudaFree(b.dv_r32);
     cudaFree(b.rc32);
     b = BlockH();
 }
@@ -210,7 +222,8 @@ struct knc_ctx {
     int cur = 0;
     // per-column tables (all blocks share the mesh's polar grid)
     double *d_qv = nullptr, *d_qc = nullptr, *d_cot = nullptr;
-    float *d_ar_q = nullptr, *d_aq_q = nullptr, *d_dv_q = nullptr, *d_cot32 = nullptr;
+    float2 *d_ar_q = nullptr, *d_aq_q = nullptr, *d_dv_q = nullptr;
+    float* d_cot32 = nullptr;
     GeomH col;   // host copy of the column tables
     // device block table and tiles
     DevBlock* d_table = nullptr;
@@ -317,7 +330,7 @@ int alloc_block(knc_ctx* c, int32_t index, BlockH& b) {
     const int64_t nr = c->mesh.p.block_size, nq = c->mesh.p.num_polar_zones;
     auto key = std::make_pair(nr, nq);
     auto it = c->pool.find(key);
-    b.geom = make_geometry(c->mesh, index);
+    b.geom = make_geometry(c->mesh, index, true, c->hp.system == KNC_SYSTEM_RELATIVISTIC ? LIGHT_SPEED_H : 1.0);
     b.index = index;
     b.nr = nr;
     b.nq = nq;
@@ -335,6 +348,7 @@ int alloc_block(knc_ctx* c, int32_t index, BlockH& b) {
         b.ar_r = r.ar_r;
         b.aq_r = r.aq_r;
         b.dv_r = r.dv_r;
+        b.dv_r32 = r.dv_r32;
         b.rc32 = r.rc32;
     } else {
         const size_t n = (size_t)(nr * nq);
@@ -349,6 +363,7 @@ int alloc_block(knc_ctx* c, int32_t index, BlockH& b) {
         CK(dalloc(&b.ar_r, (size_t)nr + 1));
         CK(dalloc(&b.aq_r, (size_t)nr));
         CK(dalloc(&b.dv_r, (size_t)nr));
+        CK(dalloc(&b.dv_r32, (size_t)nr));
         CK(dalloc(&b.rc32, (size_t)nr));
     }
     const GeomH& G = b.geom;
@@ -358,9 +373,10 @@ int alloc_block(knc_ctx* c, int32_t index, BlockH& b) {
     CK(cudaMemcpyAsync(b.dv, G.dv.data(), G.dv.size() * 8, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(b.rc, G.rc.data(), G.rc.size() * 8, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(b.rv, G.rv.data(), G.rv.size() * 8, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(b.ar_r, G.ar_r.data(), G.ar_r.size() * 4, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(b.aq_r, G.aq_r.data(), G.aq_r.size() * 4, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(b.dv_r, G.dv_r.data(), G.dv_r.size() * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.ar_r, G.ar_r.data(), G.ar_r.size() * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.aq_r, G.aq_r.data(), G.aq_r.size() * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.dv_r, G.dv_r.data(), G.dv_r.size() * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.dv_r32, G.dv_r32.data(), G.dv_r32.size() * 4, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(b.rc32, G.rc32.data(), G.rc32.size() * 4, cudaMemcpyHostToDevice, s));
     // host geometry vectors are only needed for positions, volumes, ghosts
     b.geom.ar.clear();
@@ -412,6 +428,7 @@ int rebuild_table(knc_ctx* c) {
         d.aq_q = c->d_aq_q;
         d.dv_r = b.dv_r;
         d.dv_q = c->d_dv_q;
+        d.dv_r32 = b.dv_r32;
         d.rc32 = b.rc32;
         d.cot32 = c->d_cot32;
         d.nr = (int32_t)b.nr;
@@ -898,7 +915,7 @@ int time_step_impl(knc_ctx* c, double* dt) {
 }
 
 int setup_columns(knc_ctx* c) {
-    const GeomH G = make_geometry(c->mesh, 0);
+    const GeomH G = make_geometry(c->mesh, 0, true, c->hp.system == KNC_SYSTEM_RELATIVISTIC ? LIGHT_SPEED_H : 1.0);
     c->col = G;
     cudaStream_t s = c->stream;
     CK(upload(&c->d_qv, G.qv, s));

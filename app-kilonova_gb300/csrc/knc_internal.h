@@ -39,16 +39,19 @@ struct DevBlock {
     const double* qv;      // [nq+1]
     const double* qc;      // [nq]
     const double* cot;     // [nq]
-    // mixed path geometry factors (FP32):
-    //   A_r(i,j) = ar_r[i] * ar_q[j]      ar_r = r_i^2,  ar_q = pi (s0+s1) |chord|
-    //   A_q(i,j) = aq_r[i] * aq_q[j]      aq_r = pi (r1^2 - r0^2), aq_q = sin(theta_j)
-    //   dV(i,j)  = dv_r[i] * dv_q[j]      dv_r = (r1^3 - r0^3) 2 pi / 3, dv_q = cos0 - cos1
-    const float* ar_r;     // [nr+1]
-    const float* ar_q;     // [nq]
-    const float* aq_r;     // [nr]
-    const float* aq_q;     // [nq+1]
-    const float* dv_r;     // [nr]
-    const float* dv_q;     // [nq]
+    // mixed path geometry factors, each an unevaluated FP32 pair hi + lo
+    // (about 48 bits), with the flux scale c folded into the radial factors:
+    //   c A_r(i,j) = ar_r[i] * ar_q[j]    ar_r = c r_i^2,  ar_q = pi (s0+s1) |chord|
+    //   c A_q(i,j) = aq_r[i] * aq_q[j]    aq_r = c pi (r1^2 - r0^2), aq_q = sin(theta_j)
+    //   c dV(i,j)  = dv_r[i] * dv_q[j]    dv_r = c (r1^3 - r0^3) 2 pi / 3, dv_q = cos0 - cos1
+    // dV alone (for c2p) is dv_r / c * dv_q; the plain-FP32 dv_r32 holds it.
+    const float2* ar_r;    // [nr+1] (hi, lo)
+    const float2* ar_q;    // [nq]
+    const float2* aq_r;    // [nr]
+    const float2* aq_q;    // [nq+1]
+    const float2* dv_r;    // [nr]
+    const float2* dv_q;    // [nq]
+    const float* dv_r32;   // [nr] (r1^3 - r0^3) 2 pi / 3 in FP32, without c
     const float* rc32;     // [nr]
     const float* cot32;    // [nq]
     void* P_in_nbr;        // inner neighbour's P: my rows 0,1 go to its rows nr'+2, nr'+3

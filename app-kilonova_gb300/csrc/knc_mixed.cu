@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(TILE_THREADS, MLP ? 2 : 3) c2p_mixed_kernel(St
             const double* Ub = B.buf[a.sel_in];
 #pragma unroll
             for (int q = 0; q < 5; ++q) U[q] = Ub[q * n + z];
-            dV = B.dv_r[i] * B.dv_q[j];
+            dV = B.dv_r32[i] * B.dv_q[j].x;
         }
         const double m = U[0], tau = U[3];
         int kind = HYDRO_NONE;

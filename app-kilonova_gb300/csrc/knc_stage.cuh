@@ -22,6 +22,18 @@
 
 namespace knc {
 
+// a * b for double-float factors, as an unevaluated pair (hi, lo): the FP32
+// rounding of the product stays data-dependent instead of freezing a fixed
+// per-face error into every flux difference.
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+    const float h = a.x * b.x;
+    const float e = __fmaf_rn(a.x, b.x, -h);
+    return make_float2(h, __fmaf_rn(a.x, b.y, __fmaf_rn(a.y, b.x, e)));
+}
+
+// x * (hi + lo) in FP32
+__device__ __forceinline__ float df_scale(float x, float2 a) { return __fmaf_rn(x, a.x, x * a.y); }
+
 template <class R>
 struct StageSmem {
     static constexpr int TR = TILE_R, TQ = TILE_Q;
@@ -137,11 +149,15 @@ __global__ void __launch_bounds__(TILE_THREADS, MIXED ? 4 : 1) update_kernel(Sta
             const R sl = sP[(4 * PR + f + 1) * PQ + c + 2] + sGr[(4 * (TR + 2) + f) * TQ + c] * R(0.5);
             const R sr = sP[(4 * PR + f + 2) * PQ + c + 2] - sGr[(4 * (TR + 2) + f + 1) * TQ + c] * R(0.5);
             riemann(ph, pl, pr, sl, sr, 0, out);
-            R A;
-            if (MIXED) A = (R)(B.ar_r[i] * B.ar_q[j]);
-            else A = (R)B.ar[(int64_t)i * nq + j];
+            if constexpr (MIXED) {
+                const float2 A = df_mul(B.ar_r[i], B.ar_q[j]);   // c A_r
 #pragma unroll
-            for (int q = 0; q < NFIELD; ++q) out[q] = out[q] * cflux * A;
+                for (int q = 0; q < NFIELD; ++q) out[q] = df_scale(out[q], A);
+            } else {
+                const R A = (R)B.ar[(int64_t)i * nq + j];
+#pragma unroll
+                for (int q = 0; q < NFIELD; ++q) out[q] = out[q] * cflux * A;
+            }
         }
 #pragma unroll
         for (int q = 0; q < NFIELD; ++q) sFr[(q * (TR + 1) + f) * TQ + c] = out[q];
@@ -162,11 +178,15 @@ __global__ void __launch_bounds__(TILE_THREADS, MIXED ? 4 : 1) update_kernel(Sta
                 const R sl = sP[(4 * PR + r + 2) * PQ + c + 1] + sGq[(4 * TR + r) * (TQ + 2) + c] * R(0.5);
                 const R sr = sP[(4 * PR + r + 2) * PQ + c + 2] - sGq[(4 * TR + r) * (TQ + 2) + c + 1] * R(0.5);
                 riemann(ph, pl, pr, sl, sr, 1, out);
-                R A;
-                if (MIXED) A = (R)(B.aq_r[i] * B.aq_q[j]);
-                else A = (R)B.aq[(int64_t)i * (nq + 1) + j];
+                if constexpr (MIXED) {
+                    const float2 A = df_mul(B.aq_r[i], B.aq_q[j]);   // c A_theta
 #pragma unroll
-                for (int q = 0; q < NFIELD; ++q) out[q] = out[q] * cflux * A;
+                    for (int q = 0; q < NFIELD; ++q) out[q] = df_scale(out[q], A);
+                } else {
+                    const R A = (R)B.aq[(int64_t)i * (nq + 1) + j];
+#pragma unroll
+                    for (int q = 0; q < NFIELD; ++q) out[q] = out[q] * cflux * A;
+                }
             }
 #pragma unroll
             for (int q = 0; q < NFIELD; ++q) sFq[(q * TR + r) * (TQ + 1) + c] = out[q];
@@ -185,10 +205,11 @@ __global__ void __launch_bounds__(TILE_THREADS, MIXED ? 4 : 1) update_kernel(Sta
 #pragma unroll
             for (int q = 0; q < 4; ++q) Pc[q] = sP[(q * PR + r + 2) * PQ + c + 2];
             R src[4];
-            R dV;
-            if (MIXED) {
+            R dV = R(0);
+            float2 cdV = make_float2(0.f, 0.f);
+            if constexpr (MIXED) {
                 sources(ph, Pc, (R)B.rc32[i], (R)B.cot32[j], src);
-                dV = (R)(B.dv_r[i] * B.dv_q[j]);
+                cdV = df_mul(B.dv_r[i], B.dv_q[j]);   // c dV
             } else {
                 sources(ph, Pc, (R)B.rc[i], (R)B.cot[j], src);
                 dV = (R)B.dv[z];
@@ -200,7 +221,9 @@ __global__ void __launch_bounds__(TILE_THREADS, MIXED ? 4 : 1) update_kernel(Sta
             double res[NFIELD];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                const R sc = src[q] * cflux * dV;
+                R sc;
+                if constexpr (MIXED) sc = df_scale(src[q], cdV);
+                else sc = src[q] * cflux * dV;
                 const R fa = sFr[(q * (TR + 1) + r) * TQ + c];
                 const R fb = sFr[(q * (TR + 1) + r + 1) * TQ + c];
                 R du;
