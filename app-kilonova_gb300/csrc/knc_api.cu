@@ -1036,7 +1036,7 @@ int knc_last_error(const knc_ctx* c, knc_error* out) {
 
 int knc_set_model(knc_ctx* c, const knc_model_params* m) {
     if (!c || !m) return KNC_ERR_INVALID_ARGUMENT;
-    if (m->kind < KNC_MODEL_WIND || m->kind > KNC_MODEL_SPHERE)
+    if (m->kind < KNC_MODEL_WIND || m->kind > KNC_MODEL_JET_IN_STAR || m->kind == KNC_MODEL_HOST)
         return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "unknown model kind %d", m->kind);
     c->model = *m;
     c->have_model = true;

@@ -44,6 +44,9 @@ KNC_MODEL_WIND = 0
 KNC_MODEL_JET = 1
 KNC_MODEL_SPHERE = 2
 KNC_MODEL_HOST = 3
+KNC_MODEL_JET_IN_CLOUD = 4
+KNC_MODEL_KINETIC_BOMB = 5
+KNC_MODEL_JET_IN_STAR = 6
 
 KNC_KERNEL_GHOST = 0
 KNC_KERNEL_C2P = 1

@@ -255,3 +255,62 @@ class SphereModel:
         for k, v in enumerate([self.rho_in, self.rho_out, self.radius, self.pressure, self.noise]):
             m.p[k] = v
         return m
+
+
+# ---- the reference's setups, evaluated on the device ---------------------
+def _pack(kind, values):
+    m = abi.ModelParams(kind=kind, seed=0)
+    for k, v in enumerate(values):
+        m.p[k] = float(v)
+    return m
+
+
+@dataclass
+class JetInCloud:
+    """src/models/jet_in_cloud.rs:16-49 (field names as in setups/jet_in_cloud.yaml)."""
+    cloud_mass: float
+    engine_delay: float
+    engine_duration: float
+    engine_strength: float
+    engine_theta: float
+    engine_u: float
+    envelop_m1: float
+    envelop_slowest_beta: float
+    envelop_fastest_beta: float
+    envelop_psi: float
+
+    def to_c(self):
+        return _pack(abi.KNC_MODEL_JET_IN_CLOUD, [getattr(self, f.name) for f in fields(self)])
+
+
+@dataclass
+class KineticBomb:
+    """src/models/kinetic_bomb.rs:12-20."""
+    external_medium_density: float
+    launch_radius: float
+    shell_thickness: float
+    kinetic_energy: float
+    shell_mass: float
+
+    def to_c(self):
+        return _pack(abi.KNC_MODEL_KINETIC_BOMB, [getattr(self, f.name) for f in fields(self)])
+
+
+@dataclass
+class JetInStar:
+    """src/models/jet_in_star.rs:36-62."""
+    star_mass: float
+    engine_duration: float
+    engine_energy: float
+    engine_theta: float
+    engine_u: float
+    envelope_radius: float
+    envelope_mass: float
+    volume_factor: float
+
+    def to_c(self):
+        return _pack(abi.KNC_MODEL_JET_IN_STAR, [getattr(self, f.name) for f in fields(self)])
+
+
+SETUP_MODELS = {"jet_in_cloud": JetInCloud, "kinetic_bomb": KineticBomb, "jet_in_star": JetInStar,
+                "wind": WindModel, "jet": JetModel, "sphere": SphereModel}

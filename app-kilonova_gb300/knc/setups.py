@@ -14,8 +14,7 @@ import re
 from dataclasses import dataclass
 from pathlib import Path
 
-from .config import (ConfigError, Control, JetModel, Mesh, NewtonianHydro, RelativisticHydro, SphereModel,
-                     WindModel)
+from .config import (SETUP_MODELS, ConfigError, Control, Mesh, NewtonianHydro, RelativisticHydro)
 
 _NUM = re.compile(r"^[+-]?(\d+\.?\d*|\.\d+)([eE][+-]?\d+)?$")
 
@@ -92,9 +91,17 @@ class Configuration:
     control: Control
 
     def device_model(self):
-        """The device model for the synthetic setups, or None (host callback needed)."""
-        cls = {"wind": WindModel, "jet": JetModel, "sphere": SphereModel}.get(self.model_name)
-        return cls(**self.model_params) if cls else None
+        """The device model of this setup, or None when only a host callback
+        can evaluate it (halo_kilonova, wind_shock). Unknown fields raise, as
+        the reference's deny_unknown_fields does."""
+        cls = SETUP_MODELS.get(self.model_name)
+        if cls is None:
+            return None
+        names = {f for f in cls.__dataclass_fields__}
+        extra = set(self.model_params) - names
+        if extra:
+            raise ConfigError(f"unknown field(s) {sorted(extra)} for {self.model_name}")
+        return cls(**self.model_params)
 
 
 def _one_tag(d, what):

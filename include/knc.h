@@ -68,7 +68,10 @@ enum {
     KNC_MODEL_WIND = 0,      /* cold radial wind rho ~ r^-2, u^r = const            */
     KNC_MODEL_JET = 1,       /* wind-like ambient + W=const nozzle at the inner edge */
     KNC_MODEL_SPHERE = 2,    /* Newtonian over-dense sphere at rest                  */
-    KNC_MODEL_HOST = 3       /* host callback (slow path, no graph capture)          */
+    KNC_MODEL_HOST = 3,      /* host callback (slow path, no graph capture)          */
+    KNC_MODEL_JET_IN_CLOUD = 4,   /* src/models/jet_in_cloud.rs:74-257               */
+    KNC_MODEL_KINETIC_BOMB = 5,   /* src/models/kinetic_bomb.rs:78-114               */
+    KNC_MODEL_JET_IN_STAR = 6     /* src/models/jet_in_star.rs:87-236                */
 };
 
 /*
@@ -114,6 +117,14 @@ typedef struct knc_mesh_params {
  *          does, so the jet enters through the inner boundary)
  *  SPHERE: p[0]=rho inside, p[1]=rho outside, p[2]=sphere radius,
  *          p[3]=pressure, p[4]=noise amplitude
+ *  JET_IN_CLOUD: the fields of JetInCloud in declaration order
+ *          (cloud_mass, engine_delay, engine_duration, engine_strength,
+ *          engine_theta, engine_u, envelop_m1, envelop_slowest_beta,
+ *          envelop_fastest_beta, envelop_psi)
+ *  KINETIC_BOMB: (external_medium_density, launch_radius, shell_thickness,
+ *          kinetic_energy, shell_mass)
+ *  JET_IN_STAR: (star_mass, engine_duration, engine_energy, engine_theta,
+ *          engine_u, envelope_radius, envelope_mass, volume_factor)
  * Noise multiplies the density by (1 + amp * U[0,1)) with U a counter-based
  * hash of (seed, block index, i, j); it enters only the initial data, never
  * the ghost blocks, so `primitive_at` stays a pure function of (r, theta, t).

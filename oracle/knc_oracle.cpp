@@ -553,6 +553,87 @@ void model_eval(const Phys& ph, const ModelDef& Md, double r, double q, double t
         scalar = r < a[2] ? 1.0 : 0.0;
         break;
     }
+    case KNC_MODEL_JET_IN_CLOUD: {           // src/models/jet_in_cloud.rs:74-257
+        const double cloud_mass = a[0], delay = a[1], duration = a[2], strength = a[3], theta_j = a[4];
+        const double engine_u = a[5], m1 = a[6], slowest = a[7], fastest = a[8], psi = a[9];
+        const double engine_beta = engine_u / std::sqrt(1.0 + engine_u * engine_u);
+        const double r_interface = slowest * LIGHT_SPEED * t;
+        const double v_jet = engine_beta * LIGHT_SPEED;
+        const double r_head = v_jet * (t - delay);
+        const double r_tail = v_jet * (t - delay - duration);
+        const bool in_nozzle = q < theta_j || q > PI - theta_j;
+        double u, f;
+        if (in_nozzle && r < r_head && r > r_tail) {          // Zone::Jet
+            u = engine_u;
+            const double engine_gamma = std::sqrt(1.0 + engine_u * engine_u);
+            f = strength * cloud_mass / (4.0 * PI * duration) / engine_gamma;
+            scalar = 1e2;
+        } else if (r > r_interface) {                         // Zone::Envelope
+            const double b = std::min(r / t / LIGHT_SPEED, fastest);
+            u = b / std::sqrt(1.0 - b * b);
+            f = m1 / (4.0 * PI * psi * t) * (std::pow(b, -1.0 / psi) * std::pow(1.0 - b * b, 0.5 / psi - 1.0));
+            scalar = 1e-2;
+        } else {                                              // Zone::Cloud
+            u = slowest / std::sqrt(1.0 - slowest * slowest);
+            f = cloud_mass / (4.0 * PI * delay);
+            scalar = 1.0;
+        }
+        const double d = f / (r * r * u) / LIGHT_SPEED;
+        P.v[0] = d; P.v[1] = u; P.v[2] = 0.0; P.v[3] = d * 1e-3;
+        break;
+    }
+    case KNC_MODEL_KINETIC_BOMB: {           // src/models/kinetic_bomb.rs:78-114
+        const double v = std::sqrt(2.0 * a[3] / a[4]);
+        const double dur = a[2] / v;
+        if (a[1] + v * (t - dur) <= r && r < a[1] + v * t) {
+            const double d = a[4] / dur / (4.0 * PI * r * r * v);
+            P.v[0] = d; P.v[1] = v / LIGHT_SPEED; P.v[2] = 0.0; P.v[3] = d * 1e-3;
+            scalar = 1.0;
+        } else {
+            const double x = r / a[1];
+            const double d = a[0] * (x * x);
+            P.v[0] = d; P.v[1] = 0.0; P.v[2] = 0.0; P.v[3] = d * 1e-3;
+            scalar = 0.0;
+        }
+        break;
+    }
+    case KNC_MODEL_JET_IN_STAR: {            // src/models/jet_in_star.rs:87-236
+        const double R0 = 7e10, M0 = 2e33;
+        const double RHO_C = 3e7 * M0 / (1.33 * PI * R0 * R0 * R0);
+        const double R1 = 0.0017 * R0, R2 = 0.0125 * R0, R3 = 0.65 * R0;
+        const double RHO_WIND = 1e-9 * M0 / (1.33 * PI * R0 * R0 * R0);
+        const double R_NOZZ = 0.01 * R0, R_ENV = 1.2 * R0;
+        const double engine_u = a[4], theta_j = a[3], env_radius = a[5];
+        const double rho_env = a[6] / (4.0 * PI * (env_radius * env_radius) * (env_radius - R3) * a[7]);
+        const double r_head = engine_u / std::sqrt(1.0 + engine_u * engine_u) * LIGHT_SPEED * t;
+        const bool in_nozzle = q < theta_j || q > PI - theta_j;
+        double d, u = 0.0;
+        if (in_nozzle && r < r_head) {
+            const double r0 = R_NOZZ / R0;
+            const double q2 = theta_j * theta_j;
+            const double n0 = 4.0 * PI * r0 * r0 * r0 * (1.0 - std::exp(-2.0 / q2)) * q2;
+            const double g = (r / R_NOZZ) * std::exp(-std::pow(r / R_NOZZ, 2.0) / 2.0) *
+                             std::exp((std::pow(std::cos(q), 2.0) - 1.0) / q2);
+            const double l = g / n0 * a[2] / (4.0 * PI * a[1]);
+            const double rate = l / (std::sqrt(1.0 + engine_u * engine_u) * LIGHT_SPEED * LIGHT_SPEED);
+            d = rate / (r * r * engine_u * LIGHT_SPEED);
+            u = engine_u;
+            scalar = 1e2;
+        } else if (r < R3) {
+            const double core = RHO_C * std::pow(1.0 - r / R3, 16.7) /
+                                (1.0 + std::pow(r / R1, 3.24) / (1.0 + std::pow(r / R2, 2.57)));
+            d = core + rho_env * std::pow(r / R3, -2.0);
+            scalar = 1.0;
+        } else if (R3 < r && r < env_radius) {
+            d = rho_env * std::pow(r / R3, -2.5);
+            scalar = 1e-2 * std::pow(r / R3, -2.0);
+        } else {
+            d = RHO_WIND * std::pow(r / R_ENV, -2.0);
+            scalar = 1e-5 * std::pow(r / R_ENV, -2.0);
+        }
+        P.v[0] = d; P.v[1] = u; P.v[2] = 0.0; P.v[3] = d * 1e-10;
+        break;
+    }
     case KNC_MODEL_HOST: {
         double any[4];
         Md.host_fn(r, q, t, any, &scalar, Md.host_user);
