@@ -306,10 +306,9 @@ int validate(knc_ctx* c, const knc_hydro_params* h, const knc_mesh_params* m) {
     if (!(h->gamma_law_index > 1.0)) return set_msg(c, KNC_ERR_CONFIG, "gamma_law_index must exceed 1");
     if (m->reference_radius <= 0.0 || m->inner_radius < 0.0 || m->outer_radius < 0.0)
         return set_msg(c, KNC_ERR_CONFIG, "all radii must be positive");
-    MeshH M;
-    M.p = *m;
-    if (m->reference_radius > M.oes(0.0))
-        return set_msg(c, KNC_ERR_CONFIG, "the reference radius is outside the outer excision surface");
+    // the reference radius against the outer excision surface depends on the
+    // start time (Mesh::validate(time), src/mesh.rs:277-279): checked by
+    // knc_init_from_model, which knows the time
     if (m->has_excision_delay && m->excision_delay < 0.0)
         return set_msg(c, KNC_ERR_CONFIG, "the excision delay time must be non-negative");
     if (m->inner_excision_speed < 0.0 || m->outer_excision_speed < 0.0)
@@ -1056,6 +1055,8 @@ int knc_set_host_model(knc_ctx* c, knc_primitive_at_fn fn, void* user) {
 int knc_init_from_model(knc_ctx* c, double time) {
     if (!c) return KNC_ERR_INVALID_ARGUMENT;
     if (!c->have_model) return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "no model set");
+    if (c->mesh.p.reference_radius > c->mesh.oes(time))
+        return set_msg(c, KNC_ERR_CONFIG, "the reference radius is outside the outer excision surface");
     int r;
     CK(cudaStreamSynchronize(c->stream));
     for (auto& kv : c->blocks) release_block(c, kv.second);

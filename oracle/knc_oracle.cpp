@@ -1066,6 +1066,7 @@ int oracle_set_model(oracle_ctx* c, const knc_model_params* m) {
 
 int oracle_init_from_model(oracle_ctx* c, double time) {
     if (!c) return KNC_ERR_INVALID_ARGUMENT;
+    if (c->mesh.p.reference_radius > c->mesh.outer_excision_surface(time)) return KNC_ERR_CONFIG;
     c->blocks.clear();
     std::vector<int32_t> idx;
     for (int32_t i = 0;; ++i) {                     // Mesh::grid_blocks, mesh.rs:384-397

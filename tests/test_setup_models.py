@@ -24,7 +24,7 @@ def _run(hydro, mesh, model, t0, steps, fold):
     o.set_model(model)
     o.init_from_model(t0)
     assert g.block_indexes() == o.block_indexes()
-    assert max(field_errors(g.state(), o.state())) <= TOL
+    assert max(field_errors(g.state(), o.state(), momentum_scale=True)) <= TOL
     for _ in range(steps // fold):
         g.advance(fold)
         o.advance(fold)
@@ -40,7 +40,7 @@ def test_kinetic_bomb_one_dimensional():
                                kinetic_energy=5e50, shell_mass=1e32)
     g, o = _run(hydro, mesh, model, 0.0, 20, 5)
     assert g.time()[0] == pytest.approx(o.time()[0], rel=1e-13)
-    assert max(field_errors(g.state(), o.state())) <= TOL
+    assert max(field_errors(g.state(), o.state(), momentum_scale=True)) <= TOL
 
 
 def test_jet_in_cloud_moving_excision():
@@ -52,7 +52,7 @@ def test_jet_in_cloud_moving_excision():
                               envelop_fastest_beta=0.99, envelop_psi=0.3)
     g, o = _run(hydro, mesh, model, 1.0, 20, 5)
     assert g.time() == o.time()
-    assert max(field_errors(g.state(), o.state())) <= TOL
+    assert max(field_errors(g.state(), o.state(), momentum_scale=True)) <= TOL
 
 
 def test_jet_in_star():
@@ -62,7 +62,7 @@ def test_jet_in_star():
     model = config.JetInStar(star_mass=1e34, engine_duration=10.0, engine_energy=1e51, engine_theta=0.1,
                              engine_u=40.0, envelope_radius=1e11, envelope_mass=1e31, volume_factor=1.0)
     g, o = _run(hydro, mesh, model, 0.0, 20, 5)
-    assert max(field_errors(g.state(), o.state())) <= TOL
+    assert max(field_errors(g.state(), o.state(), momentum_scale=True)) <= TOL
 
 
 def test_host_callback_model_equals_device_model():
