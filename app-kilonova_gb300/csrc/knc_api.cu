@@ -91,10 +91,12 @@ float2 split_df(double x) {
     return make_float2(hi, (float)(x - (double)hi));
 }
 
-GeomH make_geometry(const MeshH& M, int32_t index, bool with_faces = true, double cflux = 1.0) {   // mesh.rs:246-264
+GeomH make_geometry(const MeshH& M, int32_t index, bool with_faces = true, double cflux = 1.0, int64_t nr = 0,
+                    int64_t nq = 0) {   // mesh.rs:246-264
     GeomH G;
     const ExtentH e = M.extent(index);
-    const int64_t nr = M.p.block_size, nq = M.p.num_polar_zones;
+    if (nr <= 0) nr = M.p.block_size;
+    if (nq <= 0) nq = M.p.num_polar_zones;
     G.nr = nr;
     G.nq = nq;
     G.rv.resize(nr + 1);
@@ -206,6 +208,45 @@ void free_block(BlockH& b) {
     b = BlockH();
 }
 
+// One block set's device view.
+struct Layout {
+    DevBlock* d_table = nullptr;
+    int table_cap = 0;
+    int4* d_tiles = nullptr;
+    int tiles_cap = 0;
+    int ntiles = 0;
+    // halo remaps across polar-resolution changes
+    int4* d_remap = nullptr;
+    int remap_cap = 0;
+    int nremap = 0;
+    int max_nq = 0;
+    std::vector<int32_t> slot_index;   // slot -> block index
+    // edge blocks, whose outer halo rows the ghost launch writes
+    void* P_edge[2] = {nullptr, nullptr};
+    int32_t nr_edge[2] = {0, 0}, nq_edge[2] = {0, 0};
+    // ghost rows
+    int32_t ghost_lo = INT32_MIN, ghost_hi = INT32_MIN;
+    double* d_ghost_rc = nullptr;                  // [2 ends][2 rows]
+    double* d_ghost_dv[2] = {nullptr, nullptr};    // per end [2][nq]
+    int64_t ghost_nq[2] = {0, 0};
+    std::vector<double> ghost_rc_h, ghost_dv_h[2];
+    // a block activated at the start of the step this layout begins
+    int4* d_init_tiles = nullptr;
+    int n_init_tiles = 0;
+    int32_t first_stage = 0;   // stage counter when the layout took effect
+};
+
+void free_layout(Layout& l) {
+    cudaFree(l.d_table);
+    cudaFree(l.d_tiles);
+    cudaFree(l.d_remap);
+    cudaFree(l.d_ghost_rc);
+    cudaFree(l.d_ghost_dv[0]);
+    cudaFree(l.d_ghost_dv[1]);
+    cudaFree(l.d_init_tiles);
+    l = Layout();
+}
+
 }  // namespace
 
 struct knc_ctx {
@@ -220,26 +261,25 @@ struct knc_ctx {
     std::map<int32_t, BlockH> blocks;
     std::map<std::pair<int64_t, int64_t>, std::vector<BlockH>> pool;   // freed block storage by shape
     int cur = 0;
-    // per-column tables (all blocks share the mesh's polar grid)
-    double *d_qv = nullptr, *d_qc = nullptr, *d_cot = nullptr;
-    float2 *d_ar_q = nullptr, *d_aq_q = nullptr, *d_dv_q = nullptr;
-    float* d_cot32 = nullptr;
-    GeomH col;   // host copy of the column tables
-    // device block table and tiles
-    DevBlock* d_table = nullptr;
-    int table_cap = 0;
-    int4* d_tiles = nullptr;
-    int tiles_cap = 0;
-    int ntiles = 0;
+    // uneven blocks: index -> (nr, nq); other indexes use the mesh's shape
+    std::map<int32_t, std::pair<int64_t, int64_t>> shapes;
+    // per-column tables, one set per polar resolution in use
+    struct ColTab {
+        double *qv = nullptr, *qc = nullptr, *cot = nullptr;
+        float2 *ar_q = nullptr, *aq_q = nullptr, *dv_q = nullptr;
+        float* cot32 = nullptr;
+        std::vector<double> qc_h;
+    };
+    std::map<int64_t, ColTab> cols;
+    // Device view of a block set (table, tiles, remaps, ghost rows). A
+    // captured fold whose excision surfaces move holds one per block set it
+    // passes through; otherwise there is one, rebuilt in place.
+    std::vector<Layout> lays{1};
+    int cur_lay = 0;
     bool dirty = true;
-    std::vector<int32_t> slot_index;   // slot -> block index, current table
-    // ghost rows
-    int32_t ghost_lo = INT32_MIN, ghost_hi = INT32_MIN;
-    double* d_ghost_rc = nullptr;    // [2][2]
-    double* d_ghost_dv = nullptr;    // [2][2][nq]
+    std::vector<BlockH> deferred;    // retired inside a captured fold, released after it ran
     double* d_host_prim = nullptr;   // host model values
     size_t host_prim_cap = 0;
-    std::vector<double> ghost_rc_h, ghost_dv_h;
     // status
     DevStatus* d_status = nullptr;
     DevStatus* h_status = nullptr;
@@ -270,6 +310,9 @@ struct knc_ctx {
 };
 
 namespace {
+
+inline Layout& L(knc_ctx* c) { return c->lays[c->cur_lay]; }
+inline const Layout& L(const knc_ctx* c) { return c->lays[c->cur_lay]; }
 
 int set_msg(knc_ctx* c, int status, const char* fmt, ...) __attribute__((format(printf, 3, 4)));
 int set_msg(knc_ctx* c, int status, const char* fmt, ...) {
@@ -325,11 +368,42 @@ int validate(knc_ctx* c, const knc_hydro_params* h, const knc_mesh_params* m) {
     return KNC_OK;
 }
 
+std::pair<int64_t, int64_t> shape_of(const knc_ctx* c, int32_t index) {
+    auto it = c->shapes.find(index);
+    if (it != c->shapes.end()) return it->second;
+    return {c->mesh.p.block_size, c->mesh.p.num_polar_zones};
+}
+
+double cflux_of(const knc_ctx* c) { return c->hp.system == KNC_SYSTEM_RELATIVISTIC ? LIGHT_SPEED_H : 1.0; }
+
+// Column tables of a polar resolution, built on first use.
+int get_cols(knc_ctx* c, int64_t nq, knc_ctx::ColTab** out) {
+    auto it = c->cols.find(nq);
+    if (it == c->cols.end()) {
+        const GeomH G = make_geometry(c->mesh, 0, true, cflux_of(c), 2, nq);
+        knc_ctx::ColTab t;
+        cudaStream_t s = c->stream;
+        CK(upload(&t.qv, G.qv, s));
+        CK(upload(&t.qc, G.qc, s));
+        CK(upload(&t.cot, G.cot, s));
+        CK(upload(&t.ar_q, G.ar_q, s));
+        CK(upload(&t.aq_q, G.aq_q, s));
+        CK(upload(&t.dv_q, G.dv_q, s));
+        CK(upload(&t.cot32, G.cot32, s));
+        CK(cudaStreamSynchronize(s));
+        t.qc_h = G.qc;
+        it = c->cols.emplace(nq, t).first;
+    }
+    *out = &it->second;
+    return KNC_OK;
+}
+
 int alloc_block(knc_ctx* c, int32_t index, BlockH& b) {
-    const int64_t nr = c->mesh.p.block_size, nq = c->mesh.p.num_polar_zones;
+    const auto shape = shape_of(c, index);
+    const int64_t nr = shape.first, nq = shape.second;
     auto key = std::make_pair(nr, nq);
     auto it = c->pool.find(key);
-    b.geom = make_geometry(c->mesh, index, true, c->hp.system == KNC_SYSTEM_RELATIVISTIC ? LIGHT_SPEED_H : 1.0);
+    b.geom = make_geometry(c->mesh, index, true, cflux_of(c), nr, nq);
     b.index = index;
     b.nr = nr;
     b.nq = nq;
@@ -400,16 +474,22 @@ int rebuild_table(knc_ctx* c) {
     const int nb = (int)c->blocks.size();
     std::vector<DevBlock> tab(nb);
     std::vector<int4> tiles;
-    c->slot_index.clear();
+    L(c).slot_index.clear();
     int slot = 0;
     int64_t zoff = 0;
     const BlockH* prev = nullptr;
     std::vector<const BlockH*> order;
+    std::vector<int4> remaps;
+    L(c).max_nq = 0;
     for (auto& kv : c->blocks) order.push_back(&kv.second);
     for (int k = 0; k < nb; ++k) {
         const BlockH& b = *order[k];
         DevBlock& d = tab[k];
         std::memset(&d, 0, sizeof(d));
+        knc_ctx::ColTab* ct = nullptr;
+        int r0;
+        if ((r0 = get_cols(c, b.nq, &ct))) return r0;
+        L(c).max_nq = std::max<int>(L(c).max_nq, (int)b.nq);
         d.buf[0] = b.buf[0];
         d.buf[1] = b.buf[1];
         d.P = b.P;
@@ -418,52 +498,77 @@ int rebuild_table(knc_ctx* c) {
         d.dv = b.dv;
         d.rc = b.rc;
         d.rv = b.rv;
-        d.qv = c->d_qv;
-        d.qc = c->d_qc;
-        d.cot = c->d_cot;
+        d.qv = ct->qv;
+        d.qc = ct->qc;
+        d.cot = ct->cot;
         d.ar_r = b.ar_r;
-        d.ar_q = c->d_ar_q;
+        d.ar_q = ct->ar_q;
         d.aq_r = b.aq_r;
-        d.aq_q = c->d_aq_q;
+        d.aq_q = ct->aq_q;
         d.dv_r = b.dv_r;
-        d.dv_q = c->d_dv_q;
+        d.dv_q = ct->dv_q;
         d.dv_r32 = b.dv_r32;
         d.rc32 = b.rc32;
-        d.cot32 = c->d_cot32;
+        d.cot32 = ct->cot32;
+        d.slot_in = -1;
+        d.slot_out = -1;
         d.nr = (int32_t)b.nr;
         d.nq = (int32_t)b.nq;
         d.index = b.index;
-        if (prev && prev->index + 1 == b.index && prev->nq == b.nq) {
-            d.P_in_nbr = prev->P;
-            d.nr_in_nbr = (int32_t)prev->nr;
-            tab[k - 1].P_out_nbr = b.P;
-            tab[k - 1].nr_out_nbr = (int32_t)b.nr;
+        if (prev && prev->index + 1 == b.index) {
+            d.slot_in = k - 1;
+            tab[k - 1].slot_out = k;
+            if (prev->nq == b.nq) {      // same polar grid: the producer pushes halo rows
+                d.P_in_nbr = prev->P;
+                d.nr_in_nbr = (int32_t)prev->nr;
+                tab[k - 1].P_out_nbr = b.P;
+                tab[k - 1].nr_out_nbr = (int32_t)b.nr;
+            } else {                     // remapped after the recovery pass
+                remaps.push_back(make_int4(k, k - 1, 0, 0));
+                remaps.push_back(make_int4(k - 1, k, 1, 0));
+            }
         }
         for (int64_t i0 = 0; i0 < b.nr; i0 += TILE_R)
             for (int64_t j0 = 0; j0 < b.nq; j0 += TILE_Q)
                 tiles.push_back(make_int4(slot, (int)i0, (int)j0, (int)zoff));
-        c->slot_index.push_back(b.index);
+        L(c).slot_index.push_back(b.index);
         zoff += b.nr * b.nq;
         prev = &b;
         ++slot;
     }
-    if (nb > c->table_cap) {
-        cudaFree(c->d_table);
-        c->d_table = nullptr;
-        CK(dalloc(&c->d_table, (size_t)nb));
-        c->table_cap = nb;
+    if (nb > L(c).table_cap) {
+        cudaFree(L(c).d_table);
+        L(c).d_table = nullptr;
+        CK(dalloc(&L(c).d_table, (size_t)nb));
+        L(c).table_cap = nb;
     }
-    if ((int)tiles.size() > c->tiles_cap) {
-        cudaFree(c->d_tiles);
-        c->d_tiles = nullptr;
-        CK(dalloc(&c->d_tiles, tiles.size()));
-        c->tiles_cap = (int)tiles.size();
+    if ((int)tiles.size() > L(c).tiles_cap) {
+        cudaFree(L(c).d_tiles);
+        L(c).d_tiles = nullptr;
+        CK(dalloc(&L(c).d_tiles, tiles.size()));
+        L(c).tiles_cap = (int)tiles.size();
     }
-    if (nb) CK(cudaMemcpyAsync(c->d_table, tab.data(), nb * sizeof(DevBlock), cudaMemcpyHostToDevice, c->stream));
+    if (nb) CK(cudaMemcpyAsync(L(c).d_table, tab.data(), nb * sizeof(DevBlock), cudaMemcpyHostToDevice, c->stream));
     if (!tiles.empty())
-        CK(cudaMemcpyAsync(c->d_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(L(c).d_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
+    if ((int)remaps.size() > L(c).remap_cap) {
+        cudaFree(L(c).d_remap);
+        L(c).d_remap = nullptr;
+        CK(dalloc(&L(c).d_remap, remaps.size()));
+        L(c).remap_cap = (int)remaps.size();
+    }
+    if (!remaps.empty())
+        CK(cudaMemcpyAsync(L(c).d_remap, remaps.data(), remaps.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                           c->stream));
+    L(c).nremap = (int)remaps.size();
+    for (int end = 0; end < 2 && nb; ++end) {
+        const BlockH& e = *order[end ? nb - 1 : 0];
+        L(c).P_edge[end] = e.P;
+        L(c).nr_edge[end] = (int32_t)e.nr;
+        L(c).nq_edge[end] = (int32_t)e.nq;
+    }
     CK(cudaStreamSynchronize(c->stream));
-    c->ntiles = (int)tiles.size();
+    L(c).ntiles = (int)tiles.size();
     c->dirty = false;
     return KNC_OK;
 }
@@ -472,26 +577,37 @@ int rebuild_table(knc_ctx* c) {
 int update_ghost_geometry(knc_ctx* c) {
     if (c->blocks.empty()) return KNC_OK;
     const int32_t lo = c->blocks.begin()->first - 1, hi = c->blocks.rbegin()->first + 1;
-    if (lo == c->ghost_lo && hi == c->ghost_hi && c->d_ghost_rc) return KNC_OK;
-    const int64_t nq = c->mesh.p.num_polar_zones, nr = c->mesh.p.block_size;
-    const GeomH gl = make_geometry(c->mesh, lo, false), gh = make_geometry(c->mesh, hi, false);
-    c->ghost_rc_h = {gl.rc[nr - 2], gl.rc[nr - 1], gh.rc[0], gh.rc[1]};
-    c->ghost_dv_h.resize(4 * nq);
-    for (int64_t j = 0; j < nq; ++j) {
-        c->ghost_dv_h[0 * nq + j] = gl.dv[(nr - 2) * nq + j];
-        c->ghost_dv_h[1 * nq + j] = gl.dv[(nr - 1) * nq + j];
-        c->ghost_dv_h[2 * nq + j] = gh.dv[0 * nq + j];
-        c->ghost_dv_h[3 * nq + j] = gh.dv[1 * nq + j];
+    // each ghost block has its own radial shape and the polar resolution of
+    // the live block it borders
+    const int64_t nq_lo = c->blocks.begin()->second.nq, nq_hi = c->blocks.rbegin()->second.nq;
+    if (lo == L(c).ghost_lo && hi == L(c).ghost_hi && L(c).d_ghost_rc && nq_lo == L(c).ghost_nq[0] &&
+        nq_hi == L(c).ghost_nq[1])
+        return KNC_OK;
+    const int64_t nr_lo = shape_of(c, lo).first, nr_hi = shape_of(c, hi).first;
+    knc_ctx::ColTab* ct;
+    int r;
+    if ((r = get_cols(c, nq_lo, &ct)) || (r = get_cols(c, nq_hi, &ct))) return r;
+    const GeomH gl = make_geometry(c->mesh, lo, false, 1.0, nr_lo, nq_lo);
+    const GeomH gh = make_geometry(c->mesh, hi, false, 1.0, nr_hi, nq_hi);
+    L(c).ghost_rc_h = {gl.rc[nr_lo - 2], gl.rc[nr_lo - 1], gh.rc[0], gh.rc[1]};
+    L(c).ghost_dv_h[0].assign(gl.dv.begin() + (nr_lo - 2) * nq_lo, gl.dv.begin() + nr_lo * nq_lo);
+    L(c).ghost_dv_h[1].assign(gh.dv.begin(), gh.dv.begin() + 2 * nq_hi);
+    if (!L(c).d_ghost_rc) CK(dalloc(&L(c).d_ghost_rc, 4));
+    for (int end = 0; end < 2; ++end) {
+        const int64_t nq = end ? nq_hi : nq_lo;
+        if (nq != L(c).ghost_nq[end]) {
+            cudaFree(L(c).d_ghost_dv[end]);
+            L(c).d_ghost_dv[end] = nullptr;
+            CK(dalloc(&L(c).d_ghost_dv[end], (size_t)(2 * nq)));
+            L(c).ghost_nq[end] = nq;
+        }
+        CK(cudaMemcpyAsync(L(c).d_ghost_dv[end], L(c).ghost_dv_h[end].data(), 2 * nq * 8, cudaMemcpyHostToDevice,
+                           c->stream));
     }
-    if (!c->d_ghost_rc) {
-        CK(dalloc(&c->d_ghost_rc, 4));
-        CK(dalloc(&c->d_ghost_dv, (size_t)(4 * nq)));
-    }
-    CK(cudaMemcpyAsync(c->d_ghost_rc, c->ghost_rc_h.data(), 4 * 8, cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemcpyAsync(c->d_ghost_dv, c->ghost_dv_h.data(), 4 * nq * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(L(c).d_ghost_rc, L(c).ghost_rc_h.data(), 4 * 8, cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    c->ghost_lo = lo;
-    c->ghost_hi = hi;
+    L(c).ghost_lo = lo;
+    L(c).ghost_hi = hi;
     return KNC_OK;
 }
 
@@ -506,19 +622,24 @@ int ensure_host_prim(knc_ctx* c, size_t n) {
 
 // Host model values of the ghost rows (slow path: the model is a callback).
 int host_ghost_values(knc_ctx* c, double t) {
-    const int64_t nq = c->mesh.p.num_polar_zones;
-    std::vector<double> v(4 * nq * 5);
-    for (int k = 0; k < 4; ++k)
+    const int64_t nq0 = L(c).ghost_nq[0], nq1 = L(c).ghost_nq[1];
+    std::vector<double> v((2 * nq0 + 2 * nq1) * 5);
+    for (int k = 0; k < 4; ++k) {
+        const int end = k / 2;
+        const int64_t nq = end ? nq1 : nq0;
+        const std::vector<double>& qc = c->cols.at(nq).qc_h;
+        const int64_t base = end ? 2 * nq0 : 0;
         for (int64_t j = 0; j < nq; ++j) {
             double any[4], s = 0.0;
-            c->host_fn(c->ghost_rc_h[k], c->col.qc[j], t, any, &s, c->host_user);
-            double* o = &v[((int64_t)k * nq + j) * 5];
+            c->host_fn(L(c).ghost_rc_h[k], qc[j], t, any, &s, c->host_user);
+            double* o = &v[(base + (int64_t)(k % 2) * nq + j) * 5];
             o[0] = any[2];   // interpret: AnyPrimitive [u_r, u_q, rho, p] -> (rho, u_r, u_q, p)
             o[1] = any[0];
             o[2] = any[1];
             o[3] = any[3];
             o[4] = s;
         }
+    }
     int r = ensure_host_prim(c, v.size());
     if (r) return r;
     CK(cudaMemcpyAsync(c->d_host_prim, v.data(), v.size() * 8, cudaMemcpyHostToDevice, c->stream));
@@ -574,9 +695,9 @@ void drain_profile(knc_ctx* c) {
 StageArgs base_args(knc_ctx* c) {
     StageArgs a;
     std::memset(&a, 0, sizeof(a));
-    a.blocks = c->d_table;
-    a.tiles = c->d_tiles;
-    a.ntiles = c->ntiles;
+    a.blocks = L(c).d_table;
+    a.tiles = L(c).d_tiles;
+    a.ntiles = L(c).ntiles;
     a.srhd = c->hp.system == KNC_SYSTEM_RELATIVISTIC;
     a.hllc = c->hp.riemann_solver == KNC_RIEMANN_HLLC;
     a.one_dimensional = c->mesh.p.num_polar_zones == 1;
@@ -618,20 +739,19 @@ int run_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, doub
     // ghost rows at the stage time
     GhostArgs g;
     std::memset(&g, 0, sizeof(g));
-    const BlockH& first = c->blocks.begin()->second;
-    const BlockH& last = c->blocks.rbegin()->second;
-    g.P[0] = first.P;
-    g.P[1] = last.P;
+    const Layout& lay = L(c);
+    for (int end = 0; end < 2; ++end) {
+        g.P[end] = lay.P_edge[end];
+        g.nr_t[end] = lay.nr_edge[end];
+        g.nq[end] = lay.nq_edge[end];
+        g.dv[end] = lay.d_ghost_dv[end];
+        g.qc[end] = c->cols.at(lay.nq_edge[end]).qc;
+    }
     g.row0[0] = 0;
-    g.row0[1] = (int32_t)last.nr + 2;
-    g.nr_t[0] = (int32_t)first.nr;
-    g.nr_t[1] = (int32_t)last.nr;
-    g.nq = (int32_t)c->mesh.p.num_polar_zones;
-    g.ghost_index[0] = c->ghost_lo;
-    g.ghost_index[1] = c->ghost_hi;
-    g.rc = c->d_ghost_rc;
-    g.dv = c->d_ghost_dv;
-    g.qc = c->d_qc;
+    g.row0[1] = lay.nr_edge[1] + 2;
+    g.ghost_index[0] = lay.ghost_lo;
+    g.ghost_index[1] = lay.ghost_hi;
+    g.rc = lay.d_ghost_rc;
     g.model = c->model;
     g.time = t_stage;
     g.srhd = c->hp.system == KNC_SYSTEM_RELATIVISTIC;
@@ -641,7 +761,8 @@ int run_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, doub
     g.status = c->d_status;
     if (c->model.kind == KNC_MODEL_HOST) {
         if ((r = host_ghost_values(c, t_stage))) return r;
-        g.host_prim = c->d_host_prim;
+        g.host_prim[0] = c->d_host_prim;
+        g.host_prim[1] = c->d_host_prim + 2 * L(c).ghost_nq[0] * 5;
     }
     {
         ProfScope ps(c, KNC_KERNEL_GHOST);
@@ -657,8 +778,40 @@ int run_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, doub
     a.bf = bf;
     a.dt = dt;
     if ((r = launch_c2p(c, a))) return r;
+    if (L(c).nremap) {
+        CK(launch_remap(a, L(c).d_remap, L(c).nremap, L(c).max_nq, mixed(c), c->stream));
+        ++c->launches;
+    }
     if ((r = launch_update(c, a))) return r;
     return KNC_OK;
+}
+
+// Stage start times of one SSP RK step and the time after it, averaged as
+// godunov_core::runge_kutta does (t = t1 (1 - b) + t0 b). rk_step and the
+// planner of a captured fold both take their times from here.
+struct StepTimes {
+    double stage[3];
+    double end;
+};
+
+StepTimes step_times(int order, double t0, double dt) {
+    auto avg_time = [](double t1, double tb, double bf) { return t1 * (-bf + 1.0) + tb * bf; };
+    StepTimes s{};
+    s.stage[0] = t0;
+    const double t1 = t0 + dt;
+    if (order == 1) {
+        s.end = t1;
+        return s;
+    }
+    s.stage[1] = t1;
+    if (order == 2) {
+        s.end = avg_time(t1 + dt, t0, 0.5);
+        return s;
+    }
+    const double t2 = avg_time(t1 + dt, t0, 0.75);
+    s.stage[2] = t2;
+    s.end = avg_time(t2 + dt, t0, 1.0 / 3.0);
+    return s;
 }
 
 // godunov_core::runge_kutta::try_advance_async restated (SSP RK1/RK2/RK3).
@@ -668,47 +821,45 @@ int rk_step(knc_ctx* c, double dt) {
     const Rational it0 = c->iteration;
     Rational one;
     one.n = 1;
-    auto avg_time = [](double t1, double tb, double bf) { return t1 * (-bf + 1.0) + tb * bf; };
+    const int order = c->hp.runge_kutta_order;
+    const StepTimes T = step_times(order, t0, dt);
     auto avg_iter = [&](Rational i1, Rational br) {
         Rational mbr = br;
         mbr.n = -mbr.n;
         return i1.mul(mbr.add(one)).add(it0.mul(br));
     };
     int r;
-    const int order = c->hp.runge_kutta_order;
-    if ((r = run_stage(c, A, B, -1, 1.0, 0.0, t0, dt))) return r;
-    double t1 = t0 + dt;
+    if ((r = run_stage(c, A, B, -1, 1.0, 0.0, T.stage[0], dt))) return r;
     Rational i1 = it0.add(one);
     if (order == 1) {
         c->cur = B;
-        c->time = t1;
+        c->time = T.end;
         c->iteration = i1;
         return KNC_OK;
     }
     if (order == 2) {
         const double bf = 0.5;
-        if ((r = run_stage(c, B, A, A, -bf + 1.0, bf, t1, dt))) return r;
+        if ((r = run_stage(c, B, A, A, -bf + 1.0, bf, T.stage[1], dt))) return r;
         Rational half;
         half.n = 1;
         half.d = 2;
-        c->time = avg_time(t1 + dt, t0, bf);
+        c->time = T.end;
         c->iteration = avg_iter(i1.add(one), half);
         return KNC_OK;
     }
     // RK3
     const double b2 = 0.75;
-    if ((r = run_stage(c, B, B, A, -b2 + 1.0, b2, t1, dt))) return r;
+    if ((r = run_stage(c, B, B, A, -b2 + 1.0, b2, T.stage[1], dt))) return r;
     Rational q34;
     q34.n = 3;
     q34.d = 4;
-    const double t2 = avg_time(t1 + dt, t0, b2);
     const Rational i2 = avg_iter(i1.add(one), q34);
     const double b3 = 1.0 / 3.0;
-    if ((r = run_stage(c, B, A, A, -b3 + 1.0, b3, t2, dt))) return r;
+    if ((r = run_stage(c, B, A, A, -b3 + 1.0, b3, T.stage[2], dt))) return r;
     Rational q13;
     q13.n = 1;
     q13.d = 3;
-    c->time = avg_time(t2 + dt, t0, b3);
+    c->time = T.end;
     c->iteration = avg_iter(i2.add(one), q13);
     return KNC_OK;
 }
@@ -724,23 +875,33 @@ int check_status(knc_ctx* c) {
     const int32_t i = (int32_t)((k >> 20) & 0x3fffu);
     const int32_t j = (int32_t)((k >> 4) & 0xffffu);
     const int32_t kind = (int32_t)(k & 0xfu);
+    const int32_t stage = (int32_t)(k >> 48);
     std::memset(&c->err, 0, sizeof(c->err));
     c->err.kind = kind;
     c->err.i = i;
     c->err.j = j;
+    // the layout in effect at the failing stage (layouts are in stage order)
+    const Layout* lay = &c->lays.front();
+    for (const Layout& l : c->lays)
+        if (l.first_stage <= stage) lay = &l;
     if (slot >= 0x3ffeu) {
         const int end = (int)(slot - 0x3ffeu);
-        c->err.block = end ? c->ghost_hi : c->ghost_lo;
-        c->err.r = c->ghost_rc_h.empty() ? 0.0 : c->ghost_rc_h[end * 2 + i];
-        c->err.theta = c->col.qc.empty() ? 0.0 : c->col.qc[j];
-    } else if (slot < c->slot_index.size()) {
-        const int32_t index = c->slot_index[slot];
+        c->err.block = end ? lay->ghost_hi : lay->ghost_lo;
+        c->err.r = lay->ghost_rc_h.empty() ? 0.0 : lay->ghost_rc_h[end * 2 + i];
+        auto ct = c->cols.find(lay->ghost_nq[end]);
+        c->err.theta = ct == c->cols.end() ? 0.0 : ct->second.qc_h[j];
+    } else if (slot < lay->slot_index.size()) {
+        const int32_t index = lay->slot_index[slot];
         c->err.block = index;
+        const BlockH* bp = nullptr;
         auto it = c->blocks.find(index);
-        if (it != c->blocks.end()) {
-            const BlockH& b = it->second;
+        if (it != c->blocks.end()) bp = &it->second;
+        for (const BlockH& d : c->deferred)
+            if (d.index == index) bp = &d;
+        if (bp) {
+            const BlockH& b = *bp;
             c->err.r = b.geom.rc[i];
-            c->err.theta = c->col.qc[j];
+            c->err.theta = c->cols.at(b.nq).qc_h[j];
             const int sel = c->h_status->err_sel;
             double u[5];
             const int64_t n = b.nr * b.nq, z = (int64_t)i * b.nq + j;
@@ -780,8 +941,8 @@ int init_block_from_model(knc_ctx* c, int32_t index, double t) {
     int r;
     if ((r = rebuild_table(c))) return r;
     int slot = -1;
-    for (size_t k = 0; k < c->slot_index.size(); ++k)
-        if (c->slot_index[k] == index) slot = (int)k;
+    for (size_t k = 0; k < L(c).slot_index.size(); ++k)
+        if (L(c).slot_index[k] == index) slot = (int)k;
     if (slot < 0) return set_msg(c, KNC_ERR_NO_BLOCK, "block %d missing", index);
     std::vector<int4> tiles;
     const BlockH& b = c->blocks.at(index);
@@ -792,7 +953,7 @@ int init_block_from_model(knc_ctx* c, int32_t index, double t) {
     CK(cudaMemcpyAsync(d_t, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
     InitArgs ia;
     std::memset(&ia, 0, sizeof(ia));
-    ia.blocks = c->d_table;
+    ia.blocks = L(c).d_table;
     ia.tiles = d_t;
     ia.sel = c->cur;
     ia.srhd = c->hp.system == KNC_SYSTEM_RELATIVISTIC;
@@ -806,7 +967,7 @@ int init_block_from_model(knc_ctx* c, int32_t index, double t) {
         for (int64_t i = 0; i < b.nr; ++i)
             for (int64_t j = 0; j < b.nq; ++j) {
                 double any[4], s = 0.0;
-                c->host_fn(b.geom.rc[i], c->col.qc[j], t, any, &s, c->host_user);
+                c->host_fn(b.geom.rc[i], b.geom.qc[j], t, any, &s, c->host_user);
                 double* o = &v[(i * b.nq + j) * 5];
                 o[0] = any[2];
                 o[1] = any[0];
@@ -887,9 +1048,18 @@ int check_ready(knc_ctx* c) {
 int time_step_impl(knc_ctx* c, double* dt) {
     const bool global = c->hp.system == KNC_SYSTEM_RELATIVISTIC && !c->hp.adaptive_time_step;
     if (global) {   // cfl * smallest_spacing(innermost) / c, state.rs:147-149
-        const ExtentH e = c->mesh.extent(c->blocks.begin()->first);
-        const int64_t nr = c->mesh.p.block_size;
-        const double spacing = vertex_r(e, nr, 1) - vertex_r(e, nr, 0);
+        // With uneven blocks a finer block further out can hold the smallest
+        // spacing, so the minimum runs over all blocks; for equal shapes the
+        // innermost block is always the minimum and this is the reference rule.
+        double spacing = 0.0;
+        bool have = false;
+        for (auto& kv : c->blocks) {
+            const ExtentH e = c->mesh.extent(kv.first);
+            const int64_t nr = kv.second.nr;
+            const double sp = vertex_r(e, nr, 1) - vertex_r(e, nr, 0);
+            if (!have || sp < spacing) spacing = sp;
+            have = true;
+        }
         *dt = c->hp.cfl_number * spacing / LIGHT_SPEED_H;
         return KNC_OK;
     }
@@ -913,21 +1083,6 @@ int time_step_impl(knc_ctx* c, double* dt) {
     return KNC_OK;
 }
 
-int setup_columns(knc_ctx* c) {
-    const GeomH G = make_geometry(c->mesh, 0, true, c->hp.system == KNC_SYSTEM_RELATIVISTIC ? LIGHT_SPEED_H : 1.0);
-    c->col = G;
-    cudaStream_t s = c->stream;
-    CK(upload(&c->d_qv, G.qv, s));
-    CK(upload(&c->d_qc, G.qc, s));
-    CK(upload(&c->d_cot, G.cot, s));
-    CK(upload(&c->d_ar_q, G.ar_q, s));
-    CK(upload(&c->d_aq_q, G.aq_q, s));
-    CK(upload(&c->d_dv_q, G.dv_q, s));
-    CK(upload(&c->d_cot32, G.cot32, s));
-    CK(cudaStreamSynchronize(s));
-    return KNC_OK;
-}
-
 int ensure_stage(knc_ctx* c, size_t doubles) {
     if (doubles <= c->stage_cap) return KNC_OK;
     cudaFree(c->d_stage);
@@ -944,7 +1099,8 @@ int create_device_side(knc_ctx* c) {
     CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CK(dalloc(&c->d_status, 1));
     CK(cudaMallocHost((void**)&c->h_status, sizeof(DevStatus)));
-    if ((r = setup_columns(c))) return r;
+    knc_ctx::ColTab* ct;
+    if ((r = get_cols(c, c->mesh.p.num_polar_zones, &ct))) return r;
     return reset_status(c, false);
 }
 
@@ -1002,17 +1158,18 @@ void knc_destroy(knc_ctx* c) {
     for (auto& kv : c->blocks) free_block(kv.second);
     for (auto& kv : c->pool)
         for (auto& b : kv.second) free_block(b);
-    cudaFree(c->d_qv);
-    cudaFree(c->d_qc);
-    cudaFree(c->d_cot);
-    cudaFree(c->d_ar_q);
-    cudaFree(c->d_aq_q);
-    cudaFree(c->d_dv_q);
-    cudaFree(c->d_cot32);
-    cudaFree(c->d_table);
-    cudaFree(c->d_tiles);
-    cudaFree(c->d_ghost_rc);
-    cudaFree(c->d_ghost_dv);
+    for (auto& kv : c->cols) {
+        knc_ctx::ColTab& t = kv.second;
+        cudaFree(t.qv);
+        cudaFree(t.qc);
+        cudaFree(t.cot);
+        cudaFree(t.ar_q);
+        cudaFree(t.aq_q);
+        cudaFree(t.dv_q);
+        cudaFree(t.cot32);
+    }
+    for (auto& l : c->lays) free_layout(l);
+    for (auto& b : c->deferred) free_block(b);
     cudaFree(c->d_host_prim);
     cudaFree(c->d_status);
     cudaFree(c->d_mlp);
@@ -1074,8 +1231,8 @@ int knc_init_from_model(knc_ctx* c, double time) {
     if ((r = rebuild_table(c))) return r;
     InitArgs ia;
     std::memset(&ia, 0, sizeof(ia));
-    ia.blocks = c->d_table;
-    ia.tiles = c->d_tiles;
+    ia.blocks = L(c).d_table;
+    ia.tiles = L(c).d_tiles;
     ia.sel = c->cur;
     ia.srhd = c->hp.system == KNC_SYSTEM_RELATIVISTIC;
     ia.noise = 1;
@@ -1092,7 +1249,7 @@ int knc_init_from_model(knc_ctx* c, double time) {
             for (int64_t i = 0; i < b.nr; ++i)
                 for (int64_t j = 0; j < b.nq; ++j) {
                     double any[4], s = 0.0;
-                    c->host_fn(b.geom.rc[i], c->col.qc[j], time, any, &s, c->host_user);
+                    c->host_fn(b.geom.rc[i], b.geom.qc[j], time, any, &s, c->host_user);
                     double* o = &v[(off + i * b.nq + j) * 5];
                     o[0] = any[2];
                     o[1] = any[0];
@@ -1106,7 +1263,7 @@ int knc_init_from_model(knc_ctx* c, double time) {
         CK(cudaMemcpyAsync(c->d_host_prim, v.data(), v.size() * 8, cudaMemcpyHostToDevice, c->stream));
         ia.host_prim = c->d_host_prim;
     }
-    CK(launch_init_f64(ia, c->ntiles, c->stream));
+    CK(launch_init_f64(ia, L(c).ntiles, c->stream));
     ++c->launches;
     CK(cudaStreamSynchronize(c->stream));
     c->time = time;
@@ -1182,6 +1339,40 @@ int knc_block_shape(const knc_ctx* c, int64_t* nr, int64_t* nq) {
     return KNC_OK;
 }
 
+int knc_set_block_shapes(knc_ctx* c, int32_t first, int32_t count, const int32_t* nr, const int32_t* nq) {
+    if (!c || count < 0 || (count && (!nr || !nq))) return KNC_ERR_INVALID_ARGUMENT;
+    const int64_t nq0 = c->mesh.p.num_polar_zones;
+    for (int32_t k = 0; k < count; ++k) {
+        if (nr[k] < 2 || nr[k] > 16383)
+            return set_msg(c, KNC_ERR_CONFIG, "block %d: radial zones %d outside [2, 16383]", first + k, nr[k]);
+        bool pow2 = false;   // nq = nq0 * 2^m for some integer m
+        for (int64_t a = nq0, b = nq[k]; !pow2 && a > 0 && b > 0;) {
+            if (a == b) pow2 = true;
+            else if (a < b) { if (b % 2) break; b /= 2; }
+            else { if (a % 2) break; a /= 2; }
+        }
+        if (!pow2 || nq[k] > 65535 || (nq0 != 1 && nq[k] < 16) || (nq0 == 1 && nq[k] != 1))
+            return set_msg(c, KNC_ERR_CONFIG,
+                           "block %d: polar zones %d must be the mesh's %lld times a power of two, in [16, 65535]",
+                           first + k, nq[k], (long long)nq0);
+        auto it = c->blocks.find(first + k);
+        if (it != c->blocks.end() && (it->second.nr != nr[k] || it->second.nq != nq[k]))
+            return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "block %d is live with another shape", first + k);
+    }
+    for (int32_t k = 0; k < count; ++k) c->shapes[first + k] = {nr[k], nq[k]};
+    L(c).ghost_lo = INT32_MIN;   // ghost shapes may have changed
+    c->dirty = true;
+    return c->blocks.empty() ? KNC_OK : update_ghost_geometry(c);
+}
+
+int knc_block_shape_of(const knc_ctx* c, int32_t index, int64_t* nr, int64_t* nq) {
+    if (!c) return KNC_ERR_INVALID_ARGUMENT;
+    const auto sh = shape_of(c, index);
+    if (nr) *nr = sh.first;
+    if (nq) *nq = sh.second;
+    return KNC_OK;
+}
+
 int knc_set_state(knc_ctx* c, const double* cons, const double* scalar) {
     if (!c || !cons || !scalar) return KNC_ERR_INVALID_ARGUMENT;
     int64_t total = 0;
@@ -1247,6 +1438,92 @@ int knc_time_step(knc_ctx* c, double* dt) {
     return time_step_impl(c, dt);
 }
 
+namespace {
+
+// Block-set changes of a captured fold whose excision surfaces move, decided
+// on the host before capture: the step times come from step_times (the same
+// arithmetic rk_step applies), so each step's add_remove_blocks outcome
+// (src/scheme.rs:179-206) is known in advance. Every block set gets its own
+// layout with fresh device buffers; an activated block is allocated now and
+// its initial data is written by an init launch inside the graph at the step
+// it joins; a retired block's storage is held until the graph has run.
+int plan_fold(knc_ctx* c, int32_t fold, double dt, std::vector<int>& step_lay, std::vector<char>& step_init) {
+    double t = c->time;
+    const int order = c->hp.runge_kutta_order;
+    int r;
+    for (int32_t k = 0; k < fold; ++k) {
+        const int32_t inner = c->blocks.begin()->first;
+        const int32_t outer = c->blocks.rbegin()->first;
+        const bool drop = c->mesh.extent(inner).r1 < c->mesh.ies(t);
+        const bool add = c->mesh.extent(outer).r1 < c->mesh.oes(t);
+        if (drop || add) {
+            if (drop) {
+                if (c->blocks.size() == 1 && !add)
+                    return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "the inner excision surface removed every block");
+                c->deferred.push_back(c->blocks.at(inner));
+                c->blocks.erase(inner);
+            }
+            if (add && (r = insert_block(c, outer + 1))) return r;
+            c->lays.emplace_back();
+            c->cur_lay = (int)c->lays.size() - 1;
+            c->dirty = true;
+            if ((r = rebuild_table(c))) return r;
+            if ((r = update_ghost_geometry(c))) return r;
+            if (add) {
+                const BlockH& b = c->blocks.at(outer + 1);
+                const int slot = (int)L(c).slot_index.size() - 1;   // the outermost slot
+                std::vector<int4> tiles;
+                for (int64_t i0 = 0; i0 < b.nr; i0 += TILE_R)
+                    for (int64_t j0 = 0; j0 < b.nq; j0 += TILE_Q) tiles.push_back(make_int4(slot, (int)i0, (int)j0, 0));
+                CK(upload(&L(c).d_init_tiles, tiles, c->stream));
+                CK(cudaStreamSynchronize(c->stream));
+                L(c).n_init_tiles = (int)tiles.size();
+            }
+        }
+        step_lay[k] = c->cur_lay;
+        step_init[k] = add ? 1 : 0;
+        t = step_times(order, t, dt).end;
+    }
+    return KNC_OK;
+}
+
+// Initial data of the block activated at the start of this step (captured).
+int launch_activation(knc_ctx* c) {
+    InitArgs ia;
+    std::memset(&ia, 0, sizeof(ia));
+    ia.blocks = L(c).d_table;
+    ia.tiles = L(c).d_init_tiles;
+    ia.sel = c->cur;
+    ia.srhd = c->hp.system == KNC_SYSTEM_RELATIVISTIC;
+    ia.noise = 0;   // activated blocks take the model's noise-free data, like ghosts
+    ia.gm = c->hp.gamma_law_index;
+    ia.time = c->time;
+    ia.model = c->model;
+    CK(launch_init_f64(ia, L(c).n_init_tiles, c->stream));
+    ++c->launches;
+    return KNC_OK;
+}
+
+// After a captured fold ran: keep the last layout, free the others, and
+// return retired blocks' storage to the pool.
+void finish_fold(knc_ctx* c) {
+    if (c->lays.size() > 1) {
+        Layout keep = c->lays[c->cur_lay];
+        c->lays[c->cur_lay] = Layout();
+        for (auto& l : c->lays) free_layout(l);
+        c->lays.assign(1, keep);
+        c->cur_lay = 0;
+    }
+    L(c).first_stage = 0;
+    cudaFree(L(c).d_init_tiles);
+    L(c).d_init_tiles = nullptr;
+    L(c).n_init_tiles = 0;
+    for (auto& b : c->deferred) release_block(c, b);
+    c->deferred.clear();
+}
+
+}  // namespace
+
 int knc_advance(knc_ctx* c, int32_t fold) {
     if (!c || fold < 0) return KNC_ERR_INVALID_ARGUMENT;
     int r = KNC_OK;
@@ -1257,20 +1534,36 @@ int knc_advance(knc_ctx* c, int32_t fold) {
     double dt;
     if ((r = time_step_impl(c, &dt))) return r;
     const int per_step = c->hp.runge_kutta_order;
-    const bool graph = c->batched && !c->mesh.moving() && c->model.kind != KNC_MODEL_HOST && fold > 0 &&
+    const bool graph = c->batched && c->model.kind != KNC_MODEL_HOST && fold > 0 &&
                        c->stage_counter + (int64_t)fold * per_step < 0xffff;
     if (graph) {
-        // One CUDA graph holds the whole fold: ghost, c2p and update launches
-        // of every stage; a later fold with the same shape only updates the
-        // executable graph's parameters (times) instead of re-instantiating.
+        // One CUDA graph holds the whole fold: ghost, c2p, remap and update
+        // launches of every stage, and the init launch of every block the
+        // outer excision surface activates; a later fold with the same shape
+        // only updates the executable graph's parameters (times, pointers)
+        // instead of re-instantiating.
+        std::vector<int> step_lay(fold, c->cur_lay);
+        std::vector<char> step_init(fold, 0);
+        if (c->mesh.moving() && (r = plan_fold(c, fold, dt, step_lay, step_init))) {
+            c->failed = true;
+            return r;
+        }
         c->capturing = true;
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-        for (int32_t k = 0; k < fold && r == KNC_OK; ++k) r = rk_step(c, dt);
+        for (int32_t k = 0; k < fold && r == KNC_OK; ++k) {
+            if (c->cur_lay != step_lay[k]) {
+                c->cur_lay = step_lay[k];
+                L(c).first_stage = c->stage_counter;
+            }
+            if (step_init[k]) r = launch_activation(c);
+            if (r == KNC_OK) r = rk_step(c, dt);
+        }
         cudaGraph_t g = nullptr;
         const cudaError_t ec = cudaStreamEndCapture(c->stream, &g);
         c->capturing = false;
         if (r) {
             if (g) cudaGraphDestroy(g);
+            c->failed = true;
             return r;
         }
         CK(ec);
@@ -1287,7 +1580,9 @@ int knc_advance(knc_ctx* c, int32_t fold) {
         cudaGraphDestroy(g);
         CK(ei);
         CK(cudaGraphLaunch(c->graph_exec, c->stream));
-        return check_status(c);
+        r = check_status(c);
+        finish_fold(c);
+        return r;
     }
     for (int32_t k = 0; k < fold; ++k) {
         if (c->mesh.moving())
@@ -1410,7 +1705,7 @@ int knc_sample_pairs(knc_ctx* c, int32_t stride, double* out, int64_t capacity, 
     cudaError_t e = dalloc(&d_cnt, 1);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_cnt, 0, 8, c->stream);
     if (e == cudaSuccess)
-        e = launch_sample_pairs(c->d_table, c->d_tiles, c->ntiles, c->cur, stride, c->hp.gamma_law_index, d_out,
+        e = launch_sample_pairs(L(c).d_table, L(c).d_tiles, L(c).ntiles, c->cur, stride, c->hp.gamma_law_index, d_out,
                                 capacity, d_cnt, c->stream);
     ++c->launches;
     unsigned long long cnt = 0;

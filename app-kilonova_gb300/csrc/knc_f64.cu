@@ -112,15 +112,16 @@ __global__ void __launch_bounds__(TILE_THREADS) c2p_f64_kernel(StageArgs a) {
 __global__ void ghost_kernel(GhostArgs a) {
     const int end = blockIdx.y;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= 2 * a.nq || a.P[end] == nullptr) return;
-    const int row = k / a.nq, j = k - row * a.nq;
+    const int nq = a.nq[end];
+    if (k >= 2 * nq || a.P[end] == nullptr) return;
+    const int row = k / nq, j = k - row * nq;
     const double r = a.rc[end * 2 + row];
-    const double q = a.qc[j];
-    const double dV = a.dv[(end * 2 + row) * a.nq + j];
+    const double q = a.qc[end][j];
+    const double dV = a.dv[end][row * nq + j];
     double Pm[4];
     double scalar;
-    if (a.host_prim) {
-        const double* hp = a.host_prim + (((int64_t)end * 2 + row) * a.nq + j) * 5;
+    if (a.host_prim[end]) {
+        const double* hp = a.host_prim[end] + ((int64_t)row * nq + j) * 5;
         Pm[0] = hp[0];
         Pm[1] = hp[1];
         Pm[2] = hp[2];
@@ -156,8 +157,8 @@ __global__ void ghost_kernel(GhostArgs a) {
     const double w = a.srhd ? sqrt(1.0 + P[1] * P[1] + P[2] * P[2]) : 1.0;
     const double v[NFIELD] = {P[0], P[1], P[2], P[3], smass / dV / w};
     const int nrt = a.nr_t[end];
-    const int64_t pn = (int64_t)(nrt + 4) * a.nq;
-    const int64_t off = (int64_t)(a.row0[end] + row) * a.nq + j;
+    const int64_t pn = (int64_t)(nrt + 4) * nq;
+    const int64_t off = (int64_t)(a.row0[end] + row) * nq + j;
     if (a.single_precision) {
         float* Pd = reinterpret_cast<float*>(a.P[end]);
 #pragma unroll
@@ -167,6 +168,79 @@ __global__ void ghost_kernel(GhostArgs a) {
 #pragma unroll
         for (int c = 0; c < NFIELD; ++c) Pd[c * pn + off] = v[c];
     }
+}
+
+// ---- halo remap across a change of polar resolution ----------------------------
+// Target column j of a halo row from row `row` of the source block:
+//  - a finer source (R = nq_s / nq_t): conserved volume integrals and volumes
+//    of its R zones summed in column order, then the FP64 recovery (the
+//    reference's Newton from the plain guess) — a conservative merge;
+//  - a coarser source: its primitive at column j / R, copied.
+// blockIdx.y = remap item, blockIdx.x * blockDim.x + threadIdx.x = (row, j).
+template <class R>
+__global__ void remap_kernel(StageArgs a, const int4* __restrict__ items, int nitems) {
+    const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
+    if (ek != NO_ERROR && (uint32_t)(ek >> 48) < (uint32_t)a.stage) return;
+    const int4 it = items[blockIdx.y];
+    const DevBlock& T = a.blocks[it.x];
+    const DevBlock& S = a.blocks[it.y];
+    const int side = it.z;
+    const int nq_t = T.nq, nq_s = S.nq;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= 2 * nq_t) return;
+    const int row = k / nq_t, j = k - row * nq_t;
+    const int srow = side == 0 ? S.nr - 2 + row : row;          // source interior row
+    const int trow = side == 0 ? row : T.nr + 2 + row;          // target padded row
+    R v[NFIELD];
+    if (nq_s < nq_t) {
+        const R* Ps = reinterpret_cast<const R*>(S.P);
+        const int64_t pn = (int64_t)(S.nr + 4) * nq_s;
+        const int64_t off = (int64_t)(srow + 2) * nq_s + j / (nq_t / nq_s);
+#pragma unroll
+        for (int q = 0; q < NFIELD; ++q) v[q] = Ps[q * pn + off];
+    } else {
+        const int Rr = nq_s / nq_t;
+        const double* Us = S.buf[a.sel_in];
+        const int64_t n = (int64_t)S.nr * nq_s;
+        double U[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, dv = 0.0;
+        for (int m = 0; m < Rr; ++m) {
+            const int64_t z = (int64_t)srow * nq_s + j * Rr + m;
+#pragma unroll
+            for (int q = 0; q < 5; ++q) U[q] += Us[q * n + z];
+            dv += S.dv[z];
+        }
+        double u[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) u[q] = U[q] / dv;
+        double P[4] = {0.0, 0.0, 0.0, 0.0};
+        double bad = 0.0;
+        int iters = 0, kind;
+        if (a.srhd) kind = srhd_c2p_newton(a.gm, u, 0.0, P, iters, bad);
+        else kind = newt_c2p(a.gm - 1.0, u, P, bad);
+        if (kind != HYDRO_NONE && kind != HYDRO_NEGATIVE_PRESSURE)
+            atomicMin(&a.status->err_key, error_key(a.stage, it.y, srow, j * Rr, kind));
+        const double w = a.srhd ? sqrt(1.0 + P[1] * P[1] + P[2] * P[2]) : 1.0;
+        const double sv = U[4] / dv / w;
+        v[0] = (R)P[0];
+        v[1] = (R)P[1];
+        v[2] = (R)P[2];
+        v[3] = (R)P[3];
+        v[4] = (R)sv;
+    }
+    R* Pt = reinterpret_cast<R*>(T.P);
+    const int64_t pt = (int64_t)(T.nr + 4) * nq_t;
+    const int64_t ot = (int64_t)trow * nq_t + j;
+#pragma unroll
+    for (int q = 0; q < NFIELD; ++q) Pt[q * pt + ot] = v[q];
+}
+
+cudaError_t launch_remap(const StageArgs& a, const int4* remap, int nremap, int max_nq, bool single_precision,
+                         cudaStream_t s) {
+    if (nremap <= 0) return cudaSuccess;
+    dim3 grid((2 * max_nq + 127) / 128, nremap);
+    if (single_precision) remap_kernel<float><<<grid, 128, 0, s>>>(a, remap, nremap);
+    else remap_kernel<double><<<grid, 128, 0, s>>>(a, remap, nremap);
+    return cudaGetLastError();
 }
 
 // ---- initial data -------------------------------------------------------------
@@ -290,7 +364,8 @@ cudaError_t configure_f64() {
 }
 
 cudaError_t launch_ghost(const GhostArgs& a, cudaStream_t s) {
-    dim3 grid((2 * a.nq + 127) / 128, 2);
+    const int nq = a.nq[0] > a.nq[1] ? a.nq[0] : a.nq[1];
+    dim3 grid((2 * nq + 127) / 128, 2);
     ghost_kernel<<<grid, 128, 0, s>>>(a);
     return cudaGetLastError();
 }

@@ -60,6 +60,8 @@ struct DevBlock {
     int32_t index;         // block index i of BlockIndex (i, 0)
     int32_t nr_in_nbr;     // rows of the inner neighbour
     int32_t nr_out_nbr;    // rows of the outer neighbour
+    int32_t slot_in;       // slot of the inner neighbour, -1 at the inner edge
+    int32_t slot_out;      // slot of the outer neighbour, -1 at the outer edge
     int32_t pad_;
 };
 
@@ -107,12 +109,12 @@ struct GhostArgs {
     void* P[2];             // target P of the innermost / outermost block
     int32_t row0[2];        // first target row (0 for inner, nr+2 for outer)
     int32_t nr_t[2];        // target block rows (row stride nr+4)
-    int32_t nq;
+    int32_t nq[2];          // polar zones of the innermost / outermost block
     int32_t ghost_index[2];
     const double* rc;       // [2 ends][2 rows]
-    const double* dv;       // [2 ends][2 rows][nq]
-    const double* qc;       // [nq]
-    const double* host_prim;// [2][2][nq][5] model values from a host callback, or null
+    const double* dv[2];    // per end [2 rows][nq]
+    const double* qc[2];    // per end [nq]
+    const double* host_prim[2]; // per end [2][nq][5] model values from a host callback, or null
     knc_model_params model;
     double time;
     int32_t srhd;
@@ -151,6 +153,11 @@ cudaError_t launch_c2p_mixed(const StageArgs& a, cudaStream_t s);
 cudaError_t launch_update_mixed(const StageArgs& a, cudaStream_t s);
 cudaError_t launch_aos_to_soa(const double* aos, const double* scalar, double* soa, int64_t nr, int64_t nq,
                               cudaStream_t s);
+// Halo rows across a change of polar resolution (power-of-two ratio).
+// remap = {target slot, source slot, side (0: target rows 0-1 from the source's
+// last two rows; 1: target rows nr+2..nr+3 from the source's first two)}.
+cudaError_t launch_remap(const StageArgs& a, const int4* remap, int nremap, int max_nq, bool single_precision,
+                         cudaStream_t s);
 cudaError_t launch_prims_to_aos(const void* P, double* out, int64_t nr, int64_t nq, cudaStream_t s);
 cudaError_t launch_soa_to_aos(const double* soa, double* aos, double* scalar, int64_t nr, int64_t nq,
                               cudaStream_t s);

@@ -161,6 +161,8 @@ SIGNATURES = {
     "knc_num_blocks": (C.c_int, [_P, _I32P]),
     "knc_block_indexes": (C.c_int, [_P, _I32P, C.c_int32]),
     "knc_block_shape": (C.c_int, [_P, _I64P, _I64P]),
+    "knc_set_block_shapes": (C.c_int, [_P, C.c_int32, C.c_int32, _I32P, _I32P]),
+    "knc_block_shape_of": (C.c_int, [_P, C.c_int32, _I64P, _I64P]),
     "knc_set_state": (C.c_int, [_P, _DP, _DP]),
     "knc_get_state": (C.c_int, [_P, _DP, _DP]),
     "knc_set_time": (C.c_int, [_P, C.c_double, C.c_int64, C.c_int64]),

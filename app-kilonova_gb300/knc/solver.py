@@ -112,11 +112,28 @@ class Solver:
     def init_from_model(self, time: float = 0.0):
         self._check(self.lib.knc_init_from_model(self.h, float(time)), "init_from_model")
 
+    def set_block_shapes(self, first: int, nr, nq):
+        """Uneven blocks: indexes first, first+1, ... get (nr[k], nq[k]) zones."""
+        nr = np.ascontiguousarray(nr, dtype=np.int32)
+        nq = np.ascontiguousarray(nq, dtype=np.int32)
+        if nr.shape != nq.shape or nr.ndim != 1:
+            raise ValueError("nr and nq must be 1-d arrays of the same length")
+        i32 = C.POINTER(C.c_int32)
+        self._check(self.lib.knc_set_block_shapes(self.h, int(first), nr.size, nr.ctypes.data_as(i32),
+                                                  nq.ctypes.data_as(i32)), "set_block_shapes")
+
+    def shape_of(self, index: int):
+        nr = C.c_int64()
+        nq = C.c_int64()
+        self._check(self.lib.knc_block_shape_of(self.h, int(index), C.byref(nr), C.byref(nq)), "shape_of")
+        return nr.value, nq.value
+
     def add_block(self, index: int, cons, scalar):
         cons = np.ascontiguousarray(cons, dtype=np.float64)
         scalar = np.ascontiguousarray(scalar, dtype=np.float64)
-        if cons.shape != (self.nr, self.nq, 4) or scalar.shape != (self.nr, self.nq):
-            raise ValueError(f"block arrays must be ({self.nr}, {self.nq}, 4) and ({self.nr}, {self.nq})")
+        nr, nq = self.shape_of(index)
+        if cons.shape != (nr, nq, 4) or scalar.shape != (nr, nq):
+            raise ValueError(f"block arrays must be ({nr}, {nq}, 4) and ({nr}, {nq})")
         self._check(self.lib.knc_add_block(self.h, int(index), abi.dptr(cons), abi.dptr(scalar)), "add_block")
 
     def remove_block(self, index: int):
@@ -130,8 +147,9 @@ class Solver:
         return [out[k] for k in range(n.value)]
 
     def get_block(self, index: int):
-        cons = np.empty((self.nr, self.nq, 4))
-        scalar = np.empty((self.nr, self.nq))
+        nr, nq = self.shape_of(index)
+        cons = np.empty((nr, nq, 4))
+        scalar = np.empty((nr, nq))
         self._check(self.lib.knc_get_block(self.h, int(index), abi.dptr(cons), abi.dptr(scalar)), "get_block")
         return cons, scalar
 
@@ -146,7 +164,7 @@ class Solver:
 
     def get_primitives(self, index: int):
         """(rho, u_r, u_theta, p, scalar concentration) of a block, [nr, nq, 5]."""
-        out = np.empty((self.nr, self.nq, 5))
+        out = np.empty(self.shape_of(index) + (5,))
         self._check(self.lib.knc_get_primitives(self.h, int(index), abi.dptr(out)), "get_primitives")
         return out
 

@@ -184,6 +184,21 @@ int knc_num_blocks(const knc_ctx* ctx, int32_t* n);
 int knc_block_indexes(const knc_ctx* ctx, int32_t* out, int32_t capacity);
 int knc_block_shape(const knc_ctx* ctx, int64_t* nr, int64_t* nq);
 
+/* Uneven blocks (no counterpart in the reference, whose blocks all have
+ * Mesh::block_size x num_polar_zones zones, src/mesh.rs:84-113): indexes
+ * [first, first + count) get nr[k] radial and nq[k] polar zones over the same
+ * radial extent; other indexes keep the mesh's shape. nq must be the mesh's
+ * num_polar_zones times a power of two (so polar grids nest), nr in
+ * [2, 16383]. Where neighbours differ in nq, the halo rows are remapped: a
+ * finer neighbour's zones merged conservatively and recovered, a coarser one's
+ * copied. Set shapes before the blocks become live (init, add, activation);
+ * changing the shape of a live block is KNC_ERR_INVALID_ARGUMENT. Block
+ * arrays of knc_add_block / knc_get_block / the state copies use each block's
+ * own shape. */
+int knc_set_block_shapes(knc_ctx* ctx, int32_t first, int32_t count, const int32_t* nr,
+                         const int32_t* nq);
+int knc_block_shape_of(const knc_ctx* ctx, int32_t index, int64_t* nr, int64_t* nq);
+
 /* Whole-state copies for host-resident drivers: blocks in ascending index
  * order, each [nr][nq][4] then [nr][nq]; sizes must match the live state. */
 int knc_set_state(knc_ctx* ctx, const double* cons_aos, const double* scalar_mass);

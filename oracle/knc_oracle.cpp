@@ -33,6 +33,7 @@
 #include <cstring>
 #include <limits>
 #include <map>
+#include <tuple>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -462,10 +463,9 @@ struct Geometry {             // GridGeometry, mesh.rs:22-29 (+ cot of centroid)
     std::vector<double> rv, qv, ar, aq, dv, rc, qc, cot;
 };
 
-Geometry make_geometry(const MeshDef& M, int32_t index) {   // mesh.rs:246-264
+Geometry make_geometry(const MeshDef& M, int32_t index, int64_t nr, int64_t nq) {   // mesh.rs:246-264
     Geometry G;
     const Extent e = M.subgrid_extent(index);
-    const int64_t nr = M.p.block_size, nq = M.p.num_polar_zones;
     G.nr = nr;
     G.nq = nq;
     G.rv.resize(nr + 1);
@@ -688,17 +688,30 @@ struct oracle_ctx {
     double time = 0.0;
     Rational iteration;
     std::map<int32_t, Block> blocks;
-    std::map<int32_t, Geometry> geom;
+    std::map<std::tuple<int32_t, int64_t, int64_t>, Geometry> geom;
+    std::map<int32_t, std::pair<int64_t, int64_t>> shapes;   // uneven blocks: index -> (nr, nq)
     ErrorRec err;
     std::atomic<int64_t> c2p_zones{0}, c2p_iters{0};
 };
 
 namespace {
 
-const Geometry& geometry_of(oracle_ctx* c, int32_t index) {
-    auto it = c->geom.find(index);
-    if (it == c->geom.end()) it = c->geom.emplace(index, make_geometry(c->mesh, index)).first;
+std::pair<int64_t, int64_t> shape_of(const oracle_ctx* c, int32_t index) {
+    auto it = c->shapes.find(index);
+    if (it != c->shapes.end()) return it->second;
+    return {c->mesh.p.block_size, c->mesh.p.num_polar_zones};
+}
+
+const Geometry& geometry_of(oracle_ctx* c, int32_t index, int64_t nr, int64_t nq) {
+    const auto key = std::make_tuple(index, nr, nq);
+    auto it = c->geom.find(key);
+    if (it == c->geom.end()) it = c->geom.emplace(key, make_geometry(c->mesh, index, nr, nq)).first;
     return it->second;
+}
+
+const Geometry& geometry_of(oracle_ctx* c, int32_t index) {
+    const auto sh = shape_of(c, index);
+    return geometry_of(c, index, sh.first, sh.second);
 }
 
 template <class F>
@@ -777,27 +790,70 @@ bool block_to_primitive(oracle_ctx* c, int32_t index, const Block& B, const Geom
 
 // scheme.rs:68-158 for one block: halo assembly, PLM in r and theta, Godunov
 // fluxes times face areas, sources times volume, conserved update.
-void block_update(oracle_ctx* c, const Block& B, const Geometry& G, const PrimBlock& pl,
-                  const PrimBlock& p0, const PrimBlock& pr, double dt, Block& out) {
+// Halo value at column j of a block with nq columns, from row `row` of a
+// neighbour with nq_n columns (a power-of-two ratio; the reference has one
+// polar resolution everywhere, so this is the uneven-block extension):
+//  - a finer neighbour: its R = nq_n / nq zones are merged conservatively
+//    (volume integrals and volumes summed in column order) and recovered;
+//  - a coarser neighbour: its zone j / R is copied (piecewise constant).
+void halo_value(oracle_ctx* c, int64_t nq, int64_t j, const PrimBlock& pn, const Block* bn, const Geometry* gn,
+                int64_t nq_n, int64_t row, Prim& P, double& s) {
+    if (nq_n == nq) {
+        P = pn.P[row * nq + j];
+        s = pn.s[row * nq + j];
+        return;
+    }
+    if (nq_n < nq) {
+        const int64_t z = row * nq_n + j / (nq / nq_n);
+        P = pn.P[z];
+        s = pn.s[z];
+        return;
+    }
+    const int64_t R = nq_n / nq;
+    double U[5] = {0, 0, 0, 0, 0}, dv = 0.0;
+    for (int64_t m = 0; m < R; ++m) {
+        const int64_t z = row * nq_n + j * R + m;
+        for (int q = 0; q < 4; ++q) U[q] += bn->U[z * 4 + q];
+        U[4] += bn->S[z];
+        dv += gn->dv[z];
+    }
+    Cons u;
+    for (int q = 0; q < 4; ++q) u.v[q] = U[q] / dv;
+    double bad;
+    int it = 0;
+    if (c->ph.system == KNC_SYSTEM_RELATIVISTIC) srhd_c2p(c->ph, u, 0.0, P, it, bad);
+    else newt_c2p(c->ph, u, P, bad);
+    s = U[4] / dv / lorentz_factor(c->ph, P);
+}
+
+struct Neighbour {
+    const PrimBlock* prims;
+    const Block* block;        // conserved state (null for a ghost block)
+    const Geometry* geom;
+    int64_t nr, nq;
+};
+
+void block_update(oracle_ctx* c, const Block& B, const Geometry& G, const Neighbour& L, const PrimBlock& p0,
+                  const Neighbour& Rn, double dt, Block& out) {
     const Phys& ph = c->ph;
     const bool srhd = ph.system == KNC_SYSTEM_RELATIVISTIC;
     const double cflux = srhd ? LIGHT_SPEED : 1.0;
     const int64_t nr = G.nr, nq = G.nq;
-    const int64_t nl = (int64_t)pl.P.size() / nq, nrr = (int64_t)pr.P.size() / nq;
-    (void)nrr;
     // pe: rows pl[-2..], p0, pr[..2]  (scheme.rs:76-77)
     const int64_t ne = nr + 4;
     std::vector<Prim> pe(ne * nq);
     std::vector<double> se(ne * nq);
     for (int64_t k = 0; k < ne; ++k)
         for (int64_t j = 0; j < nq; ++j) {
-            const Prim* P;
-            double s;
-            if (k < 2) { const int64_t z = (nl - 2 + k) * nq + j; P = &pl.P[z]; s = pl.s[z]; }
-            else if (k < nr + 2) { const int64_t z = (k - 2) * nq + j; P = &p0.P[z]; s = p0.s[z]; }
-            else { const int64_t z = (k - nr - 2) * nq + j; P = &pr.P[z]; s = pr.s[z]; }
-            pe[k * nq + j] = *P;
-            se[k * nq + j] = s;
+            if (k < 2) {
+                halo_value(c, nq, j, *L.prims, L.block, L.geom, L.nq, L.nr - 2 + k, pe[k * nq + j], se[k * nq + j]);
+            } else if (k < nr + 2) {
+                const int64_t z = (k - 2) * nq + j;
+                pe[k * nq + j] = p0.P[z];
+                se[k * nq + j] = p0.s[z];
+            } else {
+                halo_value(c, nq, j, *Rn.prims, Rn.block, Rn.geom, Rn.nq, k - nr - 2, pe[k * nq + j], se[k * nq + j]);
+            }
         }
     const double th = ph.plm_theta;
     // radial gradients gx: rows 0..nr+2 centred on pe rows 1..nr+2 (scheme.rs:79-80)
@@ -907,8 +963,12 @@ bool stage(oracle_ctx* c, const StateView& s, double dt, StateView& out) {
     std::vector<int32_t> idx;
     for (auto& kv : s.blocks) idx.push_back(kv.first);
     const int32_t lo = idx.front() - 1, hi = idx.back() + 1;   // state.rs:128-130
-    // geometry must exist before threads read the map
-    for (int32_t k = lo; k <= hi; ++k) geometry_of(c, k);
+    // ghost blocks take their own radial shape and the adjacent live block's
+    // polar resolution; geometry must exist before threads read the map
+    std::map<int32_t, const Geometry*> gmap;
+    for (int32_t k = idx.front(); k <= idx.back(); ++k) gmap[k] = &geometry_of(c, k);
+    gmap[lo] = &geometry_of(c, lo, shape_of(c, lo).first, gmap[idx.front()]->nq);
+    gmap[hi] = &geometry_of(c, hi, shape_of(c, hi).first, gmap[idx.back()]->nq);
     std::map<int32_t, PrimBlock> prims;
     for (int32_t k = lo; k <= hi; ++k) prims[k];
     std::vector<ErrorRec> errs(idx.size() + 2);
@@ -921,10 +981,10 @@ bool stage(oracle_ctx* c, const StateView& s, double dt, StateView& out) {
         if (k < (int64_t)idx.size()) { bi = idx[k]; B = &s.blocks.at(bi); }
         else {
             bi = k == (int64_t)idx.size() ? lo : hi;
-            ghost = block_from_model(c, bi, c->geom.at(bi), s.time, false);
+            ghost = block_from_model(c, bi, *gmap.at(bi), s.time, false);
             B = &ghost;
         }
-        ok[k] = block_to_primitive(c, bi, *B, c->geom.at(bi), prims.at(bi), errs[k]);
+        ok[k] = block_to_primitive(c, bi, *B, *gmap.at(bi), prims.at(bi), errs[k]);
     });
     for (size_t k = 0; k < ok.size(); ++k)
         if (!ok[k]) {
@@ -940,8 +1000,12 @@ bool stage(oracle_ctx* c, const StateView& s, double dt, StateView& out) {
     for (int32_t b : idx) out.blocks[b];
     parallel_for(c->threads, (int64_t)idx.size(), [&](int64_t k) {
         const int32_t b = idx[k];
-        block_update(c, s.blocks.at(b), c->geom.at(b), prims.at(b - 1), prims.at(b), prims.at(b + 1),
-                     dt, out.blocks.at(b));
+        auto nb = [&](int32_t n) {
+            const Geometry* g = gmap.at(n);
+            auto it = s.blocks.find(n);
+            return Neighbour{&prims.at(n), it == s.blocks.end() ? nullptr : &it->second, g, g->nr, g->nq};
+        };
+        block_update(c, s.blocks.at(b), *gmap.at(b), nb(b - 1), prims.at(b), nb(b + 1), dt, out.blocks.at(b));
     });
     out.time = s.time + dt;
     Rational one;
@@ -1074,9 +1138,10 @@ int oracle_init_from_model(oracle_ctx* c, double time) {
         idx.push_back(i);
         if (i > 1000000) return KNC_ERR_CONFIG;
     }
-    for (int32_t i : idx) { geometry_of(c, i); c->blocks[i]; }
+    std::vector<const Geometry*> gs;
+    for (int32_t i : idx) { gs.push_back(&geometry_of(c, i)); c->blocks[i]; }
     parallel_for(c->threads, (int64_t)idx.size(), [&](int64_t k) {
-        c->blocks.at(idx[k]) = block_from_model(c, idx[k], c->geom.at(idx[k]), time, true);
+        c->blocks.at(idx[k]) = block_from_model(c, idx[k], *gs[k], time, true);
     });
     c->time = time;
     c->iteration.n = 0;
@@ -1086,12 +1151,37 @@ int oracle_init_from_model(oracle_ctx* c, double time) {
 
 int oracle_add_block(oracle_ctx* c, int32_t index, const double* cons, const double* scalar) {
     if (!c || !cons || !scalar) return KNC_ERR_INVALID_ARGUMENT;
-    const int64_t n = c->mesh.p.block_size * c->mesh.p.num_polar_zones;
+    const auto sh = shape_of(c, index);
+    const int64_t n = sh.first * sh.second;
     Block B;
     B.U.assign(cons, cons + n * 4);
     B.S.assign(scalar, scalar + n);
     geometry_of(c, index);
     c->blocks[index] = std::move(B);
+    return KNC_OK;
+}
+
+int oracle_set_block_shapes(oracle_ctx* c, int32_t first, int32_t count, const int32_t* nr, const int32_t* nq) {
+    if (!c || count < 0 || (count && (!nr || !nq))) return KNC_ERR_INVALID_ARGUMENT;
+    const int64_t nq0 = c->mesh.p.num_polar_zones;
+    for (int32_t k = 0; k < count; ++k) {
+        // nq = nq0 * 2^m, so the polar grids of any two blocks nest
+        int64_t a = nq0, b = nq[k];
+        while (a > 0 && b > 0 && a != b && ((a < b && b % 2 == 0) || (a > b && a % 2 == 0))) {
+            if (a < b) b /= 2;
+            else a /= 2;
+        }
+        if (nr[k] < 2 || a != b || (nq0 != 1 && nq[k] < 16) || (nq0 == 1 && nq[k] != 1)) return KNC_ERR_CONFIG;
+    }
+    for (int32_t k = 0; k < count; ++k) c->shapes[first + k] = {nr[k], nq[k]};
+    return KNC_OK;
+}
+
+int oracle_block_shape_of(const oracle_ctx* c, int32_t index, int64_t* nr, int64_t* nq) {
+    if (!c) return KNC_ERR_INVALID_ARGUMENT;
+    const auto sh = shape_of(c, index);
+    if (nr) *nr = sh.first;
+    if (nq) *nq = sh.second;
     return KNC_OK;
 }
 
@@ -1147,10 +1237,15 @@ int oracle_time_step(oracle_ctx* c, double* dt) {
     if (!c || !dt || c->blocks.empty()) return KNC_ERR_INVALID_ARGUMENT;
     const bool global = c->ph.system == KNC_SYSTEM_RELATIVISTIC && !c->hp.adaptive_time_step;
     if (global) {
-        const int32_t inner = c->blocks.begin()->first;
-        const Extent e = c->mesh.subgrid_extent(inner);
-        const int64_t nr = c->mesh.p.block_size;
-        const double spacing = vertex_r(e, nr, 1) - vertex_r(e, nr, 0);   // mesh.rs:304-307
+        // smallest_spacing of the innermost block (mesh.rs:304-307); with
+        // uneven blocks the minimum over all blocks, which for equal shapes is
+        // always the innermost block's
+        double spacing = std::numeric_limits<double>::max();
+        for (auto& kv : c->blocks) {
+            const Extent e = c->mesh.subgrid_extent(kv.first);
+            const int64_t nr = shape_of(c, kv.first).first;
+            spacing = std::min(spacing, vertex_r(e, nr, 1) - vertex_r(e, nr, 0));
+        }
         *dt = c->hp.cfl_number * spacing / LIGHT_SPEED;
         return KNC_OK;
     }
@@ -1275,7 +1370,7 @@ int oracle_block_geometry(const knc_mesh_params* m, int32_t index, double* rv, d
     if (!m) return KNC_ERR_INVALID_ARGUMENT;
     MeshDef M;
     M.p = *m;
-    const Geometry G = make_geometry(M, index);
+    const Geometry G = make_geometry(M, index, m->block_size, m->num_polar_zones);
     if (rv) std::memcpy(rv, G.rv.data(), G.rv.size() * sizeof(double));
     if (qv) std::memcpy(qv, G.qv.data(), G.qv.size() * sizeof(double));
     if (ar) std::memcpy(ar, G.ar.data(), G.ar.size() * sizeof(double));

@@ -36,6 +36,12 @@ int oracle_init_from_model(oracle_ctx* ctx, double time);
 int oracle_add_block(oracle_ctx* ctx, int32_t index, const double* cons_aos,
                      const double* scalar_mass);
 int oracle_remove_block(oracle_ctx* ctx, int32_t index);
+/* Uneven blocks: shapes (nr, nq) of indexes [first, first + count); other
+ * indexes keep (block_size, num_polar_zones). Neighbouring polar resolutions
+ * must differ by a power of two (halo rows are remapped, see knc_oracle.cpp). */
+int oracle_set_block_shapes(oracle_ctx* ctx, int32_t first, int32_t count, const int32_t* nr,
+                            const int32_t* nq);
+int oracle_block_shape_of(const oracle_ctx* ctx, int32_t index, int64_t* nr, int64_t* nq);
 int oracle_get_block(oracle_ctx* ctx, int32_t index, double* cons_aos,
                      double* scalar_mass);
 int oracle_num_blocks(const oracle_ctx* ctx, int32_t* n);

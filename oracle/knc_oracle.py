@@ -46,6 +46,8 @@ def load():
         "oracle_init_from_model": (C.c_int, [P, C.c_double]),
         "oracle_add_block": (C.c_int, [P, C.c_int32, DP, DP]),
         "oracle_remove_block": (C.c_int, [P, C.c_int32]),
+        "oracle_set_block_shapes": (C.c_int, [P, C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+        "oracle_block_shape_of": (C.c_int, [P, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
         "oracle_get_block": (C.c_int, [P, C.c_int32, DP, DP]),
         "oracle_num_blocks": (C.c_int, [P, C.POINTER(C.c_int32)]),
         "oracle_block_indexes": (C.c_int, [P, C.POINTER(C.c_int32), C.c_int32]),
@@ -127,6 +129,19 @@ class Oracle:
     def remove_block(self, index):
         self._check(self.lib.oracle_remove_block(self.h, index), "remove_block")
 
+    def set_block_shapes(self, first, nr, nq):
+        nr = np.ascontiguousarray(nr, dtype=np.int32)
+        nq = np.ascontiguousarray(nq, dtype=np.int32)
+        i32 = C.POINTER(C.c_int32)
+        self._check(self.lib.oracle_set_block_shapes(self.h, first, len(nr), nr.ctypes.data_as(i32),
+                                                     nq.ctypes.data_as(i32)), "set_block_shapes")
+
+    def shape_of(self, index):
+        a = C.c_int64()
+        b = C.c_int64()
+        self.lib.oracle_block_shape_of(self.h, index, C.byref(a), C.byref(b))
+        return a.value, b.value
+
     def block_indexes(self):
         n = C.c_int32()
         self.lib.oracle_num_blocks(self.h, C.byref(n))
@@ -135,8 +150,9 @@ class Oracle:
         return [out[k] for k in range(n.value)]
 
     def get_block(self, index):
-        cons = np.empty((self.nr, self.nq, 4))
-        scalar = np.empty((self.nr, self.nq))
+        nr, nq = self.shape_of(index)
+        cons = np.empty((nr, nq, 4))
+        scalar = np.empty((nr, nq))
         self._check(self.lib.oracle_get_block(self.h, index, _d(cons), _d(scalar)), "get_block")
         return cons, scalar
 
