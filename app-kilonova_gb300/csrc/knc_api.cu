@@ -215,6 +215,13 @@ struct Layout {
     int4* d_tiles = nullptr;
     int tiles_cap = 0;
     int ntiles = 0;
+    int4* d_utiles = nullptr;   // update tiles of `utr` rows
+    int utiles_cap = 0;
+    int nutiles = 0;
+    int utr = 0;
+    int4* d_chunks = nullptr;   // fused recovery chunks {slot, z0, nz, 0} of <= stage_threads(utr) zones
+    int chunks_cap = 0;
+    int nchunks = 0;
     // halo remaps across polar-resolution changes
     int4* d_remap = nullptr;
     int remap_cap = 0;
@@ -239,6 +246,8 @@ struct Layout {
 void free_layout(Layout& l) {
     cudaFree(l.d_table);
     cudaFree(l.d_tiles);
+    cudaFree(l.d_utiles);
+    cudaFree(l.d_chunks);
     cudaFree(l.d_remap);
     cudaFree(l.d_ghost_rc);
     cudaFree(l.d_ghost_dv[0]);
@@ -292,6 +301,12 @@ struct knc_ctx {
     int32_t precision = KNC_PRECISION_FP64;
     int32_t guess = KNC_GUESS_PLAIN;
     int32_t batched = 0;
+    int32_t utr = 8;   // update tile rows (4, 8 or 16)
+    int32_t fused = 0;         // one cooperative launch per stage
+    int32_t ctas_per_sm = 0;   // fused grid: CTAs per SM (0: the occupancy bound)
+    int32_t sms = 0;
+    bool coop = false;         // the device supports cooperative launches
+    unsigned long long bar_epoch = 0;   // grid-barrier arrivals issued since the status reset
     double w_split = 2.0;
     float* d_mlp = nullptr;
     // bookkeeping
@@ -299,8 +314,8 @@ struct knc_ctx {
     bool profiling = false;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_events;
     std::vector<cudaEvent_t> event_pool;
-    double prof_ms[KNC_KERNEL_KINDS] = {0, 0, 0};
-    int64_t prof_count[KNC_KERNEL_KINDS] = {0, 0, 0};
+    double prof_ms[KNC_KERNEL_KINDS] = {};
+    int64_t prof_count[KNC_KERNEL_KINDS] = {};
     bool capturing = false;
     cudaGraphExec_t graph_exec = nullptr;
     cudaEvent_t marks[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -470,10 +485,11 @@ void release_block(knc_ctx* c, BlockH& b) {
 
 // Rebuild the device block table and the tile list after the block set changed.
 int rebuild_table(knc_ctx* c) {
-    if (!c->dirty) return KNC_OK;
+    if (!c->dirty && L(c).utr == c->utr) return KNC_OK;
     const int nb = (int)c->blocks.size();
     std::vector<DevBlock> tab(nb);
-    std::vector<int4> tiles;
+    std::vector<int4> tiles, utiles, chunks;
+    const int nt = stage_threads(c->utr);
     L(c).slot_index.clear();
     int slot = 0;
     int64_t zoff = 0;
@@ -531,6 +547,10 @@ int rebuild_table(knc_ctx* c) {
         for (int64_t i0 = 0; i0 < b.nr; i0 += TILE_R)
             for (int64_t j0 = 0; j0 < b.nq; j0 += TILE_Q)
                 tiles.push_back(make_int4(slot, (int)i0, (int)j0, (int)zoff));
+        for (int64_t i0 = 0; i0 < b.nr; i0 += c->utr)
+            for (int64_t j0 = 0; j0 < b.nq; j0 += TILE_Q) utiles.push_back(make_int4(slot, (int)i0, (int)j0, 0));
+        for (int64_t z0 = 0; z0 < b.nr * b.nq; z0 += nt)
+            chunks.push_back(make_int4(slot, (int)z0, (int)std::min<int64_t>(nt, b.nr * b.nq - z0), 0));
         L(c).slot_index.push_back(b.index);
         zoff += b.nr * b.nq;
         prev = &b;
@@ -551,6 +571,27 @@ int rebuild_table(knc_ctx* c) {
     if (nb) CK(cudaMemcpyAsync(L(c).d_table, tab.data(), nb * sizeof(DevBlock), cudaMemcpyHostToDevice, c->stream));
     if (!tiles.empty())
         CK(cudaMemcpyAsync(L(c).d_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
+    if ((int)utiles.size() > L(c).utiles_cap) {
+        cudaFree(L(c).d_utiles);
+        L(c).d_utiles = nullptr;
+        CK(dalloc(&L(c).d_utiles, utiles.size()));
+        L(c).utiles_cap = (int)utiles.size();
+    }
+    if (!utiles.empty())
+        CK(cudaMemcpyAsync(L(c).d_utiles, utiles.data(), utiles.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                           c->stream));
+    L(c).nutiles = (int)utiles.size();
+    L(c).utr = c->utr;
+    if ((int)chunks.size() > L(c).chunks_cap) {
+        cudaFree(L(c).d_chunks);
+        L(c).d_chunks = nullptr;
+        CK(dalloc(&L(c).d_chunks, chunks.size()));
+        L(c).chunks_cap = (int)chunks.size();
+    }
+    if (!chunks.empty())
+        CK(cudaMemcpyAsync(L(c).d_chunks, chunks.data(), chunks.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                           c->stream));
+    L(c).nchunks = (int)chunks.size();
     if ((int)remaps.size() > L(c).remap_cap) {
         cudaFree(L(c).d_remap);
         L(c).d_remap = nullptr;
@@ -698,6 +739,9 @@ StageArgs base_args(knc_ctx* c) {
     a.blocks = L(c).d_table;
     a.tiles = L(c).d_tiles;
     a.ntiles = L(c).ntiles;
+    a.utiles = L(c).d_utiles;
+    a.nutiles = L(c).nutiles;
+    a.utr = L(c).utr;
     a.srhd = c->hp.system == KNC_SYSTEM_RELATIVISTIC;
     a.hllc = c->hp.riemann_solver == KNC_RIEMANN_HLLC;
     a.one_dimensional = c->mesh.p.num_polar_zones == 1;
@@ -728,6 +772,23 @@ int launch_update(knc_ctx* c, const StageArgs& a) {
     ++c->launches;
     CK(e);
     return KNC_OK;
+}
+
+// CTAs of a fused launch: ctas_per_sm (or the occupancy bound) x SMs, no more
+// than the largest phase has work items.
+int fused_grid(knc_ctx* c) {
+    int per_sm = 1;
+    const bool mlp = c->guess == KNC_GUESS_MLP && c->d_mlp;
+    const cudaError_t e = mixed(c) ? fused_max_ctas_mixed(mlp, c->utr, &per_sm)
+                                   : fused_max_ctas_f64(mlp && c->hp.system == KNC_SYSTEM_RELATIVISTIC, c->utr, &per_sm);
+    if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+    if (c->ctas_per_sm > 0 && c->ctas_per_sm < per_sm) per_sm = c->ctas_per_sm;
+    const Layout& l = L(c);
+    const int nt = stage_threads(c->utr);
+    const int need_a = (int)(2 * l.nq_edge[0] + nt - 1) / nt + (int)(2 * l.nq_edge[1] + nt - 1) / nt + l.nchunks;
+    const int need_b = (int)(((int64_t)l.nremap * 2 * l.max_nq + nt - 1) / nt);
+    const int need = std::max(std::max(need_a, need_b), std::max(l.nutiles, 1));
+    return std::min(per_sm * c->sms, need);
 }
 
 // One Euler stage U_out = avg(U_in + dt L(U_in), U_base), src/scheme.rs:16-173.
@@ -764,11 +825,6 @@ int run_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, doub
         g.host_prim[0] = c->d_host_prim;
         g.host_prim[1] = c->d_host_prim + 2 * L(c).ghost_nq[0] * 5;
     }
-    {
-        ProfScope ps(c, KNC_KERNEL_GHOST);
-        CK(launch_ghost(g, c->stream));
-    }
-    ++c->launches;
     StageArgs a = base_args(c);
     a.stage = stage;
     a.sel_in = sel_in;
@@ -777,9 +833,33 @@ int run_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, doub
     a.w1 = w1;
     a.bf = bf;
     a.dt = dt;
+    if (c->fused) {
+        // the whole stage in one cooperative launch (grid barriers between phases)
+        FusedArgs f;
+        std::memset(&f, 0, sizeof(f));
+        f.chunks = lay.d_chunks;
+        f.nchunks = lay.nchunks;
+        f.nremap = lay.nremap;
+        f.remap = lay.d_remap;
+        f.max_nq = lay.max_nq;
+        f.bar_base = c->bar_epoch;
+        const int grid = fused_grid(c);
+        c->bar_epoch += (unsigned long long)grid * (lay.nremap ? 2u : 1u);
+        ProfScope ps(c, KNC_KERNEL_FUSED);
+        CK(mixed(c) ? launch_stage_fused_mixed(a, g, f, grid, c->stream)
+                    : launch_stage_fused_f64(a, g, f, grid, c->stream));
+        ++c->launches;
+        return KNC_OK;
+    }
+    {
+        ProfScope ps(c, KNC_KERNEL_GHOST);
+        CK(mixed(c) ? launch_ghost_mixed(g, c->stream) : launch_ghost_f64(g, c->stream));
+    }
+    ++c->launches;
     if ((r = launch_c2p(c, a))) return r;
-    if (L(c).nremap) {
-        CK(launch_remap(a, L(c).d_remap, L(c).nremap, L(c).max_nq, mixed(c), c->stream));
+    if (lay.nremap) {
+        CK(mixed(c) ? launch_remap_mixed(a, lay.d_remap, lay.nremap, lay.max_nq, c->stream)
+                    : launch_remap_f64(a, lay.d_remap, lay.nremap, lay.max_nq, c->stream));
         ++c->launches;
     }
     if ((r = launch_update(c, a))) return r;
@@ -869,6 +949,10 @@ int check_status(knc_ctx* c) {
     CK(cudaMemcpyAsync(c->h_status, c->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     const unsigned long long k = c->h_status->err_key;
+    if (c->h_status->bar_abort) {
+        c->failed = true;
+        return set_msg(c, KNC_ERR_TIMEOUT, "a grid barrier of the fused stage timed out");
+    }
     if (k == NO_ERROR) return KNC_OK;
     c->failed = true;
     const uint32_t slot = (uint32_t)((k >> 34) & 0x3fffu);
@@ -930,6 +1014,9 @@ int reset_status(knc_ctx* c, bool keep_stats) {
     s.err_key = NO_ERROR;
     s.err_sel = 0;
     s.dt_bits = ~0ull;
+    s.bar_count = 0;
+    s.bar_abort = 0;
+    c->bar_epoch = 0;
     CK(cudaMemcpyAsync(c->d_status, &s, sizeof(s), cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     c->stage_counter = 0;
@@ -1097,6 +1184,12 @@ int create_device_side(knc_ctx* c) {
     CK(configure_kernels());
     CK(cudaGetDevice(&c->device));
     CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    {
+        int coop = 0;
+        CK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device));
+        CK(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device));
+        c->coop = coop != 0;
+    }
     CK(dalloc(&c->d_status, 1));
     CK(cudaMallocHost((void**)&c->h_status, sizeof(DevStatus)));
     knc_ctx::ColTab* ct;
@@ -1648,6 +1741,101 @@ int knc_set_c2p_guess(knc_ctx* c, int32_t guess, const float* w, size_t n) {
     CK(cudaMemcpyAsync(c->d_mlp, w, n * 4, cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     c->guess = guess;
+    return KNC_OK;
+}
+
+int knc_set_tuning(knc_ctx* c, const knc_tuning* t) {
+    if (!c || !t) return KNC_ERR_INVALID_ARGUMENT;
+    if (t->tile_rows != 4 && t->tile_rows != 8 && t->tile_rows != 16)
+        return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "tile_rows must be 4, 8 or 16");
+    if (t->ctas_per_sm < 0) return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "ctas_per_sm must be >= 0");
+    if (t->fused && !c->coop)
+        return set_msg(c, KNC_ERR_UNSUPPORTED, "the device has no cooperative launch (fused stage)");
+    c->utr = t->tile_rows;
+    c->fused = t->fused ? 1 : 0;
+    c->ctas_per_sm = t->ctas_per_sm;
+    return KNC_OK;
+}
+
+int knc_get_tuning(const knc_ctx* c, knc_tuning* t) {
+    if (!c || !t) return KNC_ERR_INVALID_ARGUMENT;
+    t->tile_rows = c->utr;
+    t->fused = c->fused;
+    t->ctas_per_sm = c->ctas_per_sm;
+    t->reserved = 0;
+    return KNC_OK;
+}
+
+int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out) {
+    if (!c || reps < 1) return KNC_ERR_INVALID_ARGUMENT;
+    int r;
+    if ((r = check_ready(c))) return r;
+    if ((r = rebuild_table(c))) return r;
+    if ((r = update_ghost_geometry(c))) return r;
+    if ((r = reset_status(c, true))) return r;
+    double dt;
+    if ((r = time_step_impl(c, &dt))) return r;
+    DevStatus saved;
+    CK(cudaMemcpy(&saved, c->d_status, sizeof(saved), cudaMemcpyDeviceToHost));
+    const knc_tuning keep = {c->utr, c->fused, c->ctas_per_sm, 0};
+    std::vector<knc_tuning> cands;
+    for (int tr : {4, 8, 16}) {
+        cands.push_back({tr, 0, 0, 0});
+        if (!c->coop) continue;
+        c->utr = tr;
+        int per_sm = 1;
+        const bool mlp = c->guess == KNC_GUESS_MLP && c->d_mlp;
+        CK(mixed(c) ? fused_max_ctas_mixed(mlp, tr, &per_sm)
+                    : fused_max_ctas_f64(mlp && c->hp.system == KNC_SYSTEM_RELATIVISTIC, tr, &per_sm));
+        for (int k = 1; k <= per_sm && k <= 8; ++k) cands.push_back({tr, 1, k, 0});
+    }
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    knc_tuning best = keep;
+    double best_ms = -1.0;
+    const bool prof = c->profiling;
+    c->profiling = false;
+    for (const knc_tuning& t : cands) {
+        c->utr = t.tile_rows;
+        c->fused = t.fused;
+        c->ctas_per_sm = t.ctas_per_sm;
+        if ((r = rebuild_table(c))) break;
+        // the first stage reads buf[cur] and writes buf[1 - cur]: the state stays
+        if ((r = run_stage(c, c->cur, 1 - c->cur, -1, 1.0, 0.0, c->time, dt))) break;
+        CK(cudaEventRecord(e0, c->stream));
+        for (int k = 0; k < reps && r == KNC_OK; ++k) r = run_stage(c, c->cur, 1 - c->cur, -1, 1.0, 0.0, c->time, dt);
+        CK(cudaEventRecord(e1, c->stream));
+        CK(cudaEventSynchronize(e1));
+        if (r) break;
+        if ((r = check_status(c))) break;
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        const double per = (double)ms / reps;
+        if (best_ms < 0.0 || per < best_ms) {
+            best_ms = per;
+            best = t;
+        }
+        c->stage_counter = 0;
+    }
+    c->profiling = prof;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    saved.bar_count = 0;
+    saved.bar_abort = 0;
+    CK(cudaMemcpy(c->d_status, &saved, sizeof(saved), cudaMemcpyHostToDevice));
+    c->stage_counter = 0;
+    c->bar_epoch = 0;
+    c->utr = best.tile_rows;
+    c->fused = best.fused;
+    c->ctas_per_sm = best.ctas_per_sm;
+    if (r) {
+        c->failed = false;
+        return r;
+    }
+    if ((r = rebuild_table(c))) return r;
+    if (best_out) *best_out = best;
+    if (ms_out) *ms_out = best_ms;
     return KNC_OK;
 }
 

@@ -11,6 +11,8 @@
 // Without FMA contraction every expression rounds exactly like the CPU
 // oracle's, so this path reproduces the reference arithmetic bit for bit
 // wherever the libm-free operations (+ - * / sqrt) are all that is used.
+#include "knc_fused.cuh"
+#include "knc_halo.cuh"
 #include "knc_internal.h"
 #include "knc_mlp.cuh"
 #include "knc_models.cuh"
@@ -21,28 +23,14 @@ namespace knc {
 
 // ---- c2p -------------------------------------------------------------------
 // MLP = true: the Newton recovery starts from the learned pressure guess; the
-// plain guess p = 0 is retried when that start does not converge.
+// plain guess p = 0 is retried when that start does not converge. Every
+// thread of a warp calls zone() together (the guess is a warp-wide inference).
 template <bool MLP>
-__global__ void __launch_bounds__(TILE_THREADS) c2p_f64_kernel(StageArgs a) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
-    if (ek != NO_ERROR && (uint32_t)(ek >> 48) < (uint32_t)a.stage) return;
-    MlpWeights& W = *reinterpret_cast<MlpWeights*>(smem_raw);
-    __nv_bfloat16* act = reinterpret_cast<__nv_bfloat16*>(smem_raw + sizeof(MlpWeights)) +
-                         (threadIdx.x >> 5) * MLP_ACT_ELEMS;
-    if (MLP) {
-        mlp_load(W, a.mlp);
-        __syncthreads();
-    }
-    unsigned long long zones = 0, iters_sum = 0, fbs = 0;
-    double dtz = 1.7976931348623157e308;
-    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
-        const int4 t = a.tiles[tile];
-        const DevBlock& B = a.blocks[t.x];
-        const int i = t.y + threadIdx.x / TILE_Q;
-        const int j = t.z + threadIdx.x % TILE_Q;
+struct F64C2p {
+    static constexpr bool mlp = MLP;
+    __device__ static void zone(const StageArgs& a, int slot, const DevBlock& B, int i, int j, bool active,
+                                MlpWeights& W, __nv_bfloat16* act, C2pStats& st) {
         const int nr = B.nr, nq = B.nq;
-        const bool active = i < nr && j < nq;
         const int64_t n = (int64_t)nr * nq;
         const int64_t z = (int64_t)i * nq + j;
         double u[4] = {1.0, 0.0, 0.0, 1.0};
@@ -63,7 +51,7 @@ __global__ void __launch_bounds__(TILE_THREADS) c2p_f64_kernel(StageArgs a) {
             const double gmax = (a.gm - 1.0) * u[3];
             guess = (ok && g > 0.0) ? fmin(g, gmax) : 0.0;
         }
-        if (!active) continue;
+        if (!active) return;
         double P[4] = {0.0, 0.0, 0.0, 0.0};
         double bad = 0.0;
         int kind, iters = 0;
@@ -71,17 +59,17 @@ __global__ void __launch_bounds__(TILE_THREADS) c2p_f64_kernel(StageArgs a) {
             kind = srhd_c2p_newton(a.gm, u, guess, P, iters, bad);
             if (MLP && kind == HYDRO_ROOT_FINDER_FAILED && guess != 0.0) {
                 int it2 = 0;
-                ++fbs;
+                ++st.fbs;
                 kind = srhd_c2p_newton(a.gm, u, 0.0, P, it2, bad);
                 iters += it2;
             }
         } else {
             kind = newt_c2p(a.gm - 1.0, u, P, bad);
         }
-        ++zones;
-        iters_sum += (unsigned long long)iters;
+        ++st.zones;
+        st.it64 += (unsigned long long)iters;
         if (kind != HYDRO_NONE && kind != HYDRO_NEGATIVE_PRESSURE) {
-            atomicMin(&a.status->err_key, error_key(a.stage, t.x, i, j, kind));
+            atomicMin(&a.status->err_key, error_key(a.stage, slot, i, j, kind));
             a.status->err_sel = a.sel_in;
         }
         const double w = a.srhd ? sqrt(1.0 + P[1] * P[1] + P[2] * P[2]) : 1.0;
@@ -99,147 +87,45 @@ __global__ void __launch_bounds__(TILE_THREADS) c2p_f64_kernel(StageArgs a) {
             const double dq = B.qv[j + 1] - B.qv[j];
             const double dl = fmin(dr, dq * B.rv[i]);
             const double amax = max_signal_speed(ph, P) * a.cflux;
-            dtz = fmin(dtz, dl / amax);
+            st.dtz = fmin(st.dtz, dl / amax);
         }
     }
-    warp_reduce_stats(a.status, zones, iters_sum, 0ull, fbs, dtz, a.compute_dt != 0);
-}
+};
 
-// ---- ghost rows --------------------------------------------------------------
-// blockIdx.y = 0: inner ghost block (min index - 1), its last two rows feed
-// the innermost block's rows 0, 1; blockIdx.y = 1: outer ghost block, its
-// first two rows feed the outermost block's rows nr+2, nr+3.
-__global__ void ghost_kernel(GhostArgs a) {
-    const int end = blockIdx.y;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nq = a.nq[end];
-    if (k >= 2 * nq || a.P[end] == nullptr) return;
-    const int row = k / nq, j = k - row * nq;
-    const double r = a.rc[end * 2 + row];
-    const double q = a.qc[end][j];
-    const double dV = a.dv[end][row * nq + j];
-    double Pm[4];
-    double scalar;
-    if (a.host_prim[end]) {
-        const double* hp = a.host_prim[end] + ((int64_t)row * nq + j) * 5;
-        Pm[0] = hp[0];
-        Pm[1] = hp[1];
-        Pm[2] = hp[2];
-        Pm[3] = hp[3];
-        scalar = hp[4];
-    } else {
-        model_eval(a.model, r, q, a.time, false, a.ghost_index[end], 0, j, Pm, scalar);
-    }
-    PhysT<double> ph;
-    ph.srhd = a.srhd;
-    ph.hllc = 0;
-    ph.gm = a.gm;
-    ph.gm1 = a.gm - 1.0;
-    ph.gh = a.gm / ph.gm1;
-    ph.theta = 1.0;
-    double U[4];
-    prim_to_cons(ph, Pm, U);
-    double Uv[4];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) Uv[c] = U[c] * dV;       // from_model: U dV
-    const double smass = Uv[0] * scalar;                  // lab_frame_mass * scalar
-    double u[4];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) u[c] = Uv[c] / dV;       // try_to_primitive: U / dV
-    double P[4] = {0.0, 0.0, 0.0, 0.0};
-    double bad = 0.0;
-    int iters = 0, kind;
-    if (a.srhd) kind = srhd_c2p_newton(a.gm, u, 0.0, P, iters, bad);
-    else kind = newt_c2p(a.gm - 1.0, u, P, bad);
-    if (kind != HYDRO_NONE && kind != HYDRO_NEGATIVE_PRESSURE) {
-        atomicMin(&a.status->err_key, error_key(a.stage, 0x3ffeu + end, row, j, kind));
-    }
-    const double w = a.srhd ? sqrt(1.0 + P[1] * P[1] + P[2] * P[2]) : 1.0;
-    const double v[NFIELD] = {P[0], P[1], P[2], P[3], smass / dV / w};
-    const int nrt = a.nr_t[end];
-    const int64_t pn = (int64_t)(nrt + 4) * nq;
-    const int64_t off = (int64_t)(a.row0[end] + row) * nq + j;
-    if (a.single_precision) {
-        float* Pd = reinterpret_cast<float*>(a.P[end]);
-#pragma unroll
-        for (int c = 0; c < NFIELD; ++c) Pd[c * pn + off] = (float)v[c];
-    } else {
-        double* Pd = reinterpret_cast<double*>(a.P[end]);
-#pragma unroll
-        for (int c = 0; c < NFIELD; ++c) Pd[c * pn + off] = v[c];
-    }
-}
-
-// ---- halo remap across a change of polar resolution ----------------------------
-// Target column j of a halo row from row `row` of the source block:
-//  - a finer source (R = nq_s / nq_t): conserved volume integrals and volumes
-//    of its R zones summed in column order, then the FP64 recovery (the
-//    reference's Newton from the plain guess) — a conservative merge;
-//  - a coarser source: its primitive at column j / R, copied.
-// blockIdx.y = remap item, blockIdx.x * blockDim.x + threadIdx.x = (row, j).
-template <class R>
-__global__ void remap_kernel(StageArgs a, const int4* __restrict__ items, int nitems) {
+template <bool MLP>
+__global__ void __launch_bounds__(TILE_THREADS) c2p_f64_kernel(StageArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
     if (ek != NO_ERROR && (uint32_t)(ek >> 48) < (uint32_t)a.stage) return;
-    const int4 it = items[blockIdx.y];
-    const DevBlock& T = a.blocks[it.x];
-    const DevBlock& S = a.blocks[it.y];
-    const int side = it.z;
-    const int nq_t = T.nq, nq_s = S.nq;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= 2 * nq_t) return;
-    const int row = k / nq_t, j = k - row * nq_t;
-    const int srow = side == 0 ? S.nr - 2 + row : row;          // source interior row
-    const int trow = side == 0 ? row : T.nr + 2 + row;          // target padded row
-    R v[NFIELD];
-    if (nq_s < nq_t) {
-        const R* Ps = reinterpret_cast<const R*>(S.P);
-        const int64_t pn = (int64_t)(S.nr + 4) * nq_s;
-        const int64_t off = (int64_t)(srow + 2) * nq_s + j / (nq_t / nq_s);
-#pragma unroll
-        for (int q = 0; q < NFIELD; ++q) v[q] = Ps[q * pn + off];
-    } else {
-        const int Rr = nq_s / nq_t;
-        const double* Us = S.buf[a.sel_in];
-        const int64_t n = (int64_t)S.nr * nq_s;
-        double U[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, dv = 0.0;
-        for (int m = 0; m < Rr; ++m) {
-            const int64_t z = (int64_t)srow * nq_s + j * Rr + m;
-#pragma unroll
-            for (int q = 0; q < 5; ++q) U[q] += Us[q * n + z];
-            dv += S.dv[z];
-        }
-        double u[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) u[q] = U[q] / dv;
-        double P[4] = {0.0, 0.0, 0.0, 0.0};
-        double bad = 0.0;
-        int iters = 0, kind;
-        if (a.srhd) kind = srhd_c2p_newton(a.gm, u, 0.0, P, iters, bad);
-        else kind = newt_c2p(a.gm - 1.0, u, P, bad);
-        if (kind != HYDRO_NONE && kind != HYDRO_NEGATIVE_PRESSURE)
-            atomicMin(&a.status->err_key, error_key(a.stage, it.y, srow, j * Rr, kind));
-        const double w = a.srhd ? sqrt(1.0 + P[1] * P[1] + P[2] * P[2]) : 1.0;
-        const double sv = U[4] / dv / w;
-        v[0] = (R)P[0];
-        v[1] = (R)P[1];
-        v[2] = (R)P[2];
-        v[3] = (R)P[3];
-        v[4] = (R)sv;
+    MlpWeights& W = *reinterpret_cast<MlpWeights*>(smem_raw);
+    __nv_bfloat16* act = reinterpret_cast<__nv_bfloat16*>(smem_raw + sizeof(MlpWeights)) +
+                         (threadIdx.x >> 5) * MLP_ACT_ELEMS;
+    if (MLP) {
+        mlp_load(W, a.mlp);
+        __syncthreads();
     }
-    R* Pt = reinterpret_cast<R*>(T.P);
-    const int64_t pt = (int64_t)(T.nr + 4) * nq_t;
-    const int64_t ot = (int64_t)trow * nq_t + j;
-#pragma unroll
-    for (int q = 0; q < NFIELD; ++q) Pt[q * pt + ot] = v[q];
+    C2pStats st;
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        const int4 t = a.tiles[tile];
+        const DevBlock& B = a.blocks[t.x];
+        const int i = t.y + threadIdx.x / TILE_Q;
+        const int j = t.z + threadIdx.x % TILE_Q;
+        F64C2p<MLP>::zone(a, t.x, B, i, j, i < B.nr && j < B.nq, W, act, st);
+    }
+    warp_reduce_stats(a.status, st.zones, st.it64, 0ull, st.fbs, st.dtz, a.compute_dt != 0);
 }
 
-cudaError_t launch_remap(const StageArgs& a, const int4* remap, int nremap, int max_nq, bool single_precision,
-                         cudaStream_t s) {
+// ---- the fused stage (FP64) ----------------------------------------------------
+template <int TR, bool MLP>
+__global__ void __launch_bounds__(update_threads<TR>(), TR == 16 ? 1 : 2) stage_fused_f64_kernel(StageArgs a, GhostArgs g,
+                                                                                  FusedArgs f) {
+    stage_fused_body<double, false, TR, F64C2p<MLP>>(a, g, f);
+}
+
+cudaError_t launch_remap_f64(const StageArgs& a, const int4* remap, int nremap, int max_nq, cudaStream_t s) {
     if (nremap <= 0) return cudaSuccess;
     dim3 grid((2 * max_nq + 127) / 128, nremap);
-    if (single_precision) remap_kernel<float><<<grid, 128, 0, s>>>(a, remap, nremap);
-    else remap_kernel<double><<<grid, 128, 0, s>>>(a, remap, nremap);
+    remap_kernel<double><<<grid, 128, 0, s>>>(a, remap);
     return cudaGetLastError();
 }
 
@@ -349,21 +235,88 @@ cudaError_t launch_c2p_f64(const StageArgs& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+template <int TR>
+static void update_f64(const StageArgs& a, cudaStream_t s) {
+    update_kernel<double, false, TR><<<a.nutiles, update_threads<TR>(), StageSmem<double, TR>::bytes, s>>>(a);
+}
+
 cudaError_t launch_update_f64(const StageArgs& a, cudaStream_t s) {
-    if (a.ntiles <= 0) return cudaSuccess;
-    update_kernel<double, false><<<a.ntiles, TILE_THREADS, StageSmem<double>::bytes, s>>>(a);
+    if (a.nutiles <= 0) return cudaSuccess;
+    switch (a.utr) {
+    case 4: update_f64<4>(a, s); break;
+    case 16: update_f64<16>(a, s); break;
+    default: update_f64<8>(a, s);
+    }
     return cudaGetLastError();
 }
 
+template <int TR, bool MLP>
+static cudaError_t fused_f64(const StageArgs& a, const GhostArgs& g, const FusedArgs& f, int grid, cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(update_threads<TR>());
+    cfg.dynamicSmemBytes = fused_smem_bytes<double, TR, MLP>();
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, stage_fused_f64_kernel<TR, MLP>, a, g, f);
+}
+
+cudaError_t launch_stage_fused_f64(const StageArgs& a, const GhostArgs& g, const FusedArgs& f, int grid,
+                                   cudaStream_t s) {
+    const bool mlp = a.mlp && a.srhd;
+    switch (a.utr) {
+    case 4: return mlp ? fused_f64<4, true>(a, g, f, grid, s) : fused_f64<4, false>(a, g, f, grid, s);
+    case 16: return mlp ? fused_f64<16, true>(a, g, f, grid, s) : fused_f64<16, false>(a, g, f, grid, s);
+    default: return mlp ? fused_f64<8, true>(a, g, f, grid, s) : fused_f64<8, false>(a, g, f, grid, s);
+    }
+}
+
+template <int TR, bool MLP>
+static cudaError_t fused_ctas_f64(int* n) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, stage_fused_f64_kernel<TR, MLP>, update_threads<TR>(),
+                                                         fused_smem_bytes<double, TR, MLP>());
+}
+
+cudaError_t fused_max_ctas_f64(bool mlp, int utr, int* n) {
+    switch (utr) {
+    case 4: return mlp ? fused_ctas_f64<4, true>(n) : fused_ctas_f64<4, false>(n);
+    case 16: return mlp ? fused_ctas_f64<16, true>(n) : fused_ctas_f64<16, false>(n);
+    default: return mlp ? fused_ctas_f64<8, true>(n) : fused_ctas_f64<8, false>(n);
+    }
+}
+
+template <int TR, bool MLP>
+static cudaError_t configure_fused_f64() {
+    return cudaFuncSetAttribute(stage_fused_f64_kernel<TR, MLP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)fused_smem_bytes<double, TR, MLP>());
+}
+
+template <int TR>
+static cudaError_t configure_update_f64() {
+    return cudaFuncSetAttribute(update_kernel<double, false, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)StageSmem<double, TR>::bytes);
+}
+
 cudaError_t configure_f64() {
-    cudaError_t e = cudaFuncSetAttribute(update_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)StageSmem<double>::bytes);
+    cudaError_t e = configure_update_f64<4>();
+    if (e == cudaSuccess) e = configure_update_f64<8>();
+    if (e == cudaSuccess) e = configure_update_f64<16>();
+    if (e == cudaSuccess) e = configure_fused_f64<4, false>();
+    if (e == cudaSuccess) e = configure_fused_f64<8, false>();
+    if (e == cudaSuccess) e = configure_fused_f64<16, false>();
+    if (e == cudaSuccess) e = configure_fused_f64<4, true>();
+    if (e == cudaSuccess) e = configure_fused_f64<8, true>();
+    if (e == cudaSuccess) e = configure_fused_f64<16, true>();
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(c2p_f64_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(sizeof(MlpWeights) + 8 * MLP_ACT_ELEMS * sizeof(__nv_bfloat16)));
 }
 
-cudaError_t launch_ghost(const GhostArgs& a, cudaStream_t s) {
+cudaError_t launch_ghost_f64(const GhostArgs& a, cudaStream_t s) {
     const int nq = a.nq[0] > a.nq[1] ? a.nq[0] : a.nq[1];
     dim3 grid((2 * nq + 127) / 128, 2);
     ghost_kernel<<<grid, 128, 0, s>>>(a);

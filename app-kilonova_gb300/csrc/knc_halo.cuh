@@ -1,0 +1,156 @@
+// knc_halo.cuh — halo rows that do not come from a same-shaped neighbour.
+//
+// ghost_zone: the two ghost blocks' rows next to the mesh ends, from the model
+// at the stage time (src/scheme.rs:45-52 via BlockState::from_model and
+// try_to_primitive): model primitive -> conserved x dV -> / dV -> primitive,
+// the reference's round trip, then the scalar density.
+// remap_zone: a halo row across a change of polar resolution (uneven blocks).
+//
+// Both are included by each stage translation unit, so a path's separate and
+// fused kernels run the same instructions (the FP64 unit is compiled without
+// FMA contraction, the mixed unit with it).
+#pragma once
+
+#include "knc_internal.h"
+#include "knc_models.cuh"
+#include "knc_physics.cuh"
+
+namespace knc {
+
+// Zone k of the 2 x nq[end] ghost rows of end `end` (0: inner ghost block,
+// min index - 1, whose last two rows feed the innermost block's rows 0, 1;
+// 1: outer ghost block, whose first two rows feed rows nr+2, nr+3).
+static __device__ __noinline__ void ghost_zone(const GhostArgs& a, int end, int k) {
+    const int nq = a.nq[end];
+    if (k >= 2 * nq || a.P[end] == nullptr) return;
+    const int row = k / nq, j = k - row * nq;
+    const double r = a.rc[end * 2 + row];
+    const double q = a.qc[end][j];
+    const double dV = a.dv[end][row * nq + j];
+    double Pm[4];
+    double scalar;
+    if (a.host_prim[end]) {
+        const double* hp = a.host_prim[end] + ((int64_t)row * nq + j) * 5;
+        Pm[0] = hp[0];
+        Pm[1] = hp[1];
+        Pm[2] = hp[2];
+        Pm[3] = hp[3];
+        scalar = hp[4];
+    } else {
+        model_eval(a.model, r, q, a.time, false, a.ghost_index[end], 0, j, Pm, scalar);
+    }
+    PhysT<double> ph;
+    ph.srhd = a.srhd;
+    ph.hllc = 0;
+    ph.gm = a.gm;
+    ph.gm1 = a.gm - 1.0;
+    ph.gh = a.gm / ph.gm1;
+    ph.theta = 1.0;
+    double U[4];
+    prim_to_cons(ph, Pm, U);
+    double Uv[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) Uv[c] = U[c] * dV;       // from_model: U dV
+    const double smass = Uv[0] * scalar;                  // lab_frame_mass * scalar
+    double u[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) u[c] = Uv[c] / dV;       // try_to_primitive: U / dV
+    double P[4] = {0.0, 0.0, 0.0, 0.0};
+    double bad = 0.0;
+    int iters = 0, kind;
+    if (a.srhd) kind = srhd_c2p_newton(a.gm, u, 0.0, P, iters, bad);
+    else kind = newt_c2p(a.gm - 1.0, u, P, bad);
+    if (kind != HYDRO_NONE && kind != HYDRO_NEGATIVE_PRESSURE) {
+        atomicMin(&a.status->err_key, error_key(a.stage, 0x3ffeu + end, row, j, kind));
+    }
+    const double w = a.srhd ? sqrt(1.0 + P[1] * P[1] + P[2] * P[2]) : 1.0;
+    const double v[NFIELD] = {P[0], P[1], P[2], P[3], smass / dV / w};
+    const int nrt = a.nr_t[end];
+    const int64_t pn = (int64_t)(nrt + 4) * nq;
+    const int64_t off = (int64_t)(a.row0[end] + row) * nq + j;
+    if (a.single_precision) {
+        float* Pd = reinterpret_cast<float*>(a.P[end]);
+#pragma unroll
+        for (int c = 0; c < NFIELD; ++c) Pd[c * pn + off] = (float)v[c];
+    } else {
+        double* Pd = reinterpret_cast<double*>(a.P[end]);
+#pragma unroll
+        for (int c = 0; c < NFIELD; ++c) Pd[c * pn + off] = v[c];
+    }
+}
+
+// Halo zone k of remap item it = {target slot, source slot, side}: target
+// column j of halo row `row` from row `row` of the source's edge rows:
+//  - a finer source (R = nq_s / nq_t): conserved volume integrals and volumes
+//    of its R zones summed in column order, then the FP64 recovery (the
+//    reference's Newton from the plain guess) — a conservative merge;
+//  - a coarser source: its primitive at column j / R, copied.
+template <class R>
+static __device__ __noinline__ void remap_zone(const StageArgs& a, const int4 it, int k) {
+    const DevBlock& T = a.blocks[it.x];
+    const DevBlock& S = a.blocks[it.y];
+    const int side = it.z;
+    const int nq_t = T.nq, nq_s = S.nq;
+    if (k >= 2 * nq_t) return;
+    const int row = k / nq_t, j = k - row * nq_t;
+    const int srow = side == 0 ? S.nr - 2 + row : row;          // source interior row
+    const int trow = side == 0 ? row : T.nr + 2 + row;          // target padded row
+    R v[NFIELD];
+    if (nq_s < nq_t) {
+        const R* Ps = reinterpret_cast<const R*>(S.P);
+        const int64_t pn = (int64_t)(S.nr + 4) * nq_s;
+        const int64_t off = (int64_t)(srow + 2) * nq_s + j / (nq_t / nq_s);
+#pragma unroll
+        for (int q = 0; q < NFIELD; ++q) v[q] = Ps[q * pn + off];
+    } else {
+        const int Rr = nq_s / nq_t;
+        const double* Us = S.buf[a.sel_in];
+        const int64_t n = (int64_t)S.nr * nq_s;
+        double U[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, dv = 0.0;
+        for (int m = 0; m < Rr; ++m) {
+            const int64_t z = (int64_t)srow * nq_s + j * Rr + m;
+#pragma unroll
+            for (int q = 0; q < 5; ++q) U[q] += Us[q * n + z];
+            dv += S.dv[z];
+        }
+        double u[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) u[q] = U[q] / dv;
+        double P[4] = {0.0, 0.0, 0.0, 0.0};
+        double bad = 0.0;
+        int iters = 0, kind;
+        if (a.srhd) kind = srhd_c2p_newton(a.gm, u, 0.0, P, iters, bad);
+        else kind = newt_c2p(a.gm - 1.0, u, P, bad);
+        if (kind != HYDRO_NONE && kind != HYDRO_NEGATIVE_PRESSURE)
+            atomicMin(&a.status->err_key, error_key(a.stage, it.y, srow, j * Rr, kind));
+        const double w = a.srhd ? sqrt(1.0 + P[1] * P[1] + P[2] * P[2]) : 1.0;
+        const double sv = U[4] / dv / w;
+        v[0] = (R)P[0];
+        v[1] = (R)P[1];
+        v[2] = (R)P[2];
+        v[3] = (R)P[3];
+        v[4] = (R)sv;
+    }
+    R* Pt = reinterpret_cast<R*>(T.P);
+    const int64_t pt = (int64_t)(T.nr + 4) * nq_t;
+    const int64_t ot = (int64_t)trow * nq_t + j;
+#pragma unroll
+    for (int q = 0; q < NFIELD; ++q) Pt[q * pt + ot] = v[q];
+}
+
+// Separate-launch forms: blockIdx.y = end / remap item. Internal linkage, so
+// each translation unit keeps its own (differently compiled) kernels.
+namespace {
+
+__global__ void ghost_kernel(GhostArgs a) { ghost_zone(a, blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x); }
+
+template <class R>
+__global__ void remap_kernel(StageArgs a, const int4* __restrict__ items) {
+    const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
+    if (ek != NO_ERROR && (uint32_t)(ek >> 48) < (uint32_t)a.stage) return;
+    remap_zone<R>(a, items[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+}  // namespace
+
+}  // namespace knc

@@ -84,12 +84,18 @@ struct DevStatus {
     unsigned long long iters_fp32;
     unsigned long long fallbacks;
     unsigned long long dt_bits;     // min of dl/a over zones (double bits, positive)
+    unsigned long long bar_count;   // grid-barrier arrivals of fused launches since the last reset
+    int32_t bar_abort;              // a grid barrier gave up waiting
+    int32_t pad2;
 };
 
 struct StageArgs {
     const DevBlock* blocks;
-    const int4* tiles;      // {slot, i0, j0, 0}
+    const int4* tiles;      // {slot, i0, j0, 0}, TILE_R x TILE_Q (recovery, init)
     int32_t ntiles;
+    const int4* utiles;     // {slot, i0, j0, 0}, utr x TILE_Q (update)
+    int32_t nutiles;
+    int32_t utr;            // update tile rows: 4, 8 or 16
     int32_t stage;          // stage counter for error ordering
     int32_t sel_in, sel_out, sel_base;   // state buffer selectors; sel_base < 0: no average
     int32_t srhd, hllc;
@@ -124,6 +130,19 @@ struct GhostArgs {
     DevStatus* status;
 };
 
+// Fused-stage extras: recovery chunks {slot, z0, nz, 0} of at most
+// update_threads(utr) consecutive zones of one block, the remap items, and the
+// barrier base of this launch.
+struct FusedArgs {
+    const int4* chunks;
+    int32_t nchunks;
+    int32_t nremap;
+    const int4* remap;
+    int32_t max_nq;
+    int32_t pad_;
+    unsigned long long bar_base;
+};
+
 struct InitArgs {
     const DevBlock* blocks;
     const int4* tiles;
@@ -148,7 +167,8 @@ cudaError_t configure_kernels();
 cudaError_t launch_init_f64(const InitArgs& a, int ntiles, cudaStream_t s);
 cudaError_t launch_c2p_f64(const StageArgs& a, cudaStream_t s);
 cudaError_t launch_update_f64(const StageArgs& a, cudaStream_t s);
-cudaError_t launch_ghost(const GhostArgs& a, cudaStream_t s);
+cudaError_t launch_ghost_f64(const GhostArgs& a, cudaStream_t s);
+cudaError_t launch_ghost_mixed(const GhostArgs& a, cudaStream_t s);
 cudaError_t launch_c2p_mixed(const StageArgs& a, cudaStream_t s);
 cudaError_t launch_update_mixed(const StageArgs& a, cudaStream_t s);
 cudaError_t launch_aos_to_soa(const double* aos, const double* scalar, double* soa, int64_t nr, int64_t nq,
@@ -156,8 +176,19 @@ cudaError_t launch_aos_to_soa(const double* aos, const double* scalar, double* s
 // Halo rows across a change of polar resolution (power-of-two ratio).
 // remap = {target slot, source slot, side (0: target rows 0-1 from the source's
 // last two rows; 1: target rows nr+2..nr+3 from the source's first two)}.
-cudaError_t launch_remap(const StageArgs& a, const int4* remap, int nremap, int max_nq, bool single_precision,
-                         cudaStream_t s);
+cudaError_t launch_remap_f64(const StageArgs& a, const int4* remap, int nremap, int max_nq, cudaStream_t s);
+cudaError_t launch_remap_mixed(const StageArgs& a, const int4* remap, int nremap, int max_nq, cudaStream_t s);
+// One RK stage as one cooperative launch of `grid` CTAs (utr = a.utr); grid
+// must not exceed fused_max_ctas() x SMs.
+cudaError_t launch_stage_fused_f64(const StageArgs& a, const GhostArgs& g, const FusedArgs& f, int grid,
+                                   cudaStream_t s);
+cudaError_t launch_stage_fused_mixed(const StageArgs& a, const GhostArgs& g, const FusedArgs& f, int grid,
+                                     cudaStream_t s);
+// Resident CTAs per SM of the fused kernel for (precision, learned guess, tile rows).
+cudaError_t fused_max_ctas_f64(bool mlp, int utr, int* per_sm);
+cudaError_t fused_max_ctas_mixed(bool mlp, int utr, int* per_sm);
+// Threads of a fused / update CTA for tile rows utr.
+inline int stage_threads(int utr) { return (utr + 1) * TILE_Q; }
 cudaError_t launch_prims_to_aos(const void* P, double* out, int64_t nr, int64_t nq, cudaStream_t s);
 cudaError_t launch_soa_to_aos(const double* soa, double* aos, double* scalar, int64_t nr, int64_t nq,
                               cudaStream_t s);

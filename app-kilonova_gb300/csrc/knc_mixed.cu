@@ -16,6 +16,8 @@
 // volume-integrated state and divides rho and p by dV afterwards: no FP64
 // divisions by the cell volume.
 #include "knc_bits.cuh"
+#include "knc_fused.cuh"
+#include "knc_halo.cuh"
 #include "knc_internal.h"
 #include "knc_mlp.cuh"
 #include "knc_physics.cuh"
@@ -57,29 +59,17 @@ __device__ __forceinline__ bool newton_fast(R m, R ss, R tau, R gm, R p, R tol_a
     return false;
 }
 
+// Recovery of one zone; every thread of a warp calls zone() together (the
+// learned guess is a warp-wide inference).
 template <bool MLP>
-__global__ void __launch_bounds__(TILE_THREADS, MLP ? 2 : 3) c2p_mixed_kernel(StageArgs a) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
-    if (ek != NO_ERROR && (uint32_t)(ek >> 48) < (uint32_t)a.stage) return;
-    MlpWeights& W = *reinterpret_cast<MlpWeights*>(smem_raw);
-    __nv_bfloat16* act = reinterpret_cast<__nv_bfloat16*>(smem_raw + sizeof(MlpWeights)) +
-                         (threadIdx.x >> 5) * MLP_ACT_ELEMS;
-    if (MLP) {
-        mlp_load(W, a.mlp);
-        __syncthreads();
-    }
-    const double gm = a.gm;
-    const float gmf = (float)gm;
-    const float high_thr = (float)(1.0 - 1.0 / (a.w_split * a.w_split));
-    unsigned long long zones = 0, it64s = 0, it32s = 0, fbs = 0;
-    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
-        const int4 t = a.tiles[tile];
-        const DevBlock& B = a.blocks[t.x];
-        const int i = t.y + threadIdx.x / TILE_Q;
-        const int j = t.z + threadIdx.x % TILE_Q;
+struct MixedC2p {
+    static constexpr bool mlp = MLP;
+    __device__ static void zone(const StageArgs& a, int slot, const DevBlock& B, int i, int j, bool active,
+                                MlpWeights& W, __nv_bfloat16* act, C2pStats& st) {
+        const double gm = a.gm;
+        const float gmf = (float)gm;
+        const float high_thr = (float)(1.0 - 1.0 / (a.w_split * a.w_split));
         const int nr = B.nr, nq = B.nq;
-        const bool active = i < nr && j < nq;
         const int64_t n = (int64_t)nr * nq;
         const int64_t z = (int64_t)i * nq + j;
         double U[5] = {1.0, 0.0, 0.0, 1.0, 0.0};
@@ -113,11 +103,11 @@ __global__ void __launch_bounds__(TILE_THREADS, MLP ? 2 : 3) c2p_mixed_kernel(St
         float P[4] = {0.f, 0.f, 0.f, 0.f};
         float wz = 1.0f;
         if (active && kind == HYDRO_NONE) {
-            ++zones;
+            ++st.zones;
             float p32 = 0.f, w32 = 1.f;
             int it32 = 0;
             const bool ok32 = newton_fast<float>(mf, ssf, tauf, gmf, guess, 1e-30f, 1e-6f, 16, p32, w32, it32);
-            it32s += (unsigned long long)it32;
+            st.it32 += (unsigned long long)it32;
             if (!high && ok32) {
                 const float inv_dv = 1.0f / dV;
                 const float inv_et = 1.0f / (tauf + mf + p32);
@@ -133,16 +123,16 @@ __global__ void __launch_bounds__(TILE_THREADS, MLP ? 2 : 3) c2p_mixed_kernel(St
                 int it64 = 0;
                 bool ok = newton_fast<double>(m, ss, tau, gm, ok32 ? (double)p32 : 0.0, tol, 0.0, NEWTON_ITER_MAX,
                                               p64, w64, it64);
-                it64s += (unsigned long long)it64;
+                st.it64 += (unsigned long long)it64;
                 if (!ok) {
                     // fallback: the reference's iteration from the plain guess
-                    ++fbs;
+                    ++st.fbs;
                     const double u[4] = {m, U[1], U[2], tau};
                     double Pd[4] = {0.0, 0.0, 0.0, 0.0};
                     double bad;
                     int itf = 0;
                     const int kf = srhd_c2p_newton(gm, u, 0.0, Pd, itf, bad);
-                    it64s += (unsigned long long)itf;
+                    st.it64 += (unsigned long long)itf;
                     if (kf == HYDRO_ROOT_FINDER_FAILED) {
                         kind = kf;
                     } else {
@@ -166,7 +156,7 @@ __global__ void __launch_bounds__(TILE_THREADS, MLP ? 2 : 3) c2p_mixed_kernel(St
         }
         if (active) {
             if (kind != HYDRO_NONE) {
-                atomicMin(&a.status->err_key, error_key(a.stage, t.x, i, j, kind));
+                atomicMin(&a.status->err_key, error_key(a.stage, slot, i, j, kind));
                 a.status->err_sel = a.sel_in;
             }
             wz = sqrtf(1.0f + P[1] * P[1] + P[2] * P[2]);
@@ -174,7 +164,37 @@ __global__ void __launch_bounds__(TILE_THREADS, MLP ? 2 : 3) c2p_mixed_kernel(St
             store_prim<float>(B, i, j, v);
         }
     }
-    warp_reduce_stats(a.status, zones, it64s, it32s, fbs, 0.0, false);
+};
+
+template <bool MLP>
+__global__ void __launch_bounds__(TILE_THREADS, MLP ? 2 : 3) c2p_mixed_kernel(StageArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
+    if (ek != NO_ERROR && (uint32_t)(ek >> 48) < (uint32_t)a.stage) return;
+    MlpWeights& W = *reinterpret_cast<MlpWeights*>(smem_raw);
+    __nv_bfloat16* act = reinterpret_cast<__nv_bfloat16*>(smem_raw + sizeof(MlpWeights)) +
+                         (threadIdx.x >> 5) * MLP_ACT_ELEMS;
+    if (MLP) {
+        mlp_load(W, a.mlp);
+        __syncthreads();
+    }
+    C2pStats st;
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        const int4 t = a.tiles[tile];
+        const DevBlock& B = a.blocks[t.x];
+        const int i = t.y + threadIdx.x / TILE_Q;
+        const int j = t.z + threadIdx.x % TILE_Q;
+        MixedC2p<MLP>::zone(a, t.x, B, i, j, i < B.nr && j < B.nq, W, act, st);
+    }
+    warp_reduce_stats(a.status, st.zones, st.it64, st.it32, st.fbs, 0.0, false);
+}
+
+// ---- the fused stage (mixed) -------------------------------------------------
+template <int TR, bool MLP>
+__global__ void __launch_bounds__(update_threads<TR>(), MLP ? (TR == 4 ? 3 : TR == 8 ? 2 : 1) : (TR == 4 ? 5 : TR == 8 ? 3 : 2))
+    stage_fused_mixed_kernel(StageArgs a, GhostArgs g,
+                                                                                    FusedArgs f) {
+    stage_fused_body<float, true, TR, MixedC2p<MLP>>(a, g, f);
 }
 
 static int g_sms = 0;
@@ -201,10 +221,84 @@ cudaError_t launch_c2p_mixed(const StageArgs& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+template <int TR>
+static void update_mixed(const StageArgs& a, cudaStream_t s) {
+    update_kernel<float, true, TR><<<a.nutiles, update_threads<TR>(), StageSmem<float, TR>::bytes, s>>>(a);
+}
+
 cudaError_t launch_update_mixed(const StageArgs& a, cudaStream_t s) {
-    if (a.ntiles <= 0) return cudaSuccess;
-    update_kernel<float, true><<<a.ntiles, TILE_THREADS, StageSmem<float>::bytes, s>>>(a);
+    if (a.nutiles <= 0) return cudaSuccess;
+    switch (a.utr) {
+    case 4: update_mixed<4>(a, s); break;
+    case 16: update_mixed<16>(a, s); break;
+    default: update_mixed<8>(a, s);
+    }
     return cudaGetLastError();
+}
+
+template <int TR>
+static cudaError_t configure_update_mixed() {
+    return cudaFuncSetAttribute(update_kernel<float, true, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)StageSmem<float, TR>::bytes);
+}
+
+cudaError_t launch_ghost_mixed(const GhostArgs& a, cudaStream_t s) {
+    const int nq = a.nq[0] > a.nq[1] ? a.nq[0] : a.nq[1];
+    dim3 grid((2 * nq + 127) / 128, 2);
+    ghost_kernel<<<grid, 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_remap_mixed(const StageArgs& a, const int4* remap, int nremap, int max_nq, cudaStream_t s) {
+    if (nremap <= 0) return cudaSuccess;
+    dim3 grid((2 * max_nq + 127) / 128, nremap);
+    remap_kernel<float><<<grid, 128, 0, s>>>(a, remap);
+    return cudaGetLastError();
+}
+
+template <int TR, bool MLP>
+static cudaError_t fused_mixed(const StageArgs& a, const GhostArgs& g, const FusedArgs& f, int grid, cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(update_threads<TR>());
+    cfg.dynamicSmemBytes = fused_smem_bytes<float, TR, MLP>();
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, stage_fused_mixed_kernel<TR, MLP>, a, g, f);
+}
+
+cudaError_t launch_stage_fused_mixed(const StageArgs& a, const GhostArgs& g, const FusedArgs& f, int grid,
+                                     cudaStream_t s) {
+    const bool mlp = a.mlp != nullptr;
+    switch (a.utr) {
+    case 4: return mlp ? fused_mixed<4, true>(a, g, f, grid, s) : fused_mixed<4, false>(a, g, f, grid, s);
+    case 16: return mlp ? fused_mixed<16, true>(a, g, f, grid, s) : fused_mixed<16, false>(a, g, f, grid, s);
+    default: return mlp ? fused_mixed<8, true>(a, g, f, grid, s) : fused_mixed<8, false>(a, g, f, grid, s);
+    }
+}
+
+template <int TR, bool MLP>
+static cudaError_t fused_ctas_mixed(int* n) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, stage_fused_mixed_kernel<TR, MLP>, update_threads<TR>(),
+                                                         fused_smem_bytes<float, TR, MLP>());
+}
+
+cudaError_t fused_max_ctas_mixed(bool mlp, int utr, int* n) {
+    switch (utr) {
+    case 4: return mlp ? fused_ctas_mixed<4, true>(n) : fused_ctas_mixed<4, false>(n);
+    case 16: return mlp ? fused_ctas_mixed<16, true>(n) : fused_ctas_mixed<16, false>(n);
+    default: return mlp ? fused_ctas_mixed<8, true>(n) : fused_ctas_mixed<8, false>(n);
+    }
+}
+
+template <int TR, bool MLP>
+static cudaError_t configure_fused_mixed() {
+    return cudaFuncSetAttribute(stage_fused_mixed_kernel<TR, MLP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)fused_smem_bytes<float, TR, MLP>());
 }
 
 cudaError_t configure_f64();
@@ -213,9 +307,15 @@ cudaError_t configure_kernels() {
     static cudaError_t result = cudaErrorNotReady;
     if (result == cudaSuccess) return result;
     cudaError_t e = configure_f64();
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(update_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)StageSmem<float>::bytes);
+    if (e == cudaSuccess) e = configure_update_mixed<4>();
+    if (e == cudaSuccess) e = configure_update_mixed<8>();
+    if (e == cudaSuccess) e = configure_update_mixed<16>();
+    if (e == cudaSuccess) e = configure_fused_mixed<4, false>();
+    if (e == cudaSuccess) e = configure_fused_mixed<8, false>();
+    if (e == cudaSuccess) e = configure_fused_mixed<16, false>();
+    if (e == cudaSuccess) e = configure_fused_mixed<4, true>();
+    if (e == cudaSuccess) e = configure_fused_mixed<8, true>();
+    if (e == cudaSuccess) e = configure_fused_mixed<16, true>();
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(c2p_mixed_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(sizeof(MlpWeights) + 8 * MLP_ACT_ELEMS * sizeof(__nv_bfloat16)));

@@ -1,9 +1,12 @@
 // knc_stage.cuh — the fused flux / source / update kernel of one RK stage.
 //
-// One CTA owns a TILE_R x TILE_Q tile of one block. It stages the tile's
-// primitives plus a 2-zone halo (radial halo rows are already present in the
-// padded P array; theta halo columns come from the same block) in shared
-// memory, then:
+// One CTA owns a TR x TILE_Q tile of one block (TR = 4, 8 or 16, chosen per
+// context) and runs TR + 1 warps, so that the TR + 1 rows of radial faces and
+// the TR rows of TILE_Q + 1 polar faces are each one pass over its threads
+// (the Riemann solves are the costly part; no pass leaves most warps idle at
+// the following barrier). It stages the tile's primitives plus a 2-zone halo
+// (radial halo rows are already present in the padded P array; theta halo
+// columns come from the same block) in shared memory, then:
 //   1. PLM slopes in r for rows -1..TILE_R and in theta for columns -1..TILE_Q
 //      (zero slope on the first and last column of the block,
 //      src/scheme.rs:107-110 via ndarray_ops::extend_default_2d);
@@ -34,9 +37,14 @@ __device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
 // x * (hi + lo) in FP32
 __device__ __forceinline__ float df_scale(float x, float2 a) { return __fmaf_rn(x, a.x, x * a.y); }
 
-template <class R>
+template <int TR>
+constexpr int update_threads() {
+    return (TR + 1) * TILE_Q;
+}
+
+template <class R, int TR_>
 struct StageSmem {
-    static constexpr int TR = TILE_R, TQ = TILE_Q;
+    static constexpr int TR = TR_, TQ = TILE_Q;
     static constexpr int PR = TR + 4, PQ = TQ + 4;
     static constexpr int NP = NFIELD * PR * PQ;
     static constexpr int NGR = NFIELD * (TR + 2) * TQ;
@@ -59,29 +67,25 @@ __device__ __forceinline__ PhysT<R> make_phys(const StageArgs& a) {
     return ph;
 }
 
-template <class R, bool MIXED>
-__global__ void __launch_bounds__(TILE_THREADS, MIXED ? 4 : 1) update_kernel(StageArgs a) {
-    using S = StageSmem<R>;
+// One update tile t = {slot, i0, j0, -} with update_threads<TR>() threads.
+template <class R, bool MIXED, int TR_>
+__device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, unsigned char* smem_raw) {
+    using S = StageSmem<R, TR_>;
     constexpr int TR = S::TR, TQ = S::TQ, PR = S::PR, PQ = S::PQ;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int NT = update_threads<TR>();
     R* sP = reinterpret_cast<R*>(smem_raw);
     R* sGr = sP + S::NP;
     R* sGq = sGr + S::NGR;
     R* sFr = sGq + S::NGQ;
     R* sFq = sFr + S::NFR;
 
-    // A failed c2p in this or an earlier stage stops the step: keep the
-    // input state untouched so the failure can be reported from it.
-    if (*(volatile unsigned long long*)&a.status->err_key != NO_ERROR) return;
-
-    const int4 t = a.tiles[blockIdx.x];
     const DevBlock& B = a.blocks[t.x];
     const int nr = B.nr, nq = B.nq, i0 = t.y, j0 = t.z;
     const int tid = threadIdx.x;
     const R* P = reinterpret_cast<const R*>(B.P);
     const int64_t pn = (int64_t)(nr + 4) * nq;
     const bool one_d = a.one_dimensional != 0;
-    if (MIXED) {
+    if (MIXED && tid < TR * TQ) {
         // the state this thread updates at the end: start it towards L2 now
         const int i = i0 + tid / TQ, j = j0 + tid % TQ;
         if (i < nr && j < nq) {
@@ -95,7 +99,7 @@ __global__ void __launch_bounds__(TILE_THREADS, MIXED ? 4 : 1) update_kernel(Sta
     }
 
     // ---- stage primitives (tile rows -2..TR+1 = padded rows i0..i0+TR+3)
-    for (int k = tid; k < PR * PQ; k += TILE_THREADS) {
+    for (int k = tid; k < PR * PQ; k += NT) {
         const int rr = k / PQ, cc = k - rr * PQ;
         const int prow = i0 + rr;
         const int j = j0 - 2 + cc;
@@ -109,24 +113,30 @@ __global__ void __launch_bounds__(TILE_THREADS, MIXED ? 4 : 1) update_kernel(Sta
     const PhysT<R> ph = make_phys<R>(a);
     const R th = ph.theta;
 
-    // ---- PLM slopes
-    for (int k = tid; k < (TR + 2) * TQ; k += TILE_THREADS) {
-        const int g = k / TQ, c = k - g * TQ;
+    // ---- PLM slopes: radial for rows -1..TR, then polar for columns -1..TQ
+    // (the radial count is a whole number of warps, so no warp mixes the two)
+    {
+        constexpr int NGRZ = (TR + 2) * TQ, NGQZ = TR * (TQ + 2);
+        const int total = one_d ? NGRZ : NGRZ + NGQZ;
+        for (int k = tid; k < total; k += NT) {
+            if (k < NGRZ) {
+                const int g = k / TQ, c = k - g * TQ;
 #pragma unroll
-        for (int q = 0; q < NFIELD; ++q) {
-            const R* col = sP + (q * PR) * PQ + c + 2;
-            sGr[(q * (TR + 2) + g) * TQ + c] = plm_gradient(th, col[g * PQ], col[(g + 1) * PQ], col[(g + 2) * PQ]);
-        }
-    }
-    if (!one_d) {
-        for (int k = tid; k < TR * (TQ + 2); k += TILE_THREADS) {
-            const int r = k / (TQ + 2), c = k - r * (TQ + 2);
-            const int j = j0 - 1 + c;
-            const bool edge = j <= 0 || j >= nq - 1;
+                for (int q = 0; q < NFIELD; ++q) {
+                    const R* col = sP + (q * PR) * PQ + c + 2;
+                    sGr[(q * (TR + 2) + g) * TQ + c] =
+                        plm_gradient(th, col[g * PQ], col[(g + 1) * PQ], col[(g + 2) * PQ]);
+                }
+            } else {
+                const int kk = k - NGRZ;
+                const int r = kk / (TQ + 2), c = kk - r * (TQ + 2);
+                const int j = j0 - 1 + c;
+                const bool edge = j <= 0 || j >= nq - 1;
 #pragma unroll
-            for (int q = 0; q < NFIELD; ++q) {
-                const R* row = sP + (q * PR + r + 2) * PQ + c;
-                sGq[(q * TR + r) * (TQ + 2) + c] = edge ? R(0) : plm_gradient(th, row[0], row[1], row[2]);
+                for (int q = 0; q < NFIELD; ++q) {
+                    const R* row = sP + (q * PR + r + 2) * PQ + c;
+                    sGq[(q * TR + r) * (TQ + 2) + c] = edge ? R(0) : plm_gradient(th, row[0], row[1], row[2]);
+                }
             }
         }
     }
@@ -134,8 +144,9 @@ __global__ void __launch_bounds__(TILE_THREADS, MIXED ? 4 : 1) update_kernel(Sta
 
     const R cflux = (R)a.cflux;
 
-    // ---- radial faces i0..i0+TR (face i between zone rows i-1 and i)
-    for (int k = tid; k < (TR + 1) * TQ; k += TILE_THREADS) {
+    // ---- radial faces i0..i0+TR (face i between zone rows i-1 and i): one
+    // pass of all NT threads
+    for (int k = tid; k < (TR + 1) * TQ; k += NT) {
         const int f = k / TQ, c = k - f * TQ;
         const int i = i0 + f, j = j0 + c;
         R out[NFIELD] = {R(0), R(0), R(0), R(0), R(0)};
@@ -162,9 +173,10 @@ __global__ void __launch_bounds__(TILE_THREADS, MIXED ? 4 : 1) update_kernel(Sta
 #pragma unroll
         for (int q = 0; q < NFIELD; ++q) sFr[(q * (TR + 1) + f) * TQ + c] = out[q];
     }
-    // ---- polar faces j0..j0+TQ (face j between zone columns j-1 and j)
+    // ---- polar faces j0..j0+TQ (face j between zone columns j-1 and j): one
+    // pass, TR rows of TQ + 1 faces on (TR + 1) TQ threads
     if (!one_d) {
-        for (int k = tid; k < TR * (TQ + 1); k += TILE_THREADS) {
+        for (int k = tid; k < TR * (TQ + 1); k += NT) {
             const int r = k / (TQ + 1), c = k - r * (TQ + 1);
             const int i = i0 + r, j = j0 + c;
             R out[NFIELD] = {R(0), R(0), R(0), R(0), R(0)};
@@ -195,7 +207,7 @@ __global__ void __launch_bounds__(TILE_THREADS, MIXED ? 4 : 1) update_kernel(Sta
     __syncthreads();
 
     // ---- sources, conserved update, RK average
-    {
+    if (tid < TR * TQ) {
         const int r = tid / TQ, c = tid - r * TQ;
         const int i = i0 + r, j = j0 + c;
         if (i < nr && j < nq) {
@@ -263,6 +275,17 @@ __global__ void __launch_bounds__(TILE_THREADS, MIXED ? 4 : 1) update_kernel(Sta
             for (int q = 0; q < NFIELD; ++q) Uout[q * n + z] = res[q];
         }
     }
+}
+
+// One CTA per update tile (a.utiles).
+template <class R, bool MIXED, int TR>
+__global__ void __launch_bounds__(update_threads<TR>(), MIXED ? (TR == 4 ? 6 : TR == 8 ? 3 : 2) : 1)
+    update_kernel(StageArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    // A failed c2p in this or an earlier stage stops the step: keep the
+    // input state untouched so the failure can be reported from it.
+    if (*(volatile unsigned long long*)&a.status->err_key != NO_ERROR) return;
+    update_tile<R, MIXED, TR>(a, a.utiles[blockIdx.x], smem_raw);
 }
 
 // Block-wide reduction helpers (warp shuffles, then one atomic per warp).

@@ -51,7 +51,8 @@ KNC_MODEL_JET_IN_STAR = 6
 KNC_KERNEL_GHOST = 0
 KNC_KERNEL_C2P = 1
 KNC_KERNEL_UPDATE = 2
-KNC_KERNEL_KINDS = 3
+KNC_KERNEL_FUSED = 3
+KNC_KERNEL_KINDS = 4
 
 KNC_MLP_HIDDEN = 64
 KNC_MLP_OFF_W1 = 0
@@ -124,6 +125,11 @@ class Error(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("tile_rows", C.c_int32), ("fused", C.c_int32), ("ctas_per_sm", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
 class MlpTrainParams(C.Structure):
     _fields_ = [
         ("steps", C.c_int64),
@@ -172,6 +178,9 @@ SIGNATURES = {
     "knc_set_precision": (C.c_int, [_P, C.c_int32]),
     "knc_set_c2p_guess": (C.c_int, [_P, C.c_int32, _FP, C.c_size_t]),
     "knc_set_batched": (C.c_int, [_P, C.c_int32]),
+    "knc_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+    "knc_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+    "knc_autotune": (C.c_int, [_P, C.c_int32, C.POINTER(Tuning), _DP]),
     "knc_set_mixed_w_split": (C.c_int, [_P, C.c_double]),
     "knc_synchronize": (C.c_int, [_P]),
     "knc_c2p_stats": (C.c_int, [_P, _I64P, _I64P, _I64P, _I64P]),

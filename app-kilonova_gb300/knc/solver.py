@@ -105,6 +105,23 @@ class Solver:
     def set_batched(self, graph: bool):
         self._check(self.lib.knc_set_batched(self.h, int(bool(graph))), "set_batched")
 
+    def set_tuning(self, tile_rows: int = 8, fused: bool = False, ctas_per_sm: int = 0):
+        t = abi.Tuning(tile_rows=int(tile_rows), fused=int(bool(fused)), ctas_per_sm=int(ctas_per_sm))
+        self._check(self.lib.knc_set_tuning(self.h, C.byref(t)), "set_tuning")
+
+    def tuning(self) -> dict:
+        t = abi.Tuning()
+        self._check(self.lib.knc_get_tuning(self.h, C.byref(t)), "get_tuning")
+        return {"tile_rows": t.tile_rows, "fused": bool(t.fused), "ctas_per_sm": t.ctas_per_sm}
+
+    def autotune(self, reps: int = 5):
+        """Time every launch shape on the live state, keep the fastest; returns
+        (tuning dict, ms per stage)."""
+        t = abi.Tuning()
+        ms = C.c_double()
+        self._check(self.lib.knc_autotune(self.h, int(reps), C.byref(t), C.byref(ms)), "autotune")
+        return {"tile_rows": t.tile_rows, "fused": bool(t.fused), "ctas_per_sm": t.ctas_per_sm}, ms.value
+
     def set_mixed_w_split(self, w: float):
         self._check(self.lib.knc_set_mixed_w_split(self.h, float(w)), "set_mixed_w_split")
 
@@ -184,7 +201,7 @@ class Solver:
         ms = (C.c_double * abi.KNC_KERNEL_KINDS)()
         n = (C.c_int64 * abi.KNC_KERNEL_KINDS)()
         self._check(self.lib.knc_kernel_times(self.h, ms, n), "kernel_times")
-        names = ["ghost", "c2p", "update"]
+        names = ["ghost", "c2p", "update", "fused"]
         return {names[k]: (ms[k], n[k]) for k in range(abi.KNC_KERNEL_KINDS)}
 
     def set_time(self, t: float, num: int = 0, den: int = 1):

@@ -230,6 +230,30 @@ int knc_set_c2p_guess(knc_ctx* ctx, int32_t guess, const float* weights,
                       size_t n_weights);
 /* graph != 0: capture each `fold` of RK steps in a CUDA graph and replay it. */
 int knc_set_batched(knc_ctx* ctx, int32_t graph);
+/* Launch shape of a stage (no counterpart in the reference, whose stage is a
+ * Rayon/Tokio task per block, src/scheme.rs:16-173).
+ *   tile_rows    radial rows of an update tile (4, 8 or 16; 32 polar columns;
+ *                a tile runs on (tile_rows + 1) warps)
+ *   fused        0: a stage is four launches (ghost rows, recovery, remaps,
+ *                update); 1: one persistent cooperative launch whose phases
+ *                are separated by bounded grid barriers (bit-identical result)
+ *   ctas_per_sm  fused grid = ctas_per_sm x SMs CTAs (0: the occupancy bound;
+ *                larger values are clamped to it) */
+typedef struct knc_tuning {
+    int32_t tile_rows;
+    int32_t fused;
+    int32_t ctas_per_sm;
+    int32_t reserved;
+} knc_tuning;
+int knc_set_tuning(knc_ctx* ctx, const knc_tuning* tuning);
+int knc_get_tuning(const knc_ctx* ctx, knc_tuning* tuning);
+/* Autotuner: times every candidate shape (tile rows x separate / fused x CTAs
+ * per SM) with `reps` first-stage launches each on the live state (they write
+ * only the scratch buffer and primitives, so the state is unchanged), keeps
+ * the fastest and returns it with its time per stage (either output may be
+ * NULL). */
+int knc_autotune(knc_ctx* ctx, int32_t reps, knc_tuning* best, double* ms_per_stage);
+
 /* Mixed precision: zones whose Lorentz factor estimate exceeds this recover
  * primitives in FP64 (default 2.0); below it recovery runs in FP32. */
 int knc_set_mixed_w_split(knc_ctx* ctx, double w_split);
@@ -251,7 +275,8 @@ int knc_launch_count(const knc_ctx* ctx, int64_t* launches);
  * every launch is bracketed by events; knc_kernel_times returns, per kind
  * (KNC_KERNEL_*), the summed milliseconds and launch counts since enabling.
  * Not available while the steps run as a CUDA graph. */
-enum { KNC_KERNEL_GHOST = 0, KNC_KERNEL_C2P = 1, KNC_KERNEL_UPDATE = 2, KNC_KERNEL_KINDS = 3 };
+enum { KNC_KERNEL_GHOST = 0, KNC_KERNEL_C2P = 1, KNC_KERNEL_UPDATE = 2, KNC_KERNEL_FUSED = 3,
+       KNC_KERNEL_KINDS = 4 };
 int knc_set_profiling(knc_ctx* ctx, int32_t on);
 int knc_kernel_times(knc_ctx* ctx, double* ms, int64_t* launches);
 

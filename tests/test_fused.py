@@ -1,0 +1,130 @@
+"""Launch shapes of a stage: update tile rows, the fused persistent stage and
+the autotuner.
+
+Every shape runs the same per-zone and per-face arithmetic in the same order
+(a face on a tile edge is solved by both tiles from identical inputs), so all
+shapes must give bit-identical states: the FP64 ones equal to the oracle, the
+mixed ones equal to each other.
+"""
+import numpy as np
+import pytest
+
+from helpers import make_pair, zone_relative_errors
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(4, False), (8, False), (16, False), (4, True), (8, True), (16, True)]
+
+
+def _same(a, b):
+    return max(zone_relative_errors(a, b)) == 0.0
+
+
+@pytest.mark.parametrize("tile_rows,fused", SHAPES)
+def test_fp64_shapes_match_oracle(tile_rows, fused):
+    from knc import workloads
+    w = workloads.wind_small()
+    g, o = make_pair(w)
+    g.set_tuning(tile_rows=tile_rows, fused=fused)
+    for _ in range(2):
+        g.advance(2)
+        o.advance(2)
+    assert _same(g.state(), o.state())
+
+
+@pytest.mark.parametrize("tile_rows,fused", SHAPES)
+def test_fp64_uneven_moving_shapes_match_oracle(tile_rows, fused):
+    from knc import workloads
+    w = workloads.uneven_small(order="RK3")
+    g, o = make_pair(w)
+    g.set_tuning(tile_rows=tile_rows, fused=fused)
+    g.set_batched(True)
+    for _ in range(2):
+        g.advance(5)
+        o.advance(5)
+    assert g.block_indexes() == o.block_indexes()
+    assert _same(g.state(), o.state())
+
+
+def _mixed(w, tile_rows, fused, batched, mlp=None, steps=6):
+    import knc
+    g, _ = make_pair(w, gpu=True)
+    g.set_precision(knc.abi.KNC_PRECISION_MIXED)
+    if mlp is not None:
+        g.set_c2p_guess(knc.abi.KNC_GUESS_MLP, mlp)
+    g.set_tuning(tile_rows=tile_rows, fused=fused)
+    g.set_batched(batched)
+    for _ in range(steps // 3):
+        g.advance(3)
+    return g
+
+
+@pytest.mark.parametrize("tile_rows", [4, 8, 16])
+def test_mixed_fused_matches_separate(tile_rows):
+    from knc import workloads
+    w = workloads.wind_small()
+    ref = _mixed(w, 8, False, False)
+    g = _mixed(w, tile_rows, True, True)
+    assert _same(g.state(), ref.state())
+
+
+def test_mixed_learned_fused_matches_separate():
+    from knc import learned, workloads
+    wts = learned.init_weights(seed=3)
+    wts[-6:-3] = 0.0          # input mean
+    wts[-3:] = 1.0            # input scale
+    w = workloads.jet_small()
+    ref = _mixed(w, 8, False, False, mlp=wts)
+    g = _mixed(w, 8, True, True, mlp=wts)
+    assert _same(g.state(), ref.state())
+
+
+def test_mixed_uneven_moving_fused_graph():
+    from knc import workloads
+    w = workloads.uneven_small(order="RK3")
+    ref = _mixed(w, 8, False, False, steps=12)
+    g = _mixed(w, 16, True, True, steps=12)
+    assert g.block_indexes() == ref.block_indexes()
+    assert g.block_indexes()[0] > 0
+    assert _same(g.state(), ref.state())
+
+
+def test_autotune_keeps_state_and_results():
+    import knc
+    from knc import workloads
+    w = workloads.uneven_small()
+    g, o = make_pair(w)
+    g.set_precision(knc.abi.KNC_PRECISION_FP64)
+    before = g.state()
+    best, ms = g.autotune(reps=2)
+    assert best["tile_rows"] in (4, 8, 16) and ms > 0.0
+    assert g.tuning() == best
+    assert _same(g.state(), before)
+    g.advance(4)
+    o.advance(4)
+    assert _same(g.state(), o.state())
+    assert g.time() == o.time()
+
+
+def test_tuning_validation():
+    import knc
+    from knc import workloads
+    g, _ = make_pair(workloads.wind_small(), gpu=True)
+    with pytest.raises(knc.abi.KncError):
+        g.set_tuning(tile_rows=12)
+    with pytest.raises(knc.abi.KncError):
+        g.set_tuning(tile_rows=8, ctas_per_sm=-1)
+
+
+def test_fused_counts_one_launch_per_stage():
+    import ctypes as C
+    from knc import workloads
+    w = workloads.wind_small()
+    g, _ = make_pair(w, gpu=True)
+    g.set_tuning(tile_rows=8, fused=True)
+    n0 = C.c_int64()
+    g.lib.knc_launch_count(g.h, C.byref(n0))
+    g.advance(3)
+    n1 = C.c_int64()
+    g.lib.knc_launch_count(g.h, C.byref(n1))
+    assert n1.value - n0.value == 3 * 2      # RK2: two stages per step, one launch each
