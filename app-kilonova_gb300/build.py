@@ -29,6 +29,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 PER_FILE = {
     "knc_f64.cu": ["--fmad=false"],
     "knc_noalloc.cu": ["--fmad=false"],
+    "knc_mixed.cu": ["-prec-div=false", "-prec-sqrt=false"],
 }
 
 

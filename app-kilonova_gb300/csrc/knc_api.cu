@@ -18,7 +18,10 @@
 #include <string>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "knc_internal.h"
+#include "knc_tma.cuh"
 
 using namespace knc;
 
@@ -219,6 +222,10 @@ struct Layout {
     int utiles_cap = 0;
     int nutiles = 0;
     int utr = 0;
+    int64_t nzones = 0;         // zones of the block set
+    TmaMaps* d_tmaps = nullptr; // tensor maps per slot (tiles of `utr` rows), when every block allows them
+    int tmaps_cap = 0;
+    bool tma_ok = false;
     int4* d_chunks = nullptr;   // fused recovery chunks {slot, z0, nz, 0} of <= stage_threads(utr) zones
     int chunks_cap = 0;
     int nchunks = 0;
@@ -248,6 +255,7 @@ void free_layout(Layout& l) {
     cudaFree(l.d_tiles);
     cudaFree(l.d_utiles);
     cudaFree(l.d_chunks);
+    cudaFree(l.d_tmaps);
     cudaFree(l.d_remap);
     cudaFree(l.d_ghost_rc);
     cudaFree(l.d_ghost_dv[0]);
@@ -303,6 +311,7 @@ struct knc_ctx {
     int32_t batched = 0;
     int32_t utr = 8;   // update tile rows (4, 8 or 16)
     int32_t fused = 0;         // one cooperative launch per stage
+    int32_t tma = 0;           // mixed update stages tiles with tensor copies
     int32_t ctas_per_sm = 0;   // fused grid: CTAs per SM (0: the occupancy bound)
     int32_t sms = 0;
     bool coop = false;         // the device supports cooperative launches
@@ -311,6 +320,7 @@ struct knc_ctx {
     float* d_mlp = nullptr;
     // bookkeeping
     int64_t launches = 0;
+    int64_t zone_updates = 0;   // zones x RK steps advanced since creation
     bool profiling = false;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_events;
     std::vector<cudaEvent_t> event_pool;
@@ -483,12 +493,57 @@ void release_block(knc_ctx* c, BlockH& b) {
     b = BlockH();
 }
 
+// cuTensorMapEncodeTiled from the driver (no link-time dependency on libcuda).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+// Tensor maps of one block for update tiles of `tr` rows: P as float
+// {nq, nr+4, 5} with boxes {TILE_Q+8, tr+4, 5} (the tile, its 2-zone halo and
+// a 16-byte-aligned start column j0 - 4), each state buffer as double
+// {nq, nr, 5} with boxes {TILE_Q, tr, 5}. Needs rows of 16-byte multiples
+// (nq % 4 == 0) and a block at least one box wide.
+bool encode_block_maps(const BlockH& b, int tr, TmaMaps* m) {
+    auto enc = tensor_map_encoder();
+    if (!enc || b.nq % 4 != 0 || b.nq < TILE_Q + 8 || b.nr < tr) return false;
+    const cuuint64_t nq = (cuuint64_t)b.nq, nr = (cuuint64_t)b.nr;
+    const cuuint32_t es[3] = {1, 1, 1};
+    const cuuint64_t dimP[3] = {nq, nr + 4, (cuuint64_t)NFIELD};
+    const cuuint64_t strP[2] = {nq * 4, (nr + 4) * nq * 4};
+    const cuuint32_t boxP[3] = {(cuuint32_t)(TILE_Q + 8), (cuuint32_t)(tr + 4), (cuuint32_t)NFIELD};
+    if (enc(&m->P, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, b.P, dimP, strP, boxP, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    const cuuint64_t dimU[3] = {nq, nr, (cuuint64_t)NFIELD};
+    const cuuint64_t strU[2] = {nq * 8, nr * nq * 8};
+    const cuuint32_t boxU[3] = {(cuuint32_t)TILE_Q, (cuuint32_t)tr, (cuuint32_t)NFIELD};
+    for (int k = 0; k < 2; ++k)
+        if (enc(&m->U[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, b.buf[k], dimU, strU, boxU, es,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return false;
+    return true;
+}
+
 // Rebuild the device block table and the tile list after the block set changed.
 int rebuild_table(knc_ctx* c) {
     if (!c->dirty && L(c).utr == c->utr) return KNC_OK;
     const int nb = (int)c->blocks.size();
     std::vector<DevBlock> tab(nb);
     std::vector<int4> tiles, utiles, chunks;
+    std::vector<TmaMaps> maps(nb);
+    bool tma_ok = nb > 0;
     const int nt = stage_threads(c->utr);
     L(c).slot_index.clear();
     int slot = 0;
@@ -549,6 +604,7 @@ int rebuild_table(knc_ctx* c) {
                 tiles.push_back(make_int4(slot, (int)i0, (int)j0, (int)zoff));
         for (int64_t i0 = 0; i0 < b.nr; i0 += c->utr)
             for (int64_t j0 = 0; j0 < b.nq; j0 += TILE_Q) utiles.push_back(make_int4(slot, (int)i0, (int)j0, 0));
+        if (tma_ok) tma_ok = encode_block_maps(b, c->utr, &maps[k]);
         for (int64_t z0 = 0; z0 < b.nr * b.nq; z0 += nt)
             chunks.push_back(make_int4(slot, (int)z0, (int)std::min<int64_t>(nt, b.nr * b.nq - z0), 0));
         L(c).slot_index.push_back(b.index);
@@ -592,6 +648,18 @@ int rebuild_table(knc_ctx* c) {
         CK(cudaMemcpyAsync(L(c).d_chunks, chunks.data(), chunks.size() * sizeof(int4), cudaMemcpyHostToDevice,
                            c->stream));
     L(c).nchunks = (int)chunks.size();
+    L(c).nzones = zoff;
+    L(c).tma_ok = false;
+    if (tma_ok) {
+        if (nb > L(c).tmaps_cap) {
+            cudaFree(L(c).d_tmaps);
+            L(c).d_tmaps = nullptr;
+            CK(dalloc(&L(c).d_tmaps, (size_t)nb));
+            L(c).tmaps_cap = nb;
+        }
+        CK(cudaMemcpyAsync(L(c).d_tmaps, maps.data(), nb * sizeof(TmaMaps), cudaMemcpyHostToDevice, c->stream));
+        L(c).tma_ok = true;
+    }
     if ((int)remaps.size() > L(c).remap_cap) {
         cudaFree(L(c).d_remap);
         L(c).d_remap = nullptr;
@@ -742,6 +810,8 @@ StageArgs base_args(knc_ctx* c) {
     a.utiles = L(c).d_utiles;
     a.nutiles = L(c).nutiles;
     a.utr = L(c).utr;
+    a.tma = c->tma && L(c).tma_ok ? 1 : 0;
+    a.tmaps = L(c).tma_ok ? L(c).d_tmaps : nullptr;
     a.srhd = c->hp.system == KNC_SYSTEM_RELATIVISTIC;
     a.hllc = c->hp.riemann_solver == KNC_RIEMANN_HLLC;
     a.one_dimensional = c->mesh.p.num_polar_zones == 1;
@@ -750,6 +820,13 @@ StageArgs base_args(knc_ctx* c) {
     a.plm_theta = c->hp.plm_theta;
     a.cflux = a.srhd ? LIGHT_SPEED_H : 1.0;
     a.w_split = c->w_split;
+    a.gh = a.gm / (a.gm - 1.0);
+    a.gm_f = (float)a.gm;
+    a.gm1_f = (float)(a.gm - 1.0);
+    a.gh_f = (float)a.gh;
+    a.theta_f = (float)a.plm_theta;
+    a.cflux_f = (float)a.cflux;
+    a.high_thr_f = (float)(1.0 - 1.0 / (c->w_split * c->w_split));
     a.mlp = c->guess == KNC_GUESS_MLP ? c->d_mlp : nullptr;
     a.status = c->d_status;
     a.sel_base = -1;
@@ -833,6 +910,8 @@ int run_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, doub
     a.w1 = w1;
     a.bf = bf;
     a.dt = dt;
+    a.dt_f = (float)dt;
+    a.avg_half = w1 == 0.5 && bf == 0.5 ? 1 : 0;
     if (c->fused) {
         // the whole stage in one cooperative launch (grid barriers between phases)
         FusedArgs f;
@@ -909,6 +988,7 @@ int rk_step(knc_ctx* c, double dt) {
         return i1.mul(mbr.add(one)).add(it0.mul(br));
     };
     int r;
+    c->zone_updates += L(c).nzones;
     if ((r = run_stage(c, A, B, -1, 1.0, 0.0, T.stage[0], dt))) return r;
     Rational i1 = it0.add(one);
     if (order == 1) {
@@ -1744,6 +1824,12 @@ int knc_set_c2p_guess(knc_ctx* c, int32_t guess, const float* w, size_t n) {
     return KNC_OK;
 }
 
+int knc_zone_updates(const knc_ctx* c, int64_t* n) {
+    if (!c || !n) return KNC_ERR_INVALID_ARGUMENT;
+    *n = c->zone_updates;
+    return KNC_OK;
+}
+
 int knc_set_tuning(knc_ctx* c, const knc_tuning* t) {
     if (!c || !t) return KNC_ERR_INVALID_ARGUMENT;
     if (t->tile_rows != 4 && t->tile_rows != 8 && t->tile_rows != 16)
@@ -1754,6 +1840,7 @@ int knc_set_tuning(knc_ctx* c, const knc_tuning* t) {
     c->utr = t->tile_rows;
     c->fused = t->fused ? 1 : 0;
     c->ctas_per_sm = t->ctas_per_sm;
+    c->tma = t->tma ? 1 : 0;
     return KNC_OK;
 }
 
@@ -1762,7 +1849,7 @@ int knc_get_tuning(const knc_ctx* c, knc_tuning* t) {
     t->tile_rows = c->utr;
     t->fused = c->fused;
     t->ctas_per_sm = c->ctas_per_sm;
-    t->reserved = 0;
+    t->tma = c->tma;
     return KNC_OK;
 }
 
@@ -1777,10 +1864,11 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
     if ((r = time_step_impl(c, &dt))) return r;
     DevStatus saved;
     CK(cudaMemcpy(&saved, c->d_status, sizeof(saved), cudaMemcpyDeviceToHost));
-    const knc_tuning keep = {c->utr, c->fused, c->ctas_per_sm, 0};
+    const knc_tuning keep = {c->utr, c->fused, c->ctas_per_sm, c->tma};
     std::vector<knc_tuning> cands;
     for (int tr : {4, 8, 16}) {
         cands.push_back({tr, 0, 0, 0});
+        if (mixed(c)) cands.push_back({tr, 0, 0, 1});   // tensor-copy staging (used where every block allows it)
         if (!c->coop) continue;
         c->utr = tr;
         int per_sm = 1;
@@ -1800,7 +1888,9 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
         c->utr = t.tile_rows;
         c->fused = t.fused;
         c->ctas_per_sm = t.ctas_per_sm;
+        c->tma = t.tma;
         if ((r = rebuild_table(c))) break;
+        if (t.tma && !L(c).tma_ok) continue;
         // the first stage reads buf[cur] and writes buf[1 - cur]: the state stays
         if ((r = run_stage(c, c->cur, 1 - c->cur, -1, 1.0, 0.0, c->time, dt))) break;
         CK(cudaEventRecord(e0, c->stream));
@@ -1829,6 +1919,7 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
     c->utr = best.tile_rows;
     c->fused = best.fused;
     c->ctas_per_sm = best.ctas_per_sm;
+    c->tma = best.tma;
     if (r) {
         c->failed = false;
         return r;

@@ -224,10 +224,15 @@ cudaError_t launch_c2p_f64(const StageArgs& a, cudaStream_t s) {
     if (a.ntiles <= 0) return cudaSuccess;
     if (a.mlp && a.srhd) {
         const size_t bytes = sizeof(MlpWeights) + 8 * MLP_ACT_ELEMS * sizeof(__nv_bfloat16);
-        int dev = 0, sms = 1;
+        int dev = 0, sms = 1, per_sm = 1;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const int grid = a.ntiles < sms * 4 ? a.ntiles : sms * 4;
+        // resident CTAs only: a persistent grid larger than that runs a tail wave
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, c2p_f64_kernel<true>, TILE_THREADS, bytes) !=
+                cudaSuccess ||
+            per_sm < 1)
+            per_sm = 1;
+        const int grid = a.ntiles < sms * per_sm ? a.ntiles : sms * per_sm;
         c2p_f64_kernel<true><<<grid, TILE_THREADS, bytes, s>>>(a);
     } else {
         c2p_f64_kernel<false><<<a.ntiles, TILE_THREADS, 0, s>>>(a);

@@ -96,6 +96,8 @@ struct StageArgs {
     const int4* utiles;     // {slot, i0, j0, 0}, utr x TILE_Q (update)
     int32_t nutiles;
     int32_t utr;            // update tile rows: 4, 8 or 16
+    int32_t tma;            // mixed update: stage tiles with tensor copies (tmaps valid)
+    const void* tmaps;      // TmaMaps per slot (knc_tma.cuh), or null
     int32_t stage;          // stage counter for error ordering
     int32_t sel_in, sel_out, sel_base;   // state buffer selectors; sel_base < 0: no average
     int32_t srhd, hllc;
@@ -107,6 +109,12 @@ struct StageArgs {
     double w1, bf;          // out = (U + dU) w1 + U0 bf when sel_base >= 0
     double cflux;           // LIGHT_SPEED (SRHD) or 1
     double w_split;         // mixed path: Lorentz factor above which c2p runs in FP64
+    double gh;              // gm / (gm - 1), rounded once on the host
+    // FP32 copies rounded once on the host, so no thread converts or divides
+    // in FP64 for them (on GB300 the FP64 pipe is the narrow one)
+    float gm_f, gm1_f, gh_f, theta_f, dt_f, cflux_f;
+    float high_thr_f;       // 1 - 1 / w_split^2: |S| / (D + tau) squared above it means W > w_split
+    int32_t avg_half;       // w1 == bf == 1/2 (the RK2 average, halved exactly on the integer pipe)
     const float* mlp;       // packed MLP weights (device) or null
     DevStatus* status;
 };

@@ -15,6 +15,9 @@
 // The recovery is scale-invariant (U -> k U gives p -> k p), so it runs on the
 // volume-integrated state and divides rho and p by dV afterwards: no FP64
 // divisions by the cell volume.
+#include <map>
+#include <mutex>
+
 #include "knc_bits.cuh"
 #include "knc_fused.cuh"
 #include "knc_halo.cuh"
@@ -22,6 +25,7 @@
 #include "knc_mlp.cuh"
 #include "knc_physics.cuh"
 #include "knc_stage.cuh"
+#include "knc_tma.cuh"
 
 namespace knc {
 
@@ -59,6 +63,15 @@ __device__ __forceinline__ bool newton_fast(R m, R ss, R tau, R gm, R p, R tol_a
     return false;
 }
 
+// The learned-guess inference out of line: warps run it only when one of
+// their zones needs the FP64 recovery, so its register demand stays out of
+// the common path.
+static __device__ __noinline__ float mlp_guess_call(const MlpWeights& W, __nv_bfloat16* act, float x0, float x1,
+                                                    float x2) {
+    const float x[3] = {x0, x1, x2};
+    return mlp_warp_infer(W, act, x);
+}
+
 // Recovery of one zone; every thread of a warp calls zone() together (the
 // learned guess is a warp-wide inference).
 template <bool MLP>
@@ -67,8 +80,8 @@ struct MixedC2p {
     __device__ static void zone(const StageArgs& a, int slot, const DevBlock& B, int i, int j, bool active,
                                 MlpWeights& W, __nv_bfloat16* act, C2pStats& st) {
         const double gm = a.gm;
-        const float gmf = (float)gm;
-        const float high_thr = (float)(1.0 - 1.0 / (a.w_split * a.w_split));
+        const float gmf = a.gm_f;
+        const float high_thr = a.high_thr_f;
         const int nr = B.nr, nq = B.nq;
         const int64_t n = (int64_t)nr * nq;
         const int64_t z = (int64_t)i * nq + j;
@@ -95,7 +108,7 @@ struct MixedC2p {
             if (__any_sync(0xffffffffu, high)) {
                 float x[3];
                 const bool ok = mlp_features(m, U[1] * U[1] + U[2] * U[2], tau, x);
-                const float y = mlp_warp_infer(W, act, x);
+                const float y = mlp_guess_call(W, act, x[0], x[1], x[2]);
                 const float gsv = mf * __expf(y);
                 guess = (ok && gsv > 0.0f) ? fminf(gsv, (gmf - 1.0f) * tauf) : 0.0f;
             }
@@ -167,7 +180,7 @@ struct MixedC2p {
 };
 
 template <bool MLP>
-__global__ void __launch_bounds__(TILE_THREADS, MLP ? 2 : 3) c2p_mixed_kernel(StageArgs a) {
+__global__ void __launch_bounds__(TILE_THREADS, 3) c2p_mixed_kernel(StageArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
     if (ek != NO_ERROR && (uint32_t)(ek >> 48) < (uint32_t)a.stage) return;
@@ -209,21 +222,123 @@ static int num_sms() {
     return g_sms;
 }
 
+// Resident CTAs of a kernel on the whole device, cached per kernel.
+template <class K>
+static int resident_grid(K kernel, int threads, size_t smem) {
+    static std::mutex mu;
+    static std::map<const void*, int> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    const void* key = reinterpret_cast<const void*>(kernel);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    int per_sm = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    return cache[key] = per_sm * num_sms();
+}
+
 cudaError_t launch_c2p_mixed(const StageArgs& a, cudaStream_t s) {
     if (a.ntiles <= 0) return cudaSuccess;
     if (a.mlp) {
         const size_t bytes = sizeof(MlpWeights) + 8 * MLP_ACT_ELEMS * sizeof(__nv_bfloat16);
-        const int grid = std::min(a.ntiles, num_sms() * 4);
+        const int grid = std::min(a.ntiles, resident_grid(c2p_mixed_kernel<true>, TILE_THREADS, bytes));
         c2p_mixed_kernel<true><<<grid, TILE_THREADS, bytes, s>>>(a);
     } else {
-        c2p_mixed_kernel<false><<<a.ntiles, TILE_THREADS, 0, s>>>(a);
+        const int grid = std::min(a.ntiles, resident_grid(c2p_mixed_kernel<false>, TILE_THREADS, 0));
+        c2p_mixed_kernel<false><<<grid, TILE_THREADS, 0, s>>>(a);
     }
     return cudaGetLastError();
 }
 
+// ---- the update with tensor-copy staging ---------------------------------------
+// A persistent CTA walks its update tiles with two shared-memory buffers: while
+// it computes tile k from one, the tensor copies of tile k + 1 (primitives
+// with halo, U_in, U_base) fill the other. Same arithmetic as update_kernel.
+template <int TR>
+struct TmaSmem {
+    static constexpr size_t P_BYTES = (size_t)NFIELD * (TR + 4) * (TILE_Q + 8) * sizeof(float);
+    static constexpr size_t U_BYTES = (size_t)NFIELD * TR * TILE_Q * sizeof(double);
+    static constexpr size_t BUF = P_BYTES + 2 * U_BYTES;
+    static constexpr size_t WORK = ((StageSmem<float, TR>::work_bytes + 127) / 128) * 128;
+    static constexpr size_t bytes = 128 + 2 * BUF + WORK + 16;   // alignment slack, buffers, work, 2 mbarriers
+};
+
+constexpr int TMA_WAIT_LIMIT = 1 << 22;
+
+template <int TR>
+__global__ void __launch_bounds__(update_threads<TR>(), 1) update_tma_kernel(StageArgs a) {
+    using L = TmaSmem<TR>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char* base = smem_raw + ((128 - (smem_u32(smem_raw) & 127)) & 127);
+    unsigned char* work = base + 2 * L::BUF;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(work + L::WORK);
+    // a failed recovery in this or an earlier stage stops the step
+    if (*(volatile unsigned long long*)&a.status->err_key != NO_ERROR) return;
+    const bool avg = a.sel_base >= 0;
+    const uint32_t tx = (uint32_t)(L::P_BYTES + L::U_BYTES * (avg ? 2 : 1));
+    const TmaMaps* maps = reinterpret_cast<const TmaMaps*>(a.tmaps);
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    auto issue = [&](int tile, int b) {
+        const int4 t = a.utiles[tile];
+        const TmaMaps* m = maps + t.x;
+        unsigned char* d = base + b * L::BUF;
+        mbar_arrive_expect_tx(&bar[b], tx);
+        tma_load_3d(d, &m->P, t.z - 4, t.y, 0, &bar[b]);
+        tma_load_3d(d + L::P_BYTES, &m->U[a.sel_in], t.z, t.y, 0, &bar[b]);
+        if (avg) tma_load_3d(d + L::P_BYTES + L::U_BYTES, &m->U[a.sel_base], t.z, t.y, 0, &bar[b]);
+    };
+    int tile = blockIdx.x;
+    if (threadIdx.x == 0 && tile < a.nutiles) issue(tile, 0);
+    int k = 0;
+    bool ok = true;
+    for (; tile < a.nutiles; ++k, tile += gridDim.x) {
+        const int b = k & 1;
+        const int next = tile + gridDim.x;
+        if (threadIdx.x == 0 && next < a.nutiles) {
+            fence_proxy_async();   // the reads of buffer b ^ 1 (tile k - 1) come first
+            issue(next, b ^ 1);
+        }
+        const bool got = mbar_wait_bounded(&bar[b], (uint32_t)(k >> 1) & 1u, TMA_WAIT_LIMIT);
+        if (!__syncthreads_and(got)) {
+            ok = false;
+            break;
+        }
+        const unsigned char* d = base + b * L::BUF;
+        update_tile<float, true, TR, true>(a, a.utiles[tile], work, reinterpret_cast<const float*>(d),
+                                           reinterpret_cast<const double*>(d + L::P_BYTES),
+                                           reinterpret_cast<const double*>(d + L::P_BYTES + L::U_BYTES));
+        __syncthreads();
+    }
+    if (!ok && threadIdx.x == 0) {
+        // a copy did not complete: record it, and let the copies in flight land
+        // (bounded) before the CTA's shared memory is released
+        atomicExch(&a.status->bar_abort, 2);
+        mbar_wait_bounded(&bar[k & 1], (uint32_t)(k >> 1) & 1u, TMA_WAIT_LIMIT);
+        if (tile + gridDim.x < a.nutiles)
+            mbar_wait_bounded(&bar[(k + 1) & 1], (uint32_t)((k + 1) >> 1) & 1u, TMA_WAIT_LIMIT);
+    }
+}
+
+template <int TR>
+static void update_tma(const StageArgs& a, cudaStream_t s) {
+    const int grid = std::min(a.nutiles, resident_grid(update_tma_kernel<TR>, update_threads<TR>(), TmaSmem<TR>::bytes));
+    update_tma_kernel<TR><<<grid, update_threads<TR>(), TmaSmem<TR>::bytes, s>>>(a);
+}
+
 template <int TR>
 static void update_mixed(const StageArgs& a, cudaStream_t s) {
-    update_kernel<float, true, TR><<<a.nutiles, update_threads<TR>(), StageSmem<float, TR>::bytes, s>>>(a);
+    if (a.tma && a.tmaps) {
+        update_tma<TR>(a, s);
+        return;
+    }
+    const size_t smem = StageSmem<float, TR>::bytes;
+    const int grid = std::min(a.nutiles, resident_grid(update_kernel<float, true, TR>, update_threads<TR>(), smem));
+    update_kernel<float, true, TR><<<grid, update_threads<TR>(), smem, s>>>(a);
 }
 
 cudaError_t launch_update_mixed(const StageArgs& a, cudaStream_t s) {
@@ -238,8 +353,11 @@ cudaError_t launch_update_mixed(const StageArgs& a, cudaStream_t s) {
 
 template <int TR>
 static cudaError_t configure_update_mixed() {
-    return cudaFuncSetAttribute(update_kernel<float, true, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)StageSmem<float, TR>::bytes);
+    cudaError_t e = cudaFuncSetAttribute(update_kernel<float, true, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)StageSmem<float, TR>::bytes);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(update_tma_kernel<TR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)TmaSmem<TR>::bytes);
 }
 
 cudaError_t launch_ghost_mixed(const GhostArgs& a, cudaStream_t s) {

@@ -275,6 +275,71 @@ __device__ __forceinline__ void riemann(const PhysT<R>& ph, const R* pl, const R
     }
 }
 
+// ---- FP32 relativistic forms for the mixed stage ------------------------------
+// The quantities of srhd_side<float> for a face normal fixed at compile time,
+// with the reciprocals shared: 1/W from one rsqrt (W = W^2 / W, v_n = u_n / W,
+// 1 - v^2 = 1/W^2), 1/rho and 1/h once each.
+template <int AXIS>
+__device__ __forceinline__ void srhd_side_f32(const PhysT<float>& ph, float rho, float ur, float uq, float pre,
+                                              float s, Side<float>& S) {
+    const float uu = ur * ur + uq * uq;
+    const float w2 = 1.0f + uu;
+    const float iw = rsqrtf(w2);
+    const float w = w2 * iw;
+    const float pr = pre * (1.0f / rho);     // p / rho
+    const float h = 1.0f + pr * ph.gh;
+    const float d = rho * w;
+    const float m = d * h;
+    const float un = AXIS == 0 ? ur : uq;
+    const float ut = AXIS == 0 ? uq : ur;
+    const float vn = un * iw;
+    S.U[0] = d;
+    S.U[1] = m * ur;
+    S.U[2] = m * uq;
+    const float cs2 = ph.gm * pr * (1.0f / h);
+    const float omv2 = iw * iw;
+    const float v2 = uu * omv2;
+    const float k = 1.0f - cs2;
+    const float a = vn * k;
+    // tau without cancellation: p (gh W^2 - 1) + D u^2 / (W + 1)
+    S.U[3] = pre * (ph.gh * w2 - 1.0f) + d * uu * (1.0f / (w + 1.0f));
+    const float b = sqrtf(cs2 * omv2 * (omv2 + ut * ut * omv2 * k));
+    S.F[0] = S.U[0] * vn;
+    S.F[1] = AXIS == 0 ? S.U[1] * vn + pre : S.U[1] * vn;
+    S.F[2] = AXIS == 1 ? S.U[2] * vn + pre : S.U[2] * vn;
+    S.F[3] = (S.U[3] + pre) * vn;
+    const float inv = 1.0f / (1.0f - v2 * cs2);
+    S.lm = (a - b) * inv;
+    S.lp = (a + b) * inv;
+    S.sU = s * w;
+    S.sF = s * un;
+    S.vn = vn;
+    S.pre = pre;
+}
+
+template <int AXIS>
+__device__ __forceinline__ void riemann_srhd_f32(const PhysT<float>& ph, const float* pl, const float* pr,
+                                                 float sl, float sr, float out[5]) {
+    Side<float> L, Rr;
+    srhd_side_f32<AXIS>(ph, pl[0], pl[1], pl[2], pl[3], sl, L);
+    srhd_side_f32<AXIS>(ph, pr[0], pr[1], pr[2], pr[3], sr, Rr);
+    if (ph.hllc) srhd_hllc(L, Rr, AXIS, out);
+    else hlle(L, Rr, out);
+}
+
+// Geometric sources per unit volume for the FP32 relativistic stage: the
+// enthalpy density rho h = rho + gh p without a division.
+__device__ __forceinline__ void sources_srhd_f32(const PhysT<float>& ph, const float* P, float r, float cot,
+                                                 float S[4]) {
+    const float rho = P[0], ur = P[1], uq = P[2], pre = P[3];
+    const float mass = rho + pre * ph.gh;
+    const float ir = 1.0f / r;
+    S[0] = 0.0f;
+    S[1] = (2.0f * pre + mass * uq * uq) * ir;
+    S[2] = (pre * cot - mass * ur * uq) * ir;
+    S[3] = 0.0f;
+}
+
 // Geometric sources per unit volume (before LIGHT_SPEED and dV).
 template <class R>
 __device__ __forceinline__ void sources(const PhysT<R>& ph, const R* P, R r, R cot, R S[4]) {

@@ -52,6 +52,7 @@ struct StageSmem {
     static constexpr int NFR = NFIELD * (TR + 1) * TQ;
     static constexpr int NFQ = NFIELD * TR * (TQ + 1);
     static constexpr size_t bytes = sizeof(R) * (size_t)(NP + NGR + NGQ + NFR + NFQ);
+    static constexpr size_t work_bytes = sizeof(R) * (size_t)(NGR + NGQ + NFR + NFQ);   // without staged P
 };
 
 template <class R>
@@ -59,22 +60,38 @@ __device__ __forceinline__ PhysT<R> make_phys(const StageArgs& a) {
     PhysT<R> ph;
     ph.srhd = a.srhd;
     ph.hllc = a.hllc;
-    const double gm1 = a.gm - 1.0;
-    ph.gm = (R)a.gm;
-    ph.gm1 = (R)gm1;
-    ph.gh = (R)(a.gm / gm1);
-    ph.theta = (R)a.plm_theta;
+    if constexpr (sizeof(R) == 4) {
+        ph.gm = a.gm_f;
+        ph.gm1 = a.gm1_f;
+        ph.gh = a.gh_f;
+        ph.theta = a.theta_f;
+    } else {
+        ph.gm = a.gm;
+        ph.gm1 = a.gm - 1.0;
+        ph.gh = a.gh;
+        ph.theta = a.plm_theta;
+    }
     return ph;
 }
 
 // One update tile t = {slot, i0, j0, -} with update_threads<TR>() threads.
-template <class R, bool MIXED, int TR_>
-__device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, unsigned char* smem_raw) {
+// BOX = false: the tile's primitives are staged here from the padded P array
+// and the conserved state is read from global memory. BOX = true: both are
+// already in shared memory as tensor-copy boxes: boxP [5][TR+4][TQ+8] from
+// padded row i0 and column j0 - 4 (zero outside the block), boxU / boxU0
+// [5][TR][TQ] from row i0, column j0 (boxU0 only with an RK average).
+template <class R, bool MIXED, int TR_, bool BOX = false>
+__device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, unsigned char* smem_raw,
+                                            const R* boxP = nullptr, const double* boxU = nullptr,
+                                            const double* boxU0 = nullptr) {
     using S = StageSmem<R, TR_>;
     constexpr int TR = S::TR, TQ = S::TQ, PR = S::PR, PQ = S::PQ;
+    constexpr int PQS = BOX ? TQ + 8 : PQ;   // row stride of the staged primitives
+    constexpr int COFF = BOX ? 2 : 0;        // column of j0 - 2 in a staged row
     constexpr int NT = update_threads<TR>();
-    R* sP = reinterpret_cast<R*>(smem_raw);
-    R* sGr = sP + S::NP;
+    R* sP = BOX ? nullptr : reinterpret_cast<R*>(smem_raw);
+    const R* sPc = BOX ? boxP + COFF : sP;
+    R* sGr = reinterpret_cast<R*>(smem_raw) + (BOX ? 0 : S::NP);
     R* sGq = sGr + S::NGR;
     R* sFr = sGq + S::NGQ;
     R* sFq = sFr + S::NFR;
@@ -85,7 +102,7 @@ __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, un
     const R* P = reinterpret_cast<const R*>(B.P);
     const int64_t pn = (int64_t)(nr + 4) * nq;
     const bool one_d = a.one_dimensional != 0;
-    if (MIXED && tid < TR * TQ) {
+    if (MIXED && !BOX && tid < TR * TQ) {
         // the state this thread updates at the end: start it towards L2 now
         const int i = i0 + tid / TQ, j = j0 + tid % TQ;
         if (i < nr && j < nq) {
@@ -99,16 +116,18 @@ __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, un
     }
 
     // ---- stage primitives (tile rows -2..TR+1 = padded rows i0..i0+TR+3)
-    for (int k = tid; k < PR * PQ; k += NT) {
-        const int rr = k / PQ, cc = k - rr * PQ;
-        const int prow = i0 + rr;
-        const int j = j0 - 2 + cc;
-        const bool ok = prow < nr + 4 && j >= 0 && j < nq;
-        const int64_t off = (int64_t)prow * nq + j;
+    if (!BOX) {
+        for (int k = tid; k < PR * PQ; k += NT) {
+            const int rr = k / PQ, cc = k - rr * PQ;
+            const int prow = i0 + rr;
+            const int j = j0 - 2 + cc;
+            const bool ok = prow < nr + 4 && j >= 0 && j < nq;
+            const int64_t off = (int64_t)prow * nq + j;
 #pragma unroll
-        for (int q = 0; q < NFIELD; ++q) sP[(q * PR + rr) * PQ + cc] = ok ? P[q * pn + off] : R(0);
+            for (int q = 0; q < NFIELD; ++q) sP[(q * PR + rr) * PQ + cc] = ok ? P[q * pn + off] : R(0);
+        }
+        __syncthreads();
     }
-    __syncthreads();
 
     const PhysT<R> ph = make_phys<R>(a);
     const R th = ph.theta;
@@ -123,9 +142,9 @@ __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, un
                 const int g = k / TQ, c = k - g * TQ;
 #pragma unroll
                 for (int q = 0; q < NFIELD; ++q) {
-                    const R* col = sP + (q * PR) * PQ + c + 2;
+                    const R* col = sPc + (q * PR) * PQS + c + 2;
                     sGr[(q * (TR + 2) + g) * TQ + c] =
-                        plm_gradient(th, col[g * PQ], col[(g + 1) * PQ], col[(g + 2) * PQ]);
+                        plm_gradient(th, col[g * PQS], col[(g + 1) * PQS], col[(g + 2) * PQS]);
                 }
             } else {
                 const int kk = k - NGRZ;
@@ -134,7 +153,7 @@ __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, un
                 const bool edge = j <= 0 || j >= nq - 1;
 #pragma unroll
                 for (int q = 0; q < NFIELD; ++q) {
-                    const R* row = sP + (q * PR + r + 2) * PQ + c;
+                    const R* row = sPc + (q * PR + r + 2) * PQS + c;
                     sGq[(q * TR + r) * (TQ + 2) + c] = edge ? R(0) : plm_gradient(th, row[0], row[1], row[2]);
                 }
             }
@@ -142,7 +161,7 @@ __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, un
     }
     __syncthreads();
 
-    const R cflux = (R)a.cflux;
+    const R cflux = sizeof(R) == 4 ? (R)a.cflux_f : (R)a.cflux;
 
     // ---- radial faces i0..i0+TR (face i between zone rows i-1 and i): one
     // pass of all NT threads
@@ -154,12 +173,13 @@ __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, un
             R pl[4], pr[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                pl[q] = sP[(q * PR + f + 1) * PQ + c + 2] + sGr[(q * (TR + 2) + f) * TQ + c] * R(0.5);
-                pr[q] = sP[(q * PR + f + 2) * PQ + c + 2] - sGr[(q * (TR + 2) + f + 1) * TQ + c] * R(0.5);
+                pl[q] = sPc[(q * PR + f + 1) * PQS + c + 2] + sGr[(q * (TR + 2) + f) * TQ + c] * R(0.5);
+                pr[q] = sPc[(q * PR + f + 2) * PQS + c + 2] - sGr[(q * (TR + 2) + f + 1) * TQ + c] * R(0.5);
             }
-            const R sl = sP[(4 * PR + f + 1) * PQ + c + 2] + sGr[(4 * (TR + 2) + f) * TQ + c] * R(0.5);
-            const R sr = sP[(4 * PR + f + 2) * PQ + c + 2] - sGr[(4 * (TR + 2) + f + 1) * TQ + c] * R(0.5);
-            riemann(ph, pl, pr, sl, sr, 0, out);
+            const R sl = sPc[(4 * PR + f + 1) * PQS + c + 2] + sGr[(4 * (TR + 2) + f) * TQ + c] * R(0.5);
+            const R sr = sPc[(4 * PR + f + 2) * PQS + c + 2] - sGr[(4 * (TR + 2) + f + 1) * TQ + c] * R(0.5);
+            if constexpr (MIXED) riemann_srhd_f32<0>(ph, pl, pr, sl, sr, out);
+            else riemann(ph, pl, pr, sl, sr, 0, out);
             if constexpr (MIXED) {
                 const float2 A = df_mul(B.ar_r[i], B.ar_q[j]);   // c A_r
 #pragma unroll
@@ -184,12 +204,13 @@ __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, un
                 R pl[4], pr[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    pl[q] = sP[(q * PR + r + 2) * PQ + c + 1] + sGq[(q * TR + r) * (TQ + 2) + c] * R(0.5);
-                    pr[q] = sP[(q * PR + r + 2) * PQ + c + 2] - sGq[(q * TR + r) * (TQ + 2) + c + 1] * R(0.5);
+                    pl[q] = sPc[(q * PR + r + 2) * PQS + c + 1] + sGq[(q * TR + r) * (TQ + 2) + c] * R(0.5);
+                    pr[q] = sPc[(q * PR + r + 2) * PQS + c + 2] - sGq[(q * TR + r) * (TQ + 2) + c + 1] * R(0.5);
                 }
-                const R sl = sP[(4 * PR + r + 2) * PQ + c + 1] + sGq[(4 * TR + r) * (TQ + 2) + c] * R(0.5);
-                const R sr = sP[(4 * PR + r + 2) * PQ + c + 2] - sGq[(4 * TR + r) * (TQ + 2) + c + 1] * R(0.5);
-                riemann(ph, pl, pr, sl, sr, 1, out);
+                const R sl = sPc[(4 * PR + r + 2) * PQS + c + 1] + sGq[(4 * TR + r) * (TQ + 2) + c] * R(0.5);
+                const R sr = sPc[(4 * PR + r + 2) * PQS + c + 2] - sGq[(4 * TR + r) * (TQ + 2) + c + 1] * R(0.5);
+                if constexpr (MIXED) riemann_srhd_f32<1>(ph, pl, pr, sl, sr, out);
+                else riemann(ph, pl, pr, sl, sr, 1, out);
                 if constexpr (MIXED) {
                     const float2 A = df_mul(B.aq_r[i], B.aq_q[j]);   // c A_theta
 #pragma unroll
@@ -215,18 +236,18 @@ __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, un
             const int64_t z = (int64_t)i * nq + j;
             R Pc[4];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) Pc[q] = sP[(q * PR + r + 2) * PQ + c + 2];
+            for (int q = 0; q < 4; ++q) Pc[q] = sPc[(q * PR + r + 2) * PQS + c + 2];
             R src[4];
             R dV = R(0);
             float2 cdV = make_float2(0.f, 0.f);
             if constexpr (MIXED) {
-                sources(ph, Pc, (R)B.rc32[i], (R)B.cot32[j], src);
+                sources_srhd_f32(ph, Pc, B.rc32[i], B.cot32[j], src);
                 cdV = df_mul(B.dv_r[i], B.dv_q[j]);   // c dV
             } else {
                 sources(ph, Pc, (R)B.rc[i], (R)B.cot[j], src);
                 dV = (R)B.dv[z];
             }
-            const R dt = (R)a.dt;
+            const R dt = sizeof(R) == 4 ? (R)a.dt_f : (R)a.dt;
             const double* Uin = B.buf[a.sel_in];
             double* Uout = B.buf[a.sel_out];
             const double* U0 = a.sel_base >= 0 ? B.buf[a.sel_base] : nullptr;
@@ -246,7 +267,8 @@ __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, un
                     const R fd = sFq[(q * TR + r) * (TQ + 1) + c + 1];
                     du = (sc - (fb - fa) - (fd - fc)) * dt;
                 }
-                res[q] = Uin[q * n + z] + (MIXED ? f2d((float)du) : (double)du);
+                const double uin = BOX ? boxU[(q * TR + r) * TQ + c] : Uin[q * n + z];
+                res[q] = uin + (MIXED ? f2d((float)du) : (double)du);
             }
             {
                 const R fa = sFr[(4 * (TR + 1) + r) * TQ + c];
@@ -259,16 +281,19 @@ __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, un
                     const R fd = sFq[(4 * TR + r) * (TQ + 1) + c + 1];
                     ds = ((fb - fa) + (fd - fc)) * -dt;
                 }
-                res[4] = Uin[4 * n + z] + (MIXED ? f2d((float)ds) : (double)ds);
+                const double uin = BOX ? boxU[(4 * TR + r) * TQ + c] : Uin[4 * n + z];
+                res[4] = uin + (MIXED ? f2d((float)ds) : (double)ds);
             }
             if (U0) {
-                if (MIXED && a.w1 == 0.5 && a.bf == 0.5) {
+                if (MIXED && a.avg_half) {
                     // RK2 average (U1 + U0) / 2 with the halving on the integer pipe
 #pragma unroll
-                    for (int q = 0; q < NFIELD; ++q) res[q] = half_exact(res[q] + U0[q * n + z]);
+                    for (int q = 0; q < NFIELD; ++q)
+                        res[q] = half_exact(res[q] + (BOX ? boxU0[(q * TR + r) * TQ + c] : U0[q * n + z]));
                 } else {
 #pragma unroll
-                    for (int q = 0; q < NFIELD; ++q) res[q] = res[q] * a.w1 + U0[q * n + z] * a.bf;
+                    for (int q = 0; q < NFIELD; ++q)
+                        res[q] = res[q] * a.w1 + (BOX ? boxU0[(q * TR + r) * TQ + c] : U0[q * n + z]) * a.bf;
                 }
             }
 #pragma unroll
@@ -277,7 +302,8 @@ __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, un
     }
 }
 
-// One CTA per update tile (a.utiles).
+// Update tiles (a.utiles) in a grid-stride loop: the launch is sized to the
+// resident CTAs, so no CTA pays start-up per tile.
 template <class R, bool MIXED, int TR>
 __global__ void __launch_bounds__(update_threads<TR>(), MIXED ? (TR == 4 ? 6 : TR == 8 ? 3 : 2) : 1)
     update_kernel(StageArgs a) {
@@ -285,7 +311,10 @@ __global__ void __launch_bounds__(update_threads<TR>(), MIXED ? (TR == 4 ? 6 : T
     // A failed c2p in this or an earlier stage stops the step: keep the
     // input state untouched so the failure can be reported from it.
     if (*(volatile unsigned long long*)&a.status->err_key != NO_ERROR) return;
-    update_tile<R, MIXED, TR>(a, a.utiles[blockIdx.x], smem_raw);
+    for (int tile = blockIdx.x; tile < a.nutiles; tile += gridDim.x) {
+        update_tile<R, MIXED, TR>(a, a.utiles[tile], smem_raw);
+        __syncthreads();
+    }
 }
 
 // Block-wide reduction helpers (warp shuffles, then one atomic per warp).

@@ -127,7 +127,7 @@ class Error(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("tile_rows", C.c_int32), ("fused", C.c_int32), ("ctas_per_sm", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("tma", C.c_int32)]
 
 
 class MlpTrainParams(C.Structure):
@@ -179,6 +179,7 @@ SIGNATURES = {
     "knc_set_c2p_guess": (C.c_int, [_P, C.c_int32, _FP, C.c_size_t]),
     "knc_set_batched": (C.c_int, [_P, C.c_int32]),
     "knc_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+    "knc_zone_updates": (C.c_int, [_P, _I64P]),
     "knc_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
     "knc_autotune": (C.c_int, [_P, C.c_int32, C.POINTER(Tuning), _DP]),
     "knc_set_mixed_w_split": (C.c_int, [_P, C.c_double]),

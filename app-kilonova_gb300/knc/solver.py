@@ -105,14 +105,16 @@ class Solver:
     def set_batched(self, graph: bool):
         self._check(self.lib.knc_set_batched(self.h, int(bool(graph))), "set_batched")
 
-    def set_tuning(self, tile_rows: int = 8, fused: bool = False, ctas_per_sm: int = 0):
-        t = abi.Tuning(tile_rows=int(tile_rows), fused=int(bool(fused)), ctas_per_sm=int(ctas_per_sm))
+    def set_tuning(self, tile_rows: int = 8, fused: bool = False, ctas_per_sm: int = 0, tma: bool = False):
+        t = abi.Tuning(tile_rows=int(tile_rows), fused=int(bool(fused)), ctas_per_sm=int(ctas_per_sm),
+                       tma=int(bool(tma)))
         self._check(self.lib.knc_set_tuning(self.h, C.byref(t)), "set_tuning")
 
     def tuning(self) -> dict:
         t = abi.Tuning()
         self._check(self.lib.knc_get_tuning(self.h, C.byref(t)), "get_tuning")
-        return {"tile_rows": t.tile_rows, "fused": bool(t.fused), "ctas_per_sm": t.ctas_per_sm}
+        return {"tile_rows": t.tile_rows, "fused": bool(t.fused), "ctas_per_sm": t.ctas_per_sm,
+                "tma": bool(t.tma)}
 
     def autotune(self, reps: int = 5):
         """Time every launch shape on the live state, keep the fastest; returns
@@ -120,7 +122,13 @@ class Solver:
         t = abi.Tuning()
         ms = C.c_double()
         self._check(self.lib.knc_autotune(self.h, int(reps), C.byref(t), C.byref(ms)), "autotune")
-        return {"tile_rows": t.tile_rows, "fused": bool(t.fused), "ctas_per_sm": t.ctas_per_sm}, ms.value
+        return {"tile_rows": t.tile_rows, "fused": bool(t.fused), "ctas_per_sm": t.ctas_per_sm,
+                "tma": bool(t.tma)}, ms.value
+
+    def zone_updates(self) -> int:
+        n = C.c_int64()
+        self._check(self.lib.knc_zone_updates(self.h, C.byref(n)), "zone_updates")
+        return n.value
 
     def set_mixed_w_split(self, w: float):
         self._check(self.lib.knc_set_mixed_w_split(self.h, float(w)), "set_mixed_w_split")
@@ -288,6 +296,7 @@ def measure_fp64_peak() -> float:
 def build_solver(workload, precision=abi.KNC_PRECISION_FP64):
     """Solver for a knc.workloads.Workload with its model set and initial data."""
     s = Solver(workload.hydro, workload.mesh, precision=precision)
+    workload.apply_shapes(s)
     s.set_model(workload.model)
     s.init_from_model(0.0)
     return s

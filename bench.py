@@ -243,14 +243,16 @@ def run_knc(args):
     weights, train_loss = learned.train(np.concatenate([pairs, run_pairs]), steps=args.train_steps, seed=11)
     train_s = time.perf_counter() - t0
 
-    def make(mixed: bool, guess: bool, graph: bool):
-        s = knc.build_solver(w)
+    def make(mixed: bool, guess: bool, graph: bool, workload=None, tune=False):
+        s = knc.build_solver(workload or w)
         if mixed:
             s.set_precision(abi.KNC_PRECISION_MIXED)
             s.set_mixed_w_split(args.w_split)
         if guess:
             s.set_c2p_guess(abi.KNC_GUESS_MLP, weights)
         s.set_batched(graph)
+        if tune:
+            s.autotune(reps=3)
         return s
 
     def timed(s, steps, fold):
@@ -259,6 +261,7 @@ def run_knc(args):
         s.synchronize()
         barrier(pg)
         l0 = s.launch_count()
+        z0 = s.zone_updates()
         s.mark(0)
         done = 0
         while done < steps:
@@ -267,6 +270,7 @@ def run_knc(args):
             done += f
         s.mark(1)
         ms = s.elapsed_ms(0, 1)
+        timed.zone_updates = s.zone_updates() - z0
         return ms, s.launch_count() - l0
 
     # ---- plain FP64 path
@@ -280,7 +284,8 @@ def run_knc(args):
 
     # ---- headline: mixed + learned + graph
     clocks = ClockSampler(local)
-    head = make(True, True, True)
+    head = make(True, True, True, tune=True)
+    tuning = head.tuning()
     head.reset_c2p_stats()
     clocks.start()
     msh, launches = timed(head, args.steps, args.fold)
@@ -329,6 +334,33 @@ def run_knc(args):
     e2e = zones * args.steps * world / (e2e_ms * 1e-3)
     h2d = cons.array.nbytes + scal.array.nbytes
 
+    # ---- batched uneven blocks with moving excision (RK3, autotuned launch shape)
+    un = None
+    if not args.no_uneven:
+        wu = workloads.uneven(seed=1 + rank)
+        u64 = make(False, False, False, workload=wu)
+        ms_u64, _ = timed(u64, args.steps, args.fold)
+        zu64 = timed.zone_updates
+        uh = make(True, True, True, workload=wu, tune=True)
+        ms_uh, launches_u = timed(uh, args.steps, args.fold)
+        zuh = timed.zone_updates
+        ms_u64 = max_over_ranks(pg, ms_u64)
+        ms_uh = max_over_ranks(pg, ms_uh)
+        same_blocks = uh.block_indexes() == u64.block_indexes()
+        un = {"workload": f"{wu.name}: {wu.zones} zones at start, nr from 32..512 and nq from 64..256 "
+                          "per block (seeded), RK3, both excision surfaces at 0.5c",
+              "zones_start": wu.zones, "blocks_end": len(uh.block_indexes()),
+              "block_range_end": [uh.block_indexes()[0], uh.block_indexes()[-1]],
+              "value": zuh * world / (ms_uh * 1e-3), "fp64_value": zu64 * world / (ms_u64 * 1e-3),
+              "speedup_vs_fp64": (zuh / ms_uh) / (zu64 / ms_u64),
+              "ms_per_step": ms_uh / args.steps, "fp64_ms_per_step": ms_u64 / args.steps,
+              "l1_density": l1_density(uh, u64) if same_blocks else None,
+              "tuning": uh.tuning(), "launches_per_stage": launches_u / (3 * args.steps),
+              "path": "mixed + learned guess + one CUDA graph per fold; each RK3 stage one launch when the "
+                      "autotuner picks the fused form"}
+        u64.close()
+        uh.close()
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(w, args.cpu_blocks, args.cpu_steps)
@@ -344,7 +376,7 @@ def run_knc(args):
                        "zones": zones, "path": f"mixed precision (FP64 recovery above W={args.w_split}), "
                                                "learned c2p guess, CUDA graph per fold",
                        "fold": args.fold, "l2": "state 168 MB per buffer > 129 MB L2 (no flush needed)",
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": f"replicas x{world}", "tuning": tuning},
             "fp64": {"value": v64, "ms_per_step": ms64 / args.steps,
                      "newton_iters_per_zone": st64["iters_fp64"] / max(st64["zones"], 1),
                      "fp64_peak_gflops": fp64_peak},
@@ -361,6 +393,8 @@ def run_knc(args):
             "gpu_launches": launches,
             "clocks": clk,
         }
+        if un:
+            line["batched_uneven"] = un
         if cpu:
             line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
         print(json.dumps(line), flush=True)
@@ -373,8 +407,10 @@ def run_only(args):
     """One path alone on the workload, for profiler captures: warmup + steps."""
     import knc
     from knc import abi, learned, workloads
-    w = workloads.wind_large()
+    w = workloads.WORKLOADS[args.workload]()
     s = knc.build_solver(w)
+    if args.tile_rows:
+        s.set_tuning(tile_rows=args.tile_rows, fused=args.fused, tma=args.tma)
     if args.only == "mixed":
         s.set_precision(abi.KNC_PRECISION_MIXED)
         s.set_mixed_w_split(args.w_split)
@@ -407,6 +443,11 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--ref-blocks", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-uneven", action="store_true")
+    ap.add_argument("--workload", default="wind_large", help="workload of --only runs")
+    ap.add_argument("--tile-rows", type=int, default=0, help="launch shape of --only runs (0: default)")
+    ap.add_argument("--fused", action="store_true")
+    ap.add_argument("--tma", action="store_true")
     ap.add_argument("--only", choices=["fp64", "mixed"], default=None,
                     help="run one path alone (profiler captures)")
     args = ap.parse_args()

@@ -238,17 +238,21 @@ int knc_set_batched(knc_ctx* ctx, int32_t graph);
  *                update); 1: one persistent cooperative launch whose phases
  *                are separated by bounded grid barriers (bit-identical result)
  *   ctas_per_sm  fused grid = ctas_per_sm x SMs CTAs (0: the occupancy bound;
- *                larger values are clamped to it) */
+ *                larger values are clamped to it)
+ *   tma          mixed precision, separate form: the update stages each tile
+ *                (primitives with halo, U_in, U_base) with tensor copies into
+ *                double-buffered shared memory, one tile ahead; used when
+ *                every block has nq % 4 == 0, nq >= 40 and nr >= tile_rows */
 typedef struct knc_tuning {
     int32_t tile_rows;
     int32_t fused;
     int32_t ctas_per_sm;
-    int32_t reserved;
+    int32_t tma;
 } knc_tuning;
 int knc_set_tuning(knc_ctx* ctx, const knc_tuning* tuning);
 int knc_get_tuning(const knc_ctx* ctx, knc_tuning* tuning);
 /* Autotuner: times every candidate shape (tile rows x separate / fused x CTAs
- * per SM) with `reps` first-stage launches each on the live state (they write
+ * per SM x tensor-copy staging) with `reps` first-stage launches each on the live state (they write
  * only the scratch buffer and primitives, so the state is unchanged), keeps
  * the fastest and returns it with its time per stage (either output may be
  * NULL). */
@@ -270,6 +274,9 @@ int knc_c2p_stats(knc_ctx* ctx, int64_t* zones, int64_t* iters_fp64,
 int knc_reset_c2p_stats(knc_ctx* ctx);
 /* Kernel launches issued by the context since creation. */
 int knc_launch_count(const knc_ctx* ctx, int64_t* launches);
+/* Zone-updates since creation: the live zones summed over every RK step
+ * advanced (the block set of a moving mesh changes between steps). */
+int knc_zone_updates(const knc_ctx* ctx, int64_t* zone_updates);
 
 /* Per-kernel timing with CUDA events on the context's stream. While enabled,
  * every launch is bracketed by events; knc_kernel_times returns, per kind

@@ -128,3 +128,39 @@ def test_fused_counts_one_launch_per_stage():
     n1 = C.c_int64()
     g.lib.knc_launch_count(g.h, C.byref(n1))
     assert n1.value - n0.value == 3 * 2      # RK2: two stages per step, one launch each
+
+
+@pytest.mark.parametrize("tile_rows", [4, 8, 16])
+def test_mixed_tma_staging_matches(tile_rows):
+    """The tensor-copy staged update reads the same values from shared
+    memory that the plain update reads from global memory."""
+    from knc import workloads
+    w = workloads.wind_small()
+    ref = _mixed(w, tile_rows, False, False)
+    import knc
+    g, _ = make_pair(w, gpu=True)
+    g.set_precision(knc.abi.KNC_PRECISION_MIXED)
+    g.set_tuning(tile_rows=tile_rows, tma=True)
+    g.set_batched(True)
+    for _ in range(2):
+        g.advance(3)
+    assert _same(g.state(), ref.state())
+
+
+def test_mixed_tma_uneven_moving():
+    """96 uneven blocks (nq 64..256), moving excision, RK3: tensor-copy staging
+    inside the captured fold equals the plain separate launches."""
+    import knc
+    from knc import workloads
+    w = workloads.uneven()
+    ref = knc.build_solver(w)
+    ref.set_precision(knc.abi.KNC_PRECISION_MIXED)
+    g = knc.build_solver(w)
+    g.set_precision(knc.abi.KNC_PRECISION_MIXED)
+    g.set_tuning(tile_rows=8, tma=True)
+    g.set_batched(True)
+    for _ in range(2):
+        ref.advance(4)
+        g.advance(4)
+    assert g.block_indexes() == ref.block_indexes()
+    assert _same(g.state(), ref.state())
