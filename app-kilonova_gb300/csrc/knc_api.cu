@@ -222,10 +222,14 @@ struct Layout {
     int utiles_cap = 0;
     int nutiles = 0;
     int utr = 0;
+    int uform = -1;
     int64_t nzones = 0;         // zones of the block set
     TmaMaps* d_tmaps = nullptr; // tensor maps per slot (tiles of `utr` rows), when every block allows them
     int tmaps_cap = 0;
     bool tma_ok = false;
+    int4* d_strips = nullptr;   // warp strips {slot, i0, j0, rows} of `utr` rows (strip form)
+    int strips_cap = 0;
+    int nstrips = 0;
     int4* d_chunks = nullptr;   // fused recovery chunks {slot, z0, nz, 0} of <= stage_threads(utr) zones
     int chunks_cap = 0;
     int nchunks = 0;
@@ -255,6 +259,7 @@ void free_layout(Layout& l) {
     cudaFree(l.d_tiles);
     cudaFree(l.d_utiles);
     cudaFree(l.d_chunks);
+    cudaFree(l.d_strips);
     cudaFree(l.d_tmaps);
     cudaFree(l.d_remap);
     cudaFree(l.d_ghost_rc);
@@ -275,6 +280,8 @@ struct knc_ctx {
     void* host_user = nullptr;
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;        // ghost rows run here, beside the recovery
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::map<int32_t, BlockH> blocks;
     std::map<std::pair<int64_t, int64_t>, std::vector<BlockH>> pool;   // freed block storage by shape
     int cur = 0;
@@ -311,7 +318,7 @@ struct knc_ctx {
     int32_t batched = 0;
     int32_t utr = 8;   // update tile rows (4, 8 or 16)
     int32_t fused = 0;         // one cooperative launch per stage
-    int32_t tma = 0;           // mixed update stages tiles with tensor copies
+    int32_t uform = KNC_UPDATE_TILE;   // update form of the separate stage
     int32_t ctas_per_sm = 0;   // fused grid: CTAs per SM (0: the occupancy bound)
     int32_t sms = 0;
     bool coop = false;         // the device supports cooperative launches
@@ -538,10 +545,10 @@ bool encode_block_maps(const BlockH& b, int tr, TmaMaps* m) {
 
 // Rebuild the device block table and the tile list after the block set changed.
 int rebuild_table(knc_ctx* c) {
-    if (!c->dirty && L(c).utr == c->utr) return KNC_OK;
+    if (!c->dirty && L(c).utr == c->utr && L(c).uform == c->uform) return KNC_OK;
     const int nb = (int)c->blocks.size();
     std::vector<DevBlock> tab(nb);
-    std::vector<int4> tiles, utiles, chunks;
+    std::vector<int4> tiles, utiles, chunks, strips;
     std::vector<TmaMaps> maps(nb);
     bool tma_ok = nb > 0;
     const int nt = stage_threads(c->utr);
@@ -602,9 +609,16 @@ int rebuild_table(knc_ctx* c) {
         for (int64_t i0 = 0; i0 < b.nr; i0 += TILE_R)
             for (int64_t j0 = 0; j0 < b.nq; j0 += TILE_Q)
                 tiles.push_back(make_int4(slot, (int)i0, (int)j0, (int)zoff));
-        for (int64_t i0 = 0; i0 < b.nr; i0 += c->utr)
-            for (int64_t j0 = 0; j0 < b.nq; j0 += TILE_Q) utiles.push_back(make_int4(slot, (int)i0, (int)j0, 0));
-        if (tma_ok) tma_ok = encode_block_maps(b, c->utr, &maps[k]);
+        if (c->uform == KNC_UPDATE_STRIP) {
+            for (int64_t j0 = 0; j0 < b.nq; j0 += STRIP_OUT)
+                for (int64_t i0 = 0; i0 < b.nr; i0 += c->utr)
+                    strips.push_back(make_int4(slot, (int)i0, (int)j0, (int)std::min<int64_t>(c->utr, b.nr - i0)));
+        } else {
+            for (int64_t i0 = 0; i0 < b.nr; i0 += c->utr)
+                for (int64_t j0 = 0; j0 < b.nq; j0 += TILE_Q)
+                    utiles.push_back(make_int4(slot, (int)i0, (int)j0, 0));
+        }
+        if (tma_ok) tma_ok = c->utr <= 16 && encode_block_maps(b, c->utr, &maps[k]);
         for (int64_t z0 = 0; z0 < b.nr * b.nq; z0 += nt)
             chunks.push_back(make_int4(slot, (int)z0, (int)std::min<int64_t>(nt, b.nr * b.nq - z0), 0));
         L(c).slot_index.push_back(b.index);
@@ -648,6 +662,17 @@ int rebuild_table(knc_ctx* c) {
         CK(cudaMemcpyAsync(L(c).d_chunks, chunks.data(), chunks.size() * sizeof(int4), cudaMemcpyHostToDevice,
                            c->stream));
     L(c).nchunks = (int)chunks.size();
+    if ((int)strips.size() > L(c).strips_cap) {
+        cudaFree(L(c).d_strips);
+        L(c).d_strips = nullptr;
+        CK(dalloc(&L(c).d_strips, strips.size()));
+        L(c).strips_cap = (int)strips.size();
+    }
+    if (!strips.empty())
+        CK(cudaMemcpyAsync(L(c).d_strips, strips.data(), strips.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                           c->stream));
+    L(c).nstrips = (int)strips.size();
+    L(c).uform = c->uform;
     L(c).nzones = zoff;
     L(c).tma_ok = false;
     if (tma_ok) {
@@ -810,8 +835,10 @@ StageArgs base_args(knc_ctx* c) {
     a.utiles = L(c).d_utiles;
     a.nutiles = L(c).nutiles;
     a.utr = L(c).utr;
-    a.tma = c->tma && L(c).tma_ok ? 1 : 0;
+    a.tma = c->uform == KNC_UPDATE_TILE_TMA && L(c).tma_ok ? 1 : 0;
     a.tmaps = L(c).tma_ok ? L(c).d_tmaps : nullptr;
+    a.strips = c->uform == KNC_UPDATE_STRIP ? L(c).d_strips : nullptr;
+    a.nstrips = c->uform == KNC_UPDATE_STRIP ? L(c).nstrips : 0;
     a.srhd = c->hp.system == KNC_SYSTEM_RELATIVISTIC;
     a.hllc = c->hp.riemann_solver == KNC_RIEMANN_HLLC;
     a.one_dimensional = c->mesh.p.num_polar_zones == 1;
@@ -930,12 +957,24 @@ int run_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, doub
         ++c->launches;
         return KNC_OK;
     }
-    {
-        ProfScope ps(c, KNC_KERNEL_GHOST);
-        CK(mixed(c) ? launch_ghost_mixed(g, c->stream) : launch_ghost_f64(g, c->stream));
+    if (c->profiling) {
+        // timed one kernel after another
+        {
+            ProfScope ps(c, KNC_KERNEL_GHOST);
+            CK(mixed(c) ? launch_ghost_mixed(g, c->stream) : launch_ghost_f64(g, c->stream));
+        }
+        if ((r = launch_c2p(c, a))) return r;
+    } else {
+        // the ghost rows (mesh-end halos, a short FP64 latency chain) beside the
+        // recovery, which writes interior rows and inner halos only
+        CK(cudaEventRecord(c->ev_fork, c->stream));
+        CK(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+        CK(mixed(c) ? launch_ghost_mixed(g, c->side) : launch_ghost_f64(g, c->side));
+        CK(cudaEventRecord(c->ev_join, c->side));
+        if ((r = launch_c2p(c, a))) return r;
+        CK(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
     }
     ++c->launches;
-    if ((r = launch_c2p(c, a))) return r;
     if (lay.nremap) {
         CK(mixed(c) ? launch_remap_mixed(a, lay.d_remap, lay.nremap, lay.max_nq, c->stream)
                     : launch_remap_f64(a, lay.d_remap, lay.nremap, lay.max_nq, c->stream));
@@ -1264,6 +1303,9 @@ int create_device_side(knc_ctx* c) {
     CK(configure_kernels());
     CK(cudaGetDevice(&c->device));
     CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
     {
         int coop = 0;
         CK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device));
@@ -1353,6 +1395,12 @@ void knc_destroy(knc_ctx* c) {
     drain_profile(c);
     for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
     if (c->h_status) cudaFreeHost(c->h_status);
+    if (c->side) {
+        cudaStreamSynchronize(c->side);
+        cudaStreamDestroy(c->side);
+    }
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -1832,15 +1880,21 @@ int knc_zone_updates(const knc_ctx* c, int64_t* n) {
 
 int knc_set_tuning(knc_ctx* c, const knc_tuning* t) {
     if (!c || !t) return KNC_ERR_INVALID_ARGUMENT;
-    if (t->tile_rows != 4 && t->tile_rows != 8 && t->tile_rows != 16)
-        return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "tile_rows must be 4, 8 or 16");
+    if (t->update_form < KNC_UPDATE_TILE || t->update_form > KNC_UPDATE_STRIP)
+        return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "unknown update form %d", t->update_form);
+    const bool strip = t->update_form == KNC_UPDATE_STRIP && !t->fused;
+    if (strip ? (t->tile_rows < 4 || t->tile_rows > 64)
+              : (t->tile_rows != 4 && t->tile_rows != 8 && t->tile_rows != 16))
+        return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "tile_rows must be 4, 8 or 16 (tiles) or 4..64 (strips)");
+    if (strip && c->mesh.p.num_polar_zones == 1)
+        return set_msg(c, KNC_ERR_UNSUPPORTED, "warp strips need num_polar_zones > 1");
     if (t->ctas_per_sm < 0) return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "ctas_per_sm must be >= 0");
     if (t->fused && !c->coop)
         return set_msg(c, KNC_ERR_UNSUPPORTED, "the device has no cooperative launch (fused stage)");
     c->utr = t->tile_rows;
     c->fused = t->fused ? 1 : 0;
     c->ctas_per_sm = t->ctas_per_sm;
-    c->tma = t->tma ? 1 : 0;
+    c->uform = t->fused ? KNC_UPDATE_TILE : t->update_form;
     return KNC_OK;
 }
 
@@ -1849,7 +1903,7 @@ int knc_get_tuning(const knc_ctx* c, knc_tuning* t) {
     t->tile_rows = c->utr;
     t->fused = c->fused;
     t->ctas_per_sm = c->ctas_per_sm;
-    t->tma = c->tma;
+    t->update_form = c->uform;
     return KNC_OK;
 }
 
@@ -1864,11 +1918,14 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
     if ((r = time_step_impl(c, &dt))) return r;
     DevStatus saved;
     CK(cudaMemcpy(&saved, c->d_status, sizeof(saved), cudaMemcpyDeviceToHost));
-    const knc_tuning keep = {c->utr, c->fused, c->ctas_per_sm, c->tma};
+    const knc_tuning keep = {c->utr, c->fused, c->ctas_per_sm, c->uform};
     std::vector<knc_tuning> cands;
+    if (c->mesh.p.num_polar_zones > 1)
+        for (int sr : {8, 16, 32, 64}) cands.push_back({sr, 0, 0, KNC_UPDATE_STRIP});
     for (int tr : {4, 8, 16}) {
-        cands.push_back({tr, 0, 0, 0});
-        if (mixed(c)) cands.push_back({tr, 0, 0, 1});   // tensor-copy staging (used where every block allows it)
+        cands.push_back({tr, 0, 0, KNC_UPDATE_TILE});
+        // tensor-copy staging (used where every block allows it)
+        if (mixed(c)) cands.push_back({tr, 0, 0, KNC_UPDATE_TILE_TMA});
         if (!c->coop) continue;
         c->utr = tr;
         int per_sm = 1;
@@ -1888,9 +1945,9 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
         c->utr = t.tile_rows;
         c->fused = t.fused;
         c->ctas_per_sm = t.ctas_per_sm;
-        c->tma = t.tma;
+        c->uform = t.update_form;
         if ((r = rebuild_table(c))) break;
-        if (t.tma && !L(c).tma_ok) continue;
+        if (t.update_form == KNC_UPDATE_TILE_TMA && !L(c).tma_ok) continue;
         // the first stage reads buf[cur] and writes buf[1 - cur]: the state stays
         if ((r = run_stage(c, c->cur, 1 - c->cur, -1, 1.0, 0.0, c->time, dt))) break;
         CK(cudaEventRecord(e0, c->stream));
@@ -1919,7 +1976,7 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
     c->utr = best.tile_rows;
     c->fused = best.fused;
     c->ctas_per_sm = best.ctas_per_sm;
-    c->tma = best.tma;
+    c->uform = best.update_form;
     if (r) {
         c->failed = false;
         return r;

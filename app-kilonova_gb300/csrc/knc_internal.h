@@ -27,6 +27,8 @@ constexpr int TILE_R = 8;      // stage tile: rows (radial)
 constexpr int TILE_Q = 32;     // stage tile: columns (polar), one warp wide
 constexpr int TILE_THREADS = TILE_R * TILE_Q;
 constexpr int NFIELD = 5;
+constexpr int STRIP_OUT = TILE_Q - 4;   // output columns of a warp strip (2 halo lanes each side)
+constexpr int STRIP_WARPS = 4;          // independent strips per CTA
 
 struct DevBlock {
     double* buf[2];        // [5][nr][nq] state ping/pong
@@ -97,6 +99,8 @@ struct StageArgs {
     int32_t nutiles;
     int32_t utr;            // update tile rows: 4, 8 or 16
     int32_t tma;            // mixed update: stage tiles with tensor copies (tmaps valid)
+    const int4* strips;     // {slot, i0, j0, rows}: warp strips of the strip form, or null
+    int32_t nstrips;
     const void* tmaps;      // TmaMaps per slot (knc_tma.cuh), or null
     int32_t stage;          // stage counter for error ordering
     int32_t sel_in, sel_out, sel_base;   // state buffer selectors; sel_base < 0: no average

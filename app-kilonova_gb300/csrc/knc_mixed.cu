@@ -342,6 +342,13 @@ static void update_mixed(const StageArgs& a, cudaStream_t s) {
 }
 
 cudaError_t launch_update_mixed(const StageArgs& a, cudaStream_t s) {
+    if (a.strips) {
+        if (a.nstrips <= 0) return cudaSuccess;
+        const int want = (a.nstrips + STRIP_WARPS - 1) / STRIP_WARPS;
+        const int grid = std::min(want, resident_grid(update_strip_kernel<float, true>, STRIP_WARPS * 32, 0));
+        update_strip_kernel<float, true><<<grid, STRIP_WARPS * 32, 0, s>>>(a);
+        return cudaGetLastError();
+    }
     if (a.nutiles <= 0) return cudaSuccess;
     switch (a.utr) {
     case 4: update_mixed<4>(a, s); break;

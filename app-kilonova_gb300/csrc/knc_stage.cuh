@@ -317,6 +317,174 @@ __global__ void __launch_bounds__(update_threads<TR>(), MIXED ? (TR == 4 ? 6 : T
     }
 }
 
+// ---- warp strips ---------------------------------------------------------------
+// The same update as update_tile, organised per warp without shared memory or
+// CTA barriers: a warp owns a strip {slot, i0, j0, rows} of STRIP_OUT columns
+// j0..j0+STRIP_OUT-1 (lanes 2..STRIP_OUT+1; lanes 0, 1 and the last two hold
+// the polar halo) and marches down its rows. The radial window (rows i, i+1,
+// i+2 and the slope of row i) and the lower radial face flux stay in
+// registers; polar neighbours come through warp shuffles. Every face and
+// zone expression is the one update_tile evaluates, on the same values, so
+// the two forms give bit-identical states.
+
+template <class R>
+__device__ __forceinline__ void load_prim_row(const R* P, int64_t pn, int nq, int nr, int j, bool jin, int zrow,
+                                              R v[NFIELD]) {
+    const int prow = zrow + 2;   // padded row
+    const bool ok = jin && prow < nr + 4;
+    const int64_t off = ok ? (int64_t)prow * nq + j : 0;
+#pragma unroll
+    for (int q = 0; q < NFIELD; ++q) v[q] = ok ? P[q * pn + off] : R(0);
+}
+
+template <class R, bool MIXED>
+__device__ __forceinline__ void strip_face(const PhysT<R>& ph, const StageArgs& a, const DevBlock& B, int axis,
+                                           const R* pl, const R* pr, int i, int j, int nq, R cflux, R out[NFIELD]) {
+    if constexpr (MIXED) {
+        if (axis == 0) riemann_srhd_f32<0>(ph, pl, pr, pl[4], pr[4], out);
+        else riemann_srhd_f32<1>(ph, pl, pr, pl[4], pr[4], out);
+        const float2 A = axis == 0 ? df_mul(B.ar_r[i], B.ar_q[j]) : df_mul(B.aq_r[i], B.aq_q[j]);
+#pragma unroll
+        for (int q = 0; q < NFIELD; ++q) out[q] = df_scale(out[q], A);
+    } else {
+        riemann(ph, pl, pr, pl[4], pr[4], axis, out);
+        const R A = axis == 0 ? (R)B.ar[(int64_t)i * nq + j] : (R)B.aq[(int64_t)i * (nq + 1) + j];
+#pragma unroll
+        for (int q = 0; q < NFIELD; ++q) out[q] = out[q] * cflux * A;
+    }
+}
+
+template <class R, bool MIXED>
+__device__ __forceinline__ void update_strip(const StageArgs& a, const int4 it, const PhysT<R>& ph) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const DevBlock& B = a.blocks[it.x];
+    const int nr = B.nr, nq = B.nq, i0 = it.y, j0 = it.z, rows = it.w;
+    const int j = j0 - 2 + lane;
+    const bool jin = j >= 0 && j < nq;
+    const bool writes = lane >= 2 && lane < 2 + STRIP_OUT && jin;
+    const R* P = reinterpret_cast<const R*>(B.P);
+    const int64_t pn = (int64_t)(nr + 4) * nq;
+    const int64_t n = (int64_t)nr * nq;
+    const R th = ph.theta;
+    const R cflux = sizeof(R) == 4 ? (R)a.cflux_f : (R)a.cflux;
+    const R dt = sizeof(R) == 4 ? (R)a.dt_f : (R)a.dt;
+    const double* Uin = B.buf[a.sel_in];
+    double* Uout = B.buf[a.sel_out];
+    const double* U0 = a.sel_base >= 0 ? B.buf[a.sel_base] : nullptr;
+    const bool pedge = j <= 0 || j >= nq - 1;   // zero polar slope on the block's first and last column
+
+    // rows i0-2 .. i0+1, slopes of rows i0-1 and i0, the flux through face i0
+    R Pa[NFIELD], P0[NFIELD], P1[NFIELD], P2[NFIELD], g0[NFIELD], Flo[NFIELD];
+    load_prim_row(P, pn, nq, nr, j, jin, i0 - 2, Pa);
+    load_prim_row(P, pn, nq, nr, j, jin, i0 - 1, P2);   // P2 as scratch for row i0-1
+    load_prim_row(P, pn, nq, nr, j, jin, i0, P0);
+    load_prim_row(P, pn, nq, nr, j, jin, i0 + 1, P1);
+    {
+        R gm[NFIELD], pl[NFIELD], pr[NFIELD];
+#pragma unroll
+        for (int q = 0; q < NFIELD; ++q) {
+            gm[q] = plm_gradient(th, Pa[q], P2[q], P0[q]);
+            g0[q] = plm_gradient(th, P2[q], P0[q], P1[q]);
+            pl[q] = P2[q] + gm[q] * R(0.5);
+            pr[q] = P0[q] - g0[q] * R(0.5);
+        }
+#pragma unroll
+        for (int q = 0; q < NFIELD; ++q) Flo[q] = R(0);
+        if (i0 <= nr && j < nq && jin) strip_face<R, MIXED>(ph, a, B, 0, pl, pr, i0, j, nq, cflux, Flo);
+    }
+    load_prim_row(P, pn, nq, nr, j, jin, i0 + 2, P2);
+
+    // per-column factors
+    const int jc = jin ? j : 0;
+    for (int s = 0; s < rows; ++s) {
+        const int i = i0 + s;
+        // the next row, one step ahead
+        R Pn[NFIELD];
+        load_prim_row(P, pn, nq, nr, j, jin, i + 3, Pn);
+        // ---- polar: slopes of row i, the face j - 1 | j, its right neighbour's
+        R gq[NFIELD], plq[NFIELD], prq[NFIELD], Fq[NFIELD], Fq1[NFIELD];
+#pragma unroll
+        for (int q = 0; q < NFIELD; ++q) {
+            const R left = __shfl_up_sync(full, P0[q], 1);
+            const R right = __shfl_down_sync(full, P0[q], 1);
+            gq[q] = pedge ? R(0) : plm_gradient(th, left, P0[q], right);
+            plq[q] = __shfl_up_sync(full, P0[q] + gq[q] * R(0.5), 1);
+            prq[q] = P0[q] - gq[q] * R(0.5);
+            Fq[q] = R(0);
+        }
+        if (lane > 0 && i < nr && j > 0 && j < nq) strip_face<R, MIXED>(ph, a, B, 1, plq, prq, i, j, nq, cflux, Fq);
+#pragma unroll
+        for (int q = 0; q < NFIELD; ++q) Fq1[q] = __shfl_down_sync(full, Fq[q], 1);
+        // ---- radial: slope of row i+1, the face i+1
+        R g1[NFIELD], plr[NFIELD], prr[NFIELD], Fhi[NFIELD];
+#pragma unroll
+        for (int q = 0; q < NFIELD; ++q) {
+            g1[q] = plm_gradient(th, P0[q], P1[q], P2[q]);
+            plr[q] = P0[q] + g0[q] * R(0.5);
+            prr[q] = P1[q] - g1[q] * R(0.5);
+            Fhi[q] = R(0);
+        }
+        if (i + 1 <= nr && jin) strip_face<R, MIXED>(ph, a, B, 0, plr, prr, i + 1, j, nq, cflux, Fhi);
+        // ---- sources, conserved update, RK average of zone (i, j)
+        if (writes) {
+            const int64_t z = (int64_t)i * nq + jc;
+            R src[4];
+            R dV = R(0);
+            float2 cdV = make_float2(0.f, 0.f);
+            if constexpr (MIXED) {
+                sources_srhd_f32(ph, P0, B.rc32[i], B.cot32[jc], src);
+                cdV = df_mul(B.dv_r[i], B.dv_q[jc]);
+            } else {
+                sources(ph, P0, (R)B.rc[i], (R)B.cot[jc], src);
+                dV = (R)B.dv[z];
+            }
+            double res[NFIELD];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                R sc;
+                if constexpr (MIXED) sc = df_scale(src[q], cdV);
+                else sc = src[q] * cflux * dV;
+                const R du = (sc - (Fhi[q] - Flo[q]) - (Fq1[q] - Fq[q])) * dt;
+                res[q] = Uin[q * n + z] + (MIXED ? f2d((float)du) : (double)du);
+            }
+            {
+                const R ds = ((Fhi[4] - Flo[4]) + (Fq1[4] - Fq[4])) * -dt;
+                res[4] = Uin[4 * n + z] + (MIXED ? f2d((float)ds) : (double)ds);
+            }
+            if (U0) {
+                if (MIXED && a.avg_half) {
+#pragma unroll
+                    for (int q = 0; q < NFIELD; ++q) res[q] = half_exact(res[q] + U0[q * n + z]);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < NFIELD; ++q) res[q] = res[q] * a.w1 + U0[q * n + z] * a.bf;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < NFIELD; ++q) Uout[q * n + z] = res[q];
+        }
+        // ---- advance the window
+#pragma unroll
+        for (int q = 0; q < NFIELD; ++q) {
+            Flo[q] = Fhi[q];
+            g0[q] = g1[q];
+            P0[q] = P1[q];
+            P1[q] = P2[q];
+            P2[q] = Pn[q];
+        }
+    }
+}
+
+// Strips (a.strips) in a grid-stride loop over warps.
+template <class R, bool MIXED>
+__global__ void __launch_bounds__(STRIP_WARPS * 32, MIXED ? 4 : 2) update_strip_kernel(StageArgs a) {
+    if (*(volatile unsigned long long*)&a.status->err_key != NO_ERROR) return;
+    const PhysT<R> ph = make_phys<R>(a);
+    const int warp = blockIdx.x * STRIP_WARPS + (threadIdx.x >> 5);
+    for (int k = warp; k < a.nstrips; k += gridDim.x * STRIP_WARPS) update_strip<R, MIXED>(a, a.strips[k], ph);
+}
+
 // Block-wide reduction helpers (warp shuffles, then one atomic per warp).
 __device__ __forceinline__ void warp_reduce_stats(DevStatus* st, unsigned long long zones,
                                                   unsigned long long it64, unsigned long long it32,

@@ -52,6 +52,9 @@ KNC_KERNEL_GHOST = 0
 KNC_KERNEL_C2P = 1
 KNC_KERNEL_UPDATE = 2
 KNC_KERNEL_FUSED = 3
+KNC_UPDATE_TILE = 0
+KNC_UPDATE_TILE_TMA = 1
+KNC_UPDATE_STRIP = 2
 KNC_KERNEL_KINDS = 4
 
 KNC_MLP_HIDDEN = 64
@@ -127,7 +130,7 @@ class Error(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("tile_rows", C.c_int32), ("fused", C.c_int32), ("ctas_per_sm", C.c_int32),
-                ("tma", C.c_int32)]
+                ("update_form", C.c_int32)]
 
 
 class MlpTrainParams(C.Structure):

@@ -105,16 +105,20 @@ class Solver:
     def set_batched(self, graph: bool):
         self._check(self.lib.knc_set_batched(self.h, int(bool(graph))), "set_batched")
 
-    def set_tuning(self, tile_rows: int = 8, fused: bool = False, ctas_per_sm: int = 0, tma: bool = False):
+    def set_tuning(self, tile_rows: int = 8, fused: bool = False, ctas_per_sm: int = 0, tma: bool = False,
+                   strip: bool = False):
+        """Launch shape: update tiles of tile_rows rows (tma: staged by tensor
+        copies), warp strips of tile_rows rows (strip), or the fused stage."""
+        form = abi.KNC_UPDATE_STRIP if strip else abi.KNC_UPDATE_TILE_TMA if tma else abi.KNC_UPDATE_TILE
         t = abi.Tuning(tile_rows=int(tile_rows), fused=int(bool(fused)), ctas_per_sm=int(ctas_per_sm),
-                       tma=int(bool(tma)))
+                       update_form=form)
         self._check(self.lib.knc_set_tuning(self.h, C.byref(t)), "set_tuning")
 
     def tuning(self) -> dict:
         t = abi.Tuning()
         self._check(self.lib.knc_get_tuning(self.h, C.byref(t)), "get_tuning")
         return {"tile_rows": t.tile_rows, "fused": bool(t.fused), "ctas_per_sm": t.ctas_per_sm,
-                "tma": bool(t.tma)}
+                "tma": t.update_form == abi.KNC_UPDATE_TILE_TMA, "strip": t.update_form == abi.KNC_UPDATE_STRIP}
 
     def autotune(self, reps: int = 5):
         """Time every launch shape on the live state, keep the fastest; returns
@@ -123,7 +127,7 @@ class Solver:
         ms = C.c_double()
         self._check(self.lib.knc_autotune(self.h, int(reps), C.byref(t), C.byref(ms)), "autotune")
         return {"tile_rows": t.tile_rows, "fused": bool(t.fused), "ctas_per_sm": t.ctas_per_sm,
-                "tma": bool(t.tma)}, ms.value
+                "tma": t.update_form == abi.KNC_UPDATE_TILE_TMA, "strip": t.update_form == abi.KNC_UPDATE_STRIP}, ms.value
 
     def zone_updates(self) -> int:
         n = C.c_int64()

@@ -233,26 +233,32 @@ int knc_set_batched(knc_ctx* ctx, int32_t graph);
 /* Launch shape of a stage (no counterpart in the reference, whose stage is a
  * Rayon/Tokio task per block, src/scheme.rs:16-173).
  *   tile_rows    radial rows of an update tile (4, 8 or 16; 32 polar columns;
- *                a tile runs on (tile_rows + 1) warps)
+ *                a tile runs on (tile_rows + 1) warps), or of a warp strip
+ *                (4 to 64)
  *   fused        0: a stage is four launches (ghost rows, recovery, remaps,
  *                update); 1: one persistent cooperative launch whose phases
  *                are separated by bounded grid barriers (bit-identical result)
  *   ctas_per_sm  fused grid = ctas_per_sm x SMs CTAs (0: the occupancy bound;
  *                larger values are clamped to it)
- *   tma          mixed precision, separate form: the update stages each tile
- *                (primitives with halo, U_in, U_base) with tensor copies into
- *                double-buffered shared memory, one tile ahead; used when
- *                every block has nq % 4 == 0, nq >= 40 and nr >= tile_rows */
+ *   update_form  separate form only: KNC_UPDATE_TILE, or KNC_UPDATE_TILE_TMA
+ *                (mixed precision: each tile's primitives with halo, U_in and
+ *                U_base staged by tensor copies into double-buffered shared
+ *                memory, one tile ahead; used when every block has
+ *                nq % 4 == 0, nq >= 40 and nr >= tile_rows), or
+ *                KNC_UPDATE_STRIP (one warp per strip of 28 polar columns
+ *                marching down tile_rows radial rows, no shared memory; needs
+ *                num_polar_zones > 1). All forms give bit-identical states. */
+enum { KNC_UPDATE_TILE = 0, KNC_UPDATE_TILE_TMA = 1, KNC_UPDATE_STRIP = 2 };
 typedef struct knc_tuning {
     int32_t tile_rows;
     int32_t fused;
     int32_t ctas_per_sm;
-    int32_t tma;
+    int32_t update_form;
 } knc_tuning;
 int knc_set_tuning(knc_ctx* ctx, const knc_tuning* tuning);
 int knc_get_tuning(const knc_ctx* ctx, knc_tuning* tuning);
 /* Autotuner: times every candidate shape (tile rows x separate / fused x CTAs
- * per SM x tensor-copy staging) with `reps` first-stage launches each on the live state (they write
+ * per SM x update form) with `reps` first-stage launches each on the live state (they write
  * only the scratch buffer and primitives, so the state is unchanged), keeps
  * the fastest and returns it with its time per stage (either output may be
  * NULL). */

@@ -14,6 +14,7 @@ from helpers import make_pair, zone_relative_errors
 pytestmark = pytest.mark.gpu
 
 SHAPES = [(4, False), (8, False), (16, False), (4, True), (8, True), (16, True)]
+STRIPS = [4, 8, 16, 64]
 
 
 def _same(a, b):
@@ -114,6 +115,12 @@ def test_tuning_validation():
         g.set_tuning(tile_rows=12)
     with pytest.raises(knc.abi.KncError):
         g.set_tuning(tile_rows=8, ctas_per_sm=-1)
+    with pytest.raises(knc.abi.KncError):
+        g.set_tuning(tile_rows=32)            # tiles: 4, 8 or 16 rows
+    with pytest.raises(knc.abi.KncError):
+        g.set_tuning(tile_rows=128, strip=True)
+    g.set_tuning(tile_rows=32, strip=True)
+    assert g.tuning()["strip"]
 
 
 def test_fused_counts_one_launch_per_stage():
@@ -158,6 +165,63 @@ def test_mixed_tma_uneven_moving():
     g = knc.build_solver(w)
     g.set_precision(knc.abi.KNC_PRECISION_MIXED)
     g.set_tuning(tile_rows=8, tma=True)
+    g.set_batched(True)
+    for _ in range(2):
+        ref.advance(4)
+        g.advance(4)
+    assert g.block_indexes() == ref.block_indexes()
+    assert _same(g.state(), ref.state())
+
+
+@pytest.mark.parametrize("rows", STRIPS)
+def test_fp64_strips_match_oracle(rows):
+    from knc import workloads
+    w = workloads.wind_small()
+    g, o = make_pair(w)
+    g.set_tuning(tile_rows=rows, strip=True)
+    for _ in range(2):
+        g.advance(2)
+        o.advance(2)
+    assert _same(g.state(), o.state())
+
+
+def test_fp64_strips_uneven_moving_match_oracle():
+    from knc import workloads
+    w = workloads.uneven_small(order="RK3", riemann="HLLC")
+    g, o = make_pair(w)
+    g.set_tuning(tile_rows=16, strip=True)
+    g.set_batched(True)
+    for _ in range(2):
+        g.advance(5)
+        o.advance(5)
+    assert g.block_indexes() == o.block_indexes()
+    assert _same(g.state(), o.state())
+
+
+@pytest.mark.parametrize("rows", STRIPS)
+def test_mixed_strips_match_tiles(rows):
+    import knc
+    from knc import workloads
+    w = workloads.wind_small()
+    ref = _mixed(w, 8, False, False)
+    g, _ = make_pair(w, gpu=True)
+    g.set_precision(knc.abi.KNC_PRECISION_MIXED)
+    g.set_tuning(tile_rows=rows, strip=True)
+    g.set_batched(True)
+    for _ in range(2):
+        g.advance(3)
+    assert _same(g.state(), ref.state())
+
+
+def test_mixed_strips_uneven_moving():
+    import knc
+    from knc import workloads
+    w = workloads.uneven()
+    ref = knc.build_solver(w)
+    ref.set_precision(knc.abi.KNC_PRECISION_MIXED)
+    g = knc.build_solver(w)
+    g.set_precision(knc.abi.KNC_PRECISION_MIXED)
+    g.set_tuning(tile_rows=32, strip=True)
     g.set_batched(True)
     for _ in range(2):
         ref.advance(4)
