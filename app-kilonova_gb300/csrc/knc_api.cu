@@ -839,6 +839,7 @@ StageArgs base_args(knc_ctx* c) {
     a.tmaps = L(c).tma_ok ? L(c).d_tmaps : nullptr;
     a.strips = c->uform == KNC_UPDATE_STRIP ? L(c).d_strips : nullptr;
     a.nstrips = c->uform == KNC_UPDATE_STRIP ? L(c).nstrips : 0;
+    a.strip_ctas = c->ctas_per_sm >= 4 && c->ctas_per_sm <= 6 ? c->ctas_per_sm : 4;
     a.srhd = c->hp.system == KNC_SYSTEM_RELATIVISTIC;
     a.hllc = c->hp.riemann_solver == KNC_RIEMANN_HLLC;
     a.one_dimensional = c->mesh.p.num_polar_zones == 1;
@@ -1921,7 +1922,9 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
     const knc_tuning keep = {c->utr, c->fused, c->ctas_per_sm, c->uform};
     std::vector<knc_tuning> cands;
     if (c->mesh.p.num_polar_zones > 1)
-        for (int sr : {8, 16, 32, 64}) cands.push_back({sr, 0, 0, KNC_UPDATE_STRIP});
+        for (int sr : {8, 16, 32, 64})
+            for (int mb : {4, 5, 6})
+                if (mixed(c) || mb == 4) cands.push_back({sr, 0, mb, KNC_UPDATE_STRIP});
     for (int tr : {4, 8, 16}) {
         cands.push_back({tr, 0, 0, KNC_UPDATE_TILE});
         // tensor-copy staging (used where every block allows it)

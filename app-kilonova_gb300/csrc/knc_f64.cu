@@ -248,7 +248,7 @@ static void update_f64(const StageArgs& a, cudaStream_t s) {
 cudaError_t launch_update_f64(const StageArgs& a, cudaStream_t s) {
     if (a.strips) {
         if (a.nstrips <= 0) return cudaSuccess;
-        update_strip_kernel<double, false><<<(a.nstrips + STRIP_WARPS - 1) / STRIP_WARPS, STRIP_WARPS * 32, 0, s>>>(a);
+        update_strip_kernel<double, false, 2><<<(a.nstrips + STRIP_WARPS - 1) / STRIP_WARPS, STRIP_WARPS * 32, 0, s>>>(a);
         return cudaGetLastError();
     }
     if (a.nutiles <= 0) return cudaSuccess;

@@ -101,6 +101,7 @@ struct StageArgs {
     int32_t tma;            // mixed update: stage tiles with tensor copies (tmaps valid)
     const int4* strips;     // {slot, i0, j0, rows}: warp strips of the strip form, or null
     int32_t nstrips;
+    int32_t strip_ctas;     // strip form: CTAs per SM the kernel is built for (4, 5 or 6)
     const void* tmaps;      // TmaMaps per slot (knc_tma.cuh), or null
     int32_t stage;          // stage counter for error ordering
     int32_t sel_in, sel_out, sel_base;   // state buffer selectors; sel_base < 0: no average

@@ -72,6 +72,8 @@ static __device__ __noinline__ float mlp_guess_call(const MlpWeights& W, __nv_bf
     return mlp_warp_infer(W, act, x);
 }
 
+constexpr int TMA_WAIT_LIMIT = 1 << 22;   // mbarrier polls before a copy counts as lost
+
 // Recovery of one zone; every thread of a warp calls zone() together (the
 // learned guess is a warp-wide inference).
 template <bool MLP>
@@ -263,8 +265,6 @@ struct TmaSmem {
     static constexpr size_t bytes = 128 + 2 * BUF + WORK + 16;   // alignment slack, buffers, work, 2 mbarriers
 };
 
-constexpr int TMA_WAIT_LIMIT = 1 << 22;
-
 template <int TR>
 __global__ void __launch_bounds__(update_threads<TR>(), 1) update_tma_kernel(StageArgs a) {
     using L = TmaSmem<TR>;
@@ -341,12 +341,21 @@ static void update_mixed(const StageArgs& a, cudaStream_t s) {
     update_kernel<float, true, TR><<<grid, update_threads<TR>(), smem, s>>>(a);
 }
 
+template <int MB>
+static void update_strips(const StageArgs& a, cudaStream_t s) {
+    const int want = (a.nstrips + STRIP_WARPS - 1) / STRIP_WARPS;
+    const int grid = std::min(want, resident_grid(update_strip_kernel<float, true, MB>, STRIP_WARPS * 32, 0));
+    update_strip_kernel<float, true, MB><<<grid, STRIP_WARPS * 32, 0, s>>>(a);
+}
+
 cudaError_t launch_update_mixed(const StageArgs& a, cudaStream_t s) {
     if (a.strips) {
         if (a.nstrips <= 0) return cudaSuccess;
-        const int want = (a.nstrips + STRIP_WARPS - 1) / STRIP_WARPS;
-        const int grid = std::min(want, resident_grid(update_strip_kernel<float, true>, STRIP_WARPS * 32, 0));
-        update_strip_kernel<float, true><<<grid, STRIP_WARPS * 32, 0, s>>>(a);
+        switch (a.strip_ctas) {
+        case 5: update_strips<5>(a, s); break;
+        case 6: update_strips<6>(a, s); break;
+        default: update_strips<4>(a, s);
+        }
         return cudaGetLastError();
     }
     if (a.nutiles <= 0) return cudaSuccess;

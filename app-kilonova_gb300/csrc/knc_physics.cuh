@@ -65,6 +65,21 @@ __device__ __forceinline__ R plm_gradient(R theta, R a, R b, R c) {
     return R(0);
 }
 
+// FP32 generalised minmod without branches (the mixed stage): with
+// x, y, z as in plm_gradient, y has the sign of x and z whenever those two
+// agree (c - a = (c - b) + (b - a)), so the result is min(|x|, |y|, |z|) with
+// the sign of x when x and z are non-zero and of one sign, else 0. The one
+// difference from plm_gradient<float> is the sign of a zero result when
+// 0.5 (c - a) underflows, which no sum with it can see.
+__device__ __forceinline__ float plm_gradient_f32(float theta, float a, float b, float c) {
+    const float x = theta * (b - a);
+    const float y = 0.5f * (c - a);
+    const float z = theta * (c - b);
+    const float m = fminf(fabsf(x), fminf(fabsf(y), fabsf(z)));
+    const bool agree = ((__float_as_uint(x) ^ __float_as_uint(z)) & 0x80000000u) == 0u && x != 0.0f && z != 0.0f;
+    return agree ? copysignf(m, x) : 0.0f;
+}
+
 // One side of an interface: conserved state, normal flux, outer wave speeds,
 // the passive scalar's conserved density (s W) and flux (s u_n).
 template <class R>

@@ -80,6 +80,14 @@ __device__ __forceinline__ PhysT<R> make_phys(const StageArgs& a) {
 // already in shared memory as tensor-copy boxes: boxP [5][TR+4][TQ+8] from
 // padded row i0 and column j0 - 4 (zero outside the block), boxU / boxU0
 // [5][TR][TQ] from row i0, column j0 (boxU0 only with an RK average).
+// The slope limiter of a stage: the reference's form in FP64, the
+// branch-free form in the mixed stage.
+template <class R, bool MIXED>
+__device__ __forceinline__ R stage_plm(R theta, R a, R b, R c) {
+    if constexpr (MIXED) return plm_gradient_f32(theta, a, b, c);
+    else return plm_gradient(theta, a, b, c);
+}
+
 template <class R, bool MIXED, int TR_, bool BOX = false>
 __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, unsigned char* smem_raw,
                                             const R* boxP = nullptr, const double* boxU = nullptr,
@@ -144,7 +152,7 @@ __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, un
                 for (int q = 0; q < NFIELD; ++q) {
                     const R* col = sPc + (q * PR) * PQS + c + 2;
                     sGr[(q * (TR + 2) + g) * TQ + c] =
-                        plm_gradient(th, col[g * PQS], col[(g + 1) * PQS], col[(g + 2) * PQS]);
+                        stage_plm<R, MIXED>(th, col[g * PQS], col[(g + 1) * PQS], col[(g + 2) * PQS]);
                 }
             } else {
                 const int kk = k - NGRZ;
@@ -154,7 +162,7 @@ __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, un
 #pragma unroll
                 for (int q = 0; q < NFIELD; ++q) {
                     const R* row = sPc + (q * PR + r + 2) * PQS + c;
-                    sGq[(q * TR + r) * (TQ + 2) + c] = edge ? R(0) : plm_gradient(th, row[0], row[1], row[2]);
+                    sGq[(q * TR + r) * (TQ + 2) + c] = edge ? R(0) : stage_plm<R, MIXED>(th, row[0], row[1], row[2]);
                 }
             }
         }
@@ -384,8 +392,8 @@ __device__ __forceinline__ void update_strip(const StageArgs& a, const int4 it, 
         R gm[NFIELD], pl[NFIELD], pr[NFIELD];
 #pragma unroll
         for (int q = 0; q < NFIELD; ++q) {
-            gm[q] = plm_gradient(th, Pa[q], P2[q], P0[q]);
-            g0[q] = plm_gradient(th, P2[q], P0[q], P1[q]);
+            gm[q] = stage_plm<R, MIXED>(th, Pa[q], P2[q], P0[q]);
+            g0[q] = stage_plm<R, MIXED>(th, P2[q], P0[q], P1[q]);
             pl[q] = P2[q] + gm[q] * R(0.5);
             pr[q] = P0[q] - g0[q] * R(0.5);
         }
@@ -408,7 +416,7 @@ __device__ __forceinline__ void update_strip(const StageArgs& a, const int4 it, 
         for (int q = 0; q < NFIELD; ++q) {
             const R left = __shfl_up_sync(full, P0[q], 1);
             const R right = __shfl_down_sync(full, P0[q], 1);
-            gq[q] = pedge ? R(0) : plm_gradient(th, left, P0[q], right);
+            gq[q] = pedge ? R(0) : stage_plm<R, MIXED>(th, left, P0[q], right);
             plq[q] = __shfl_up_sync(full, P0[q] + gq[q] * R(0.5), 1);
             prq[q] = P0[q] - gq[q] * R(0.5);
             Fq[q] = R(0);
@@ -420,7 +428,7 @@ __device__ __forceinline__ void update_strip(const StageArgs& a, const int4 it, 
         R g1[NFIELD], plr[NFIELD], prr[NFIELD], Fhi[NFIELD];
 #pragma unroll
         for (int q = 0; q < NFIELD; ++q) {
-            g1[q] = plm_gradient(th, P0[q], P1[q], P2[q]);
+            g1[q] = stage_plm<R, MIXED>(th, P0[q], P1[q], P2[q]);
             plr[q] = P0[q] + g0[q] * R(0.5);
             prr[q] = P1[q] - g1[q] * R(0.5);
             Fhi[q] = R(0);
@@ -476,9 +484,11 @@ __device__ __forceinline__ void update_strip(const StageArgs& a, const int4 it, 
     }
 }
 
-// Strips (a.strips) in a grid-stride loop over warps.
-template <class R, bool MIXED>
-__global__ void __launch_bounds__(STRIP_WARPS * 32, MIXED ? 4 : 2) update_strip_kernel(StageArgs a) {
+// Strips (a.strips) in a grid-stride loop over warps; MB = resident CTAs per
+// SM the register allocation is sized for (a tuning choice: more warps
+// against fewer registers).
+template <class R, bool MIXED, int MB>
+__global__ void __launch_bounds__(STRIP_WARPS * 32, MB) update_strip_kernel(StageArgs a) {
     if (*(volatile unsigned long long*)&a.status->err_key != NO_ERROR) return;
     const PhysT<R> ph = make_phys<R>(a);
     const int warp = blockIdx.x * STRIP_WARPS + (threadIdx.x >> 5);

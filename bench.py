@@ -410,7 +410,7 @@ def run_only(args):
     w = workloads.WORKLOADS[args.workload]()
     s = knc.build_solver(w)
     if args.tile_rows:
-        s.set_tuning(tile_rows=args.tile_rows, fused=args.fused, tma=args.tma)
+        s.set_tuning(tile_rows=args.tile_rows, fused=args.fused, tma=args.tma, strip=args.strip)
     if args.only == "mixed":
         s.set_precision(abi.KNC_PRECISION_MIXED)
         s.set_mixed_w_split(args.w_split)
@@ -448,6 +448,7 @@ def main():
     ap.add_argument("--tile-rows", type=int, default=0, help="launch shape of --only runs (0: default)")
     ap.add_argument("--fused", action="store_true")
     ap.add_argument("--tma", action="store_true")
+    ap.add_argument("--strip", action="store_true")
     ap.add_argument("--only", choices=["fp64", "mixed"], default=None,
                     help="run one path alone (profiler captures)")
     args = ap.parse_args()

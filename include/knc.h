@@ -239,7 +239,9 @@ int knc_set_batched(knc_ctx* ctx, int32_t graph);
  *                update); 1: one persistent cooperative launch whose phases
  *                are separated by bounded grid barriers (bit-identical result)
  *   ctas_per_sm  fused grid = ctas_per_sm x SMs CTAs (0: the occupancy bound;
- *                larger values are clamped to it)
+ *                larger values are clamped to it); mixed warp strips: the
+ *                CTAs per SM the strip kernel's registers are sized for
+ *                (4, 5 or 6; other values: 4)
  *   update_form  separate form only: KNC_UPDATE_TILE, or KNC_UPDATE_TILE_TMA
  *                (mixed precision: each tile's primitives with halo, U_in and
  *                U_base staged by tensor copies into double-buffered shared
