@@ -1922,7 +1922,7 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
     const knc_tuning keep = {c->utr, c->fused, c->ctas_per_sm, c->uform};
     std::vector<knc_tuning> cands;
     if (c->mesh.p.num_polar_zones > 1)
-        for (int sr : {8, 16, 32, 64})
+        for (int sr : {4, 8, 16, 32, 64})
             for (int mb : {4, 5, 6})
                 if (mixed(c) || mb == 4) cands.push_back({sr, 0, mb, KNC_UPDATE_STRIP});
     for (int tr : {4, 8, 16}) {

@@ -39,9 +39,16 @@ sys.path.insert(0, str(ROOT / "app-kilonova_gb300"))
 
 METRIC = "zone-updates/s per GB300: mixed+learned vs plain FP64 GPU at L1<1e-6; HBM %"
 UNIT = "zone-updates/s"
-# algorithmic HBM bytes per zone-update of an RK2 step: 5 FP64 fields,
-# stage 1 reads U and writes U1 (80 B), stage 2 reads U1 and U0 and writes (120 B)
-ALG_BYTES_PER_ZONE_UPDATE = 200.0
+# Algorithmic HBM bytes per zone of the mixed RK2 step (5 fields; state FP64,
+# primitives FP32):
+#   recovery launch  reads U (40 B), writes P (20 B)                 60 B
+#   update, stage 1  reads P (20 B) and U (40 B), writes U1 (40 B)  100 B
+#   update, stage 2  also reads the RK base U0 (40 B)               140 B
+# so one update launch averages 120 B per zone and a whole step moves
+# 2 x 60 + 100 + 140 = 360 B per zone-update.
+ALG_BYTES_UPDATE_LAUNCH = 120.0
+ALG_BYTES_RECOVERY_LAUNCH = 60.0
+ALG_BYTES_PER_ZONE_UPDATE = 360.0
 
 
 def load_peaks():
@@ -297,6 +304,7 @@ def run_knc(args):
 
     # ---- same path without the graph, kernels timed with events (roofline)
     prof = make(True, True, False)
+    prof.set_tuning(**tuning)
     for _ in range(args.warmup):
         prof.advance(1)
     prof.set_profiling(True)
@@ -306,9 +314,9 @@ def run_knc(args):
     prof.close()
     dom = max(kt, key=lambda k: kt[k][0])
     dom_ms = kt[dom][0] / max(kt[dom][1], 1)
-    # one launch of a stage kernel processes one stage of every zone: half of
-    # an RK2 zone-update's algorithmic bytes
-    alg_bytes = ALG_BYTES_PER_ZONE_UPDATE * zones / 2.0
+    # one launch processes one stage of every zone
+    per_zone = {"update": ALG_BYTES_UPDATE_LAUNCH, "c2p": ALG_BYTES_RECOVERY_LAUNCH}.get(dom, 0.0)
+    alg_bytes = per_zone * zones
     achieved = alg_bytes / (dom_ms * 1e-3) / 1e9
     traffic = profiled_traffic(dom)
 
@@ -388,7 +396,11 @@ def run_knc(args):
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                          "peak_source": peak_src, "avg_launch_ms": dom_ms,
-                         "kernel_ms": {k: v[0] / max(v[1], 1) for k, v in kt.items()}},
+                         "kernel_ms": {k: v[0] / max(v[1], 1) for k, v in kt.items()},
+                         "alg_bytes_per_zone_launch": per_zone,
+                         "step": {"alg_bytes_per_zone_update": ALG_BYTES_PER_ZONE_UPDATE,
+                                  "achieved": ALG_BYTES_PER_ZONE_UPDATE * value / 1e9,
+                                  "frac": ALG_BYTES_PER_ZONE_UPDATE * value / 1e9 / hbm_peak}},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d},
             "gpu_launches": launches,
             "clocks": clk,
