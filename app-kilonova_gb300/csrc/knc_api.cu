@@ -551,7 +551,7 @@ int rebuild_table(knc_ctx* c) {
     std::vector<int4> tiles, utiles, chunks, strips;
     std::vector<TmaMaps> maps(nb);
     bool tma_ok = nb > 0;
-    const int nt = stage_threads(c->utr);
+    const int nt = stage_threads(fused_tr(c->utr));
     L(c).slot_index.clear();
     int slot = 0;
     int64_t zoff = 0;
@@ -889,10 +889,11 @@ int fused_grid(knc_ctx* c) {
     if (e != cudaSuccess || per_sm < 1) per_sm = 1;
     if (c->ctas_per_sm > 0 && c->ctas_per_sm < per_sm) per_sm = c->ctas_per_sm;
     const Layout& l = L(c);
-    const int nt = stage_threads(c->utr);
+    const int nt = stage_threads(fused_tr(c->utr));
     const int need_a = (int)(2 * l.nq_edge[0] + nt - 1) / nt + (int)(2 * l.nq_edge[1] + nt - 1) / nt + l.nchunks;
     const int need_b = (int)(((int64_t)l.nremap * 2 * l.max_nq + nt - 1) / nt);
-    const int need = std::max(std::max(need_a, need_b), std::max(l.nutiles, 1));
+    const int need_c = l.uform == KNC_UPDATE_STRIP ? (l.nstrips + nt / 32 - 1) / (nt / 32) : l.nutiles;
+    const int need = std::max(std::max(need_a, need_b), std::max(need_c, 1));
     return std::min(per_sm * c->sms, need);
 }
 
@@ -1883,7 +1884,7 @@ int knc_set_tuning(knc_ctx* c, const knc_tuning* t) {
     if (!c || !t) return KNC_ERR_INVALID_ARGUMENT;
     if (t->update_form < KNC_UPDATE_TILE || t->update_form > KNC_UPDATE_STRIP)
         return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "unknown update form %d", t->update_form);
-    const bool strip = t->update_form == KNC_UPDATE_STRIP && !t->fused;
+    const bool strip = t->update_form == KNC_UPDATE_STRIP;
     if (strip ? (t->tile_rows < 4 || t->tile_rows > 64)
               : (t->tile_rows != 4 && t->tile_rows != 8 && t->tile_rows != 16))
         return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "tile_rows must be 4, 8 or 16 (tiles) or 4..64 (strips)");
@@ -1895,7 +1896,8 @@ int knc_set_tuning(knc_ctx* c, const knc_tuning* t) {
     c->utr = t->tile_rows;
     c->fused = t->fused ? 1 : 0;
     c->ctas_per_sm = t->ctas_per_sm;
-    c->uform = t->fused ? KNC_UPDATE_TILE : t->update_form;
+    // the fused stage stages its tiles itself (no tensor-copy form)
+    c->uform = t->fused && t->update_form == KNC_UPDATE_TILE_TMA ? KNC_UPDATE_TILE : t->update_form;
     return KNC_OK;
 }
 
@@ -1935,7 +1937,16 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
         const bool mlp = c->guess == KNC_GUESS_MLP && c->d_mlp;
         CK(mixed(c) ? fused_max_ctas_mixed(mlp, tr, &per_sm)
                     : fused_max_ctas_f64(mlp && c->hp.system == KNC_SYSTEM_RELATIVISTIC, tr, &per_sm));
-        for (int k = 1; k <= per_sm && k <= 8; ++k) cands.push_back({tr, 1, k, 0});
+        for (int k = 1; k <= per_sm && k <= 8; ++k) cands.push_back({tr, 1, k, KNC_UPDATE_TILE});
+    }
+    if (c->coop && c->mesh.p.num_polar_zones > 1) {
+        // the fused stage with warp strips in its update phase (CTAs of 9 warps)
+        int per_sm = 1;
+        const bool mlp = c->guess == KNC_GUESS_MLP && c->d_mlp;
+        CK(mixed(c) ? fused_max_ctas_mixed(mlp, 8, &per_sm)
+                    : fused_max_ctas_f64(mlp && c->hp.system == KNC_SYSTEM_RELATIVISTIC, 8, &per_sm));
+        for (int sr : {8, 16, 32})
+            for (int k = 1; k <= per_sm && k <= 8; ++k) cands.push_back({sr, 1, k, KNC_UPDATE_STRIP});
     }
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));

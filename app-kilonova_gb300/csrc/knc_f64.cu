@@ -278,7 +278,7 @@ static cudaError_t fused_f64(const StageArgs& a, const GhostArgs& g, const Fused
 cudaError_t launch_stage_fused_f64(const StageArgs& a, const GhostArgs& g, const FusedArgs& f, int grid,
                                    cudaStream_t s) {
     const bool mlp = a.mlp && a.srhd;
-    switch (a.utr) {
+    switch (fused_tr(a.utr)) {
     case 4: return mlp ? fused_f64<4, true>(a, g, f, grid, s) : fused_f64<4, false>(a, g, f, grid, s);
     case 16: return mlp ? fused_f64<16, true>(a, g, f, grid, s) : fused_f64<16, false>(a, g, f, grid, s);
     default: return mlp ? fused_f64<8, true>(a, g, f, grid, s) : fused_f64<8, false>(a, g, f, grid, s);
@@ -292,7 +292,7 @@ static cudaError_t fused_ctas_f64(int* n) {
 }
 
 cudaError_t fused_max_ctas_f64(bool mlp, int utr, int* n) {
-    switch (utr) {
+    switch (fused_tr(utr)) {
     case 4: return mlp ? fused_ctas_f64<4, true>(n) : fused_ctas_f64<4, false>(n);
     case 16: return mlp ? fused_ctas_f64<16, true>(n) : fused_ctas_f64<16, false>(n);
     default: return mlp ? fused_ctas_f64<8, true>(n) : fused_ctas_f64<8, false>(n);

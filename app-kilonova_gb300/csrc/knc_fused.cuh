@@ -11,7 +11,7 @@
 //   -- barrier --
 //   B  halo remaps across polar-resolution changes (uneven blocks only);
 //   -- barrier (only with remaps) --
-//   C  the flux / source / update / RK-average tiles.
+//   C  the flux / source / update / RK-average tiles (or warp strips).
 // Work in each phase is a grid-stride loop over a device list, so one launch
 // shape covers every block set of a moving mesh. Because the phases call the
 // very functions the separate kernels call, the two forms give bit-identical
@@ -132,9 +132,17 @@ __device__ __forceinline__ void stage_fused_body(const StageArgs& a, const Ghost
                      *(volatile int32_t*)&a.status->bar_abort == 0;
     __syncthreads();
     if (run_update) {
-        for (int tile = blockIdx.x; tile < a.nutiles; tile += gridDim.x) {
-            update_tile<R, MIXED, TR>(a, a.utiles[tile], smem_raw);
-            __syncthreads();
+        if (a.strips) {
+            // warp strips: every warp of the grid takes strips on its own
+            constexpr int WPC = NT / 32;
+            const PhysT<R> ph = make_phys<R>(a);
+            for (int k = blockIdx.x * WPC + (int)(threadIdx.x >> 5); k < a.nstrips; k += gridDim.x * WPC)
+                update_strip<R, MIXED>(a, a.strips[k], ph);
+        } else {
+            for (int tile = blockIdx.x; tile < a.nutiles; tile += gridDim.x) {
+                update_tile<R, MIXED, TR>(a, a.utiles[tile], smem_raw);
+                __syncthreads();
+            }
         }
     }
     warp_reduce_stats(a.status, st.zones, st.it64, st.it32, st.fbs, st.dtz, false);

@@ -202,6 +202,9 @@ cudaError_t fused_max_ctas_f64(bool mlp, int utr, int* per_sm);
 cudaError_t fused_max_ctas_mixed(bool mlp, int utr, int* per_sm);
 // Threads of a fused / update CTA for tile rows utr.
 inline int stage_threads(int utr) { return (utr + 1) * TILE_Q; }
+// Tile rows the fused kernel is instantiated for: utr when it is a tile
+// size, else 8 (warp strips of other lengths run in a CTA of 9 warps).
+inline int fused_tr(int utr) { return utr == 4 || utr == 16 ? utr : 8; }
 cudaError_t launch_prims_to_aos(const void* P, double* out, int64_t nr, int64_t nq, cudaStream_t s);
 cudaError_t launch_soa_to_aos(const double* soa, double* aos, double* scalar, int64_t nr, int64_t nq,
                               cudaStream_t s);

@@ -408,7 +408,7 @@ static cudaError_t fused_mixed(const StageArgs& a, const GhostArgs& g, const Fus
 cudaError_t launch_stage_fused_mixed(const StageArgs& a, const GhostArgs& g, const FusedArgs& f, int grid,
                                      cudaStream_t s) {
     const bool mlp = a.mlp != nullptr;
-    switch (a.utr) {
+    switch (fused_tr(a.utr)) {
     case 4: return mlp ? fused_mixed<4, true>(a, g, f, grid, s) : fused_mixed<4, false>(a, g, f, grid, s);
     case 16: return mlp ? fused_mixed<16, true>(a, g, f, grid, s) : fused_mixed<16, false>(a, g, f, grid, s);
     default: return mlp ? fused_mixed<8, true>(a, g, f, grid, s) : fused_mixed<8, false>(a, g, f, grid, s);
@@ -422,7 +422,7 @@ static cudaError_t fused_ctas_mixed(int* n) {
 }
 
 cudaError_t fused_max_ctas_mixed(bool mlp, int utr, int* n) {
-    switch (utr) {
+    switch (fused_tr(utr)) {
     case 4: return mlp ? fused_ctas_mixed<4, true>(n) : fused_ctas_mixed<4, false>(n);
     case 16: return mlp ? fused_ctas_mixed<16, true>(n) : fused_ctas_mixed<16, false>(n);
     default: return mlp ? fused_ctas_mixed<8, true>(n) : fused_ctas_mixed<8, false>(n);

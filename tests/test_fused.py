@@ -228,3 +228,28 @@ def test_mixed_strips_uneven_moving():
         g.advance(4)
     assert g.block_indexes() == ref.block_indexes()
     assert _same(g.state(), ref.state())
+
+
+@pytest.mark.parametrize("rows", [8, 32])
+def test_fused_strips_match(rows):
+    """The fused stage with warp strips in its update phase: FP64 equal to the
+    oracle, mixed equal to the separate strip form."""
+    import knc
+    from knc import workloads
+    w = workloads.uneven_small(order="RK3")
+    g, o = make_pair(w)
+    g.set_tuning(tile_rows=rows, strip=True, fused=True)
+    g.set_batched(True)
+    for _ in range(2):
+        g.advance(5)
+        o.advance(5)
+    assert _same(g.state(), o.state())
+    w = workloads.wind_small()
+    ref = _mixed(w, 8, False, False)
+    m, _ = make_pair(w, gpu=True)
+    m.set_precision(knc.abi.KNC_PRECISION_MIXED)
+    m.set_tuning(tile_rows=rows, strip=True, fused=True)
+    m.set_batched(True)
+    for _ in range(2):
+        m.advance(3)
+    assert _same(m.state(), ref.state())
