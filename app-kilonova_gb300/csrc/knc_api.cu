@@ -323,6 +323,11 @@ struct knc_ctx {
     int32_t sms = 0;
     bool coop = false;         // the device supports cooperative launches
     unsigned long long bar_epoch = 0;   // grid-barrier arrivals issued since the status reset
+    // adaptive dt found on the device in the fold's first recovery, with no
+    // separate pass (set by knc_advance for one fold)
+    bool ddt = false;
+    double ddt_t0 = 0.0;   // time at the start of the fold
+    int ddt_step = 0;      // step of the fold being issued
     double w_split = 2.0;
     float* d_mlp = nullptr;
     // bookkeeping
@@ -899,7 +904,7 @@ int fused_grid(knc_ctx* c) {
 
 // One Euler stage U_out = avg(U_in + dt L(U_in), U_base), src/scheme.rs:16-173.
 int run_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, double bf, double t_stage,
-              double dt) {
+              double dt, int sub) {
     int r;
     if (c->stage_counter >= 0xffff) return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "too many stages in one call");
     const int32_t stage = c->stage_counter++;
@@ -926,6 +931,14 @@ int run_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, doub
     g.gm = c->hp.gamma_law_index;
     g.single_precision = mixed(c) ? 1 : 0;
     g.status = c->d_status;
+    if (c->ddt) {
+        g.dt_bits = &c->d_status->dt_bits;
+        g.cfl = c->hp.cfl_number;
+        g.t0 = c->ddt_t0;
+        g.order = c->hp.runge_kutta_order;
+        g.step = c->ddt_step;
+        g.sub = sub;
+    }
     if (c->model.kind == KNC_MODEL_HOST) {
         if ((r = host_ghost_values(c, t_stage))) return r;
         g.host_prim[0] = c->d_host_prim;
@@ -941,6 +954,11 @@ int run_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, doub
     a.dt = dt;
     a.dt_f = (float)dt;
     a.avg_half = w1 == 0.5 && bf == 0.5 ? 1 : 0;
+    if (c->ddt) {
+        a.dt_bits = &c->d_status->dt_bits;
+        a.cfl = c->hp.cfl_number;
+        a.compute_dt = c->ddt_step == 0 && sub == 0 ? 1 : 0;   // the fold's first recovery finds dt
+    }
     if (c->fused) {
         // the whole stage in one cooperative launch (grid barriers between phases)
         FusedArgs f;
@@ -1030,37 +1048,37 @@ int rk_step(knc_ctx* c, double dt) {
     };
     int r;
     c->zone_updates += L(c).nzones;
-    if ((r = run_stage(c, A, B, -1, 1.0, 0.0, T.stage[0], dt))) return r;
+    if ((r = run_stage(c, A, B, -1, 1.0, 0.0, T.stage[0], dt, 0))) return r;
     Rational i1 = it0.add(one);
     if (order == 1) {
         c->cur = B;
-        c->time = T.end;
+        if (!c->ddt) c->time = T.end;
         c->iteration = i1;
         return KNC_OK;
     }
     if (order == 2) {
         const double bf = 0.5;
-        if ((r = run_stage(c, B, A, A, -bf + 1.0, bf, T.stage[1], dt))) return r;
+        if ((r = run_stage(c, B, A, A, -bf + 1.0, bf, T.stage[1], dt, 1))) return r;
         Rational half;
         half.n = 1;
         half.d = 2;
-        c->time = T.end;
+        if (!c->ddt) c->time = T.end;
         c->iteration = avg_iter(i1.add(one), half);
         return KNC_OK;
     }
     // RK3
     const double b2 = 0.75;
-    if ((r = run_stage(c, B, B, A, -b2 + 1.0, b2, T.stage[1], dt))) return r;
+    if ((r = run_stage(c, B, B, A, -b2 + 1.0, b2, T.stage[1], dt, 1))) return r;
     Rational q34;
     q34.n = 3;
     q34.d = 4;
     const Rational i2 = avg_iter(i1.add(one), q34);
     const double b3 = 1.0 / 3.0;
-    if ((r = run_stage(c, B, A, A, -b3 + 1.0, b3, T.stage[2], dt))) return r;
+    if ((r = run_stage(c, B, A, A, -b3 + 1.0, b3, T.stage[2], dt, 2))) return r;
     Rational q13;
     q13.n = 1;
     q13.d = 3;
-    c->time = T.end;
+    if (!c->ddt) c->time = T.end;
     c->iteration = avg_iter(i2.add(one), q13);
     return KNC_OK;
 }
@@ -1754,9 +1772,36 @@ int knc_advance(knc_ctx* c, int32_t fold) {
     if ((r = rebuild_table(c))) return r;
     if ((r = update_ghost_geometry(c))) return r;
     if ((r = reset_status(c, true))) return r;
-    double dt;
-    if ((r = time_step_impl(c, &dt))) return r;
     const int per_step = c->hp.runge_kutta_order;
+    // Adaptive dt (State::time_step, src/state.rs:151-160) normally costs a
+    // full recovery pass before the fold. On a fixed mesh with a device model
+    // the fold's first recovery reduces dl / a_max itself, every stage reads
+    // dt = min x cfl from the device, ghost rows form their stage times there,
+    // and the host learns dt (and advances the time) when the fold is done.
+    const bool adaptive = !(c->hp.system == KNC_SYSTEM_RELATIVISTIC && !c->hp.adaptive_time_step);
+    const bool ddt = adaptive && !c->mesh.moving() && c->model.kind != KNC_MODEL_HOST && fold > 0 &&
+                     (int64_t)fold * per_step < 0xffff;
+    double dt = 0.0;
+    if (ddt) {
+        c->ddt = true;
+        c->ddt_t0 = c->time;
+        c->ddt_step = 0;
+    } else if ((r = time_step_impl(c, &dt))) {
+        return r;
+    }
+    auto finish_ddt = [&](int rr) {
+        if (!c->ddt) return rr;
+        c->ddt = false;
+        if (rr == KNC_OK) {
+            double dtmin;
+            std::memcpy(&dtmin, &c->h_status->dt_bits, 8);
+            const double dtv = dtmin * c->hp.cfl_number;
+            double t = c->ddt_t0;
+            for (int32_t k = 0; k < fold; ++k) t = step_times(per_step, t, dtv).end;
+            c->time = t;
+        }
+        return rr;
+    };
     const bool graph = c->batched && c->model.kind != KNC_MODEL_HOST && fold > 0 &&
                        c->stage_counter + (int64_t)fold * per_step < 0xffff;
     if (graph) {
@@ -1780,6 +1825,7 @@ int knc_advance(knc_ctx* c, int32_t fold) {
             }
             if (step_init[k]) r = launch_activation(c);
             if (r == KNC_OK) r = rk_step(c, dt);
+            if (c->ddt) ++c->ddt_step;
         }
         cudaGraph_t g = nullptr;
         const cudaError_t ec = cudaStreamEndCapture(c->stream, &g);
@@ -1787,8 +1833,9 @@ int knc_advance(knc_ctx* c, int32_t fold) {
         if (r) {
             if (g) cudaGraphDestroy(g);
             c->failed = true;
-            return r;
+            return finish_ddt(r);
         }
+        if (ec != cudaSuccess) c->ddt = false;
         CK(ec);
         if (c->graph_exec) {
             cudaGraphExecUpdateResultInfo info;
@@ -1801,11 +1848,12 @@ int knc_advance(knc_ctx* c, int32_t fold) {
         cudaError_t ei = cudaSuccess;
         if (!c->graph_exec) ei = cudaGraphInstantiate(&c->graph_exec, g, 0);
         cudaGraphDestroy(g);
+        if (ei == cudaSuccess) ei = cudaGraphLaunch(c->graph_exec, c->stream);
+        if (ei != cudaSuccess) c->ddt = false;
         CK(ei);
-        CK(cudaGraphLaunch(c->graph_exec, c->stream));
         r = check_status(c);
         finish_fold(c);
-        return r;
+        return finish_ddt(r);
     }
     for (int32_t k = 0; k < fold; ++k) {
         if (c->mesh.moving())
@@ -1814,9 +1862,11 @@ int knc_advance(knc_ctx* c, int32_t fold) {
             if ((r = check_status(c))) return r;
             if ((r = reset_status(c, true))) return r;
         }
-        if ((r = rk_step(c, dt))) return r;
+        r = rk_step(c, dt);
+        if (c->ddt) ++c->ddt_step;
+        if (r) return finish_ddt(r);
     }
-    return check_status(c);
+    return finish_ddt(check_status(c));
 }
 
 int knc_set_profiling(knc_ctx* c, int32_t on) {
@@ -1963,9 +2013,9 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
         if ((r = rebuild_table(c))) break;
         if (t.update_form == KNC_UPDATE_TILE_TMA && !L(c).tma_ok) continue;
         // the first stage reads buf[cur] and writes buf[1 - cur]: the state stays
-        if ((r = run_stage(c, c->cur, 1 - c->cur, -1, 1.0, 0.0, c->time, dt))) break;
+        if ((r = run_stage(c, c->cur, 1 - c->cur, -1, 1.0, 0.0, c->time, dt, 0))) break;
         CK(cudaEventRecord(e0, c->stream));
-        for (int k = 0; k < reps && r == KNC_OK; ++k) r = run_stage(c, c->cur, 1 - c->cur, -1, 1.0, 0.0, c->time, dt);
+        for (int k = 0; k < reps && r == KNC_OK; ++k) r = run_stage(c, c->cur, 1 - c->cur, -1, 1.0, 0.0, c->time, dt, 0);
         CK(cudaEventRecord(e1, c->stream));
         CK(cudaEventSynchronize(e1));
         if (r) break;

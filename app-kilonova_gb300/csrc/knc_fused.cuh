@@ -111,6 +111,13 @@ __device__ __forceinline__ void stage_fused_body(const StageArgs& a, const Ghost
             }
         }
     }
+    if (a.compute_dt) {
+        // the adaptive time step must be complete before phase C reads it
+        double dtz = st.dtz;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dtz = fmin(dtz, __shfl_down_sync(0xffffffffu, dtz, o));
+        if ((threadIdx.x & 31) == 0) atomicMin(&a.status->dt_bits, (unsigned long long)__double_as_longlong(dtz));
+    }
     grid_barrier(a.status, f.bar_base + gridDim.x);
 
     // ---- B: remaps

@@ -17,6 +17,31 @@
 
 namespace knc {
 
+// The time of stage `sub` of step `step` of a fold that started at t0 with
+// time step dt: the host's step arithmetic (the averages t1 (1 - b) + t0 b of
+// godunov_core::runge_kutta, b = 1/2; 3/4 then 1/3), rounded operation by
+// operation without contraction, so it equals the host's value bit for bit.
+__device__ __forceinline__ double fold_stage_time(double t0, double dt, int order, int step, int sub) {
+    auto avg = [](double t1, double tb, double bf) {
+        return __dadd_rn(__dmul_rn(t1, __dadd_rn(-bf, 1.0)), __dmul_rn(tb, bf));
+    };
+    double t = t0;
+    for (int k = 0;; ++k) {
+        const double t1 = __dadd_rn(t, dt);
+        double t2 = 0.0, end;
+        if (order == 1) {
+            end = t1;
+        } else if (order == 2) {
+            end = avg(__dadd_rn(t1, dt), t, 0.5);
+        } else {
+            t2 = avg(__dadd_rn(t1, dt), t, 0.75);
+            end = avg(__dadd_rn(t2, dt), t, 1.0 / 3.0);
+        }
+        if (k >= step) return sub == 0 ? t : sub == 1 ? t1 : t2;
+        t = end;
+    }
+}
+
 // Zone k of the 2 x nq[end] ghost rows of end `end` (0: inner ghost block,
 // min index - 1, whose last two rows feed the innermost block's rows 0, 1;
 // 1: outer ghost block, whose first two rows feed rows nr+2, nr+3).
@@ -37,7 +62,10 @@ static __device__ __noinline__ void ghost_zone(const GhostArgs& a, int end, int 
         Pm[3] = hp[3];
         scalar = hp[4];
     } else {
-        model_eval(a.model, r, q, a.time, false, a.ghost_index[end], 0, j, Pm, scalar);
+        const double t = a.dt_bits ? fold_stage_time(a.t0, __dmul_rn(__longlong_as_double((long long)*a.dt_bits), a.cfl),
+                                                     a.order, a.step, a.sub)
+                                   : a.time;
+        model_eval(a.model, r, q, t, false, a.ghost_index[end], 0, j, Pm, scalar);
     }
     PhysT<double> ph;
     ph.srhd = a.srhd;

@@ -102,6 +102,10 @@ struct StageArgs {
     const int4* strips;     // {slot, i0, j0, rows}: warp strips of the strip form, or null
     int32_t nstrips;
     int32_t strip_ctas;     // strip form: CTAs per SM the kernel is built for (4, 5 or 6)
+    // adaptive dt found on the device (the fold's first recovery reduces
+    // dl / a_max into *dt_bits): dt = *dt_bits x cfl replaces dt / dt_f
+    const unsigned long long* dt_bits;
+    double cfl;
     const void* tmaps;      // TmaMaps per slot (knc_tma.cuh), or null
     int32_t stage;          // stage counter for error ordering
     int32_t sel_in, sel_out, sel_base;   // state buffer selectors; sel_base < 0: no average
@@ -141,6 +145,12 @@ struct GhostArgs {
     double gm;
     int32_t single_precision;   // write float P
     DevStatus* status;
+    // adaptive dt found on the device in the fold's first recovery: the stage
+    // time is then fold_stage_time(t0, dt, order, step, sub), dt = *dt_bits x cfl
+    const unsigned long long* dt_bits;
+    double cfl;
+    double t0;
+    int32_t order, step, sub, pad_;
 };
 
 // Fused-stage extras: recovery chunks {slot, z0, nz, 0} of at most

@@ -177,6 +177,22 @@ struct MixedC2p {
             wz = sqrtf(1.0f + P[1] * P[1] + P[2] * P[2]);
             const float v[NFIELD] = {P[0], P[1], P[2], P[3], d2f_rn(U[4]) / dV / wz};
             store_prim<float>(B, i, j, v);
+            if (a.compute_dt && kind == HYDRO_NONE) {
+                // State::time_step (src/state.rs:151-160) on this stage's
+                // primitives: signal speed in FP32, dl and dl / a in FP64
+                PhysT<float> ph;
+                ph.srhd = 1;
+                ph.hllc = 0;
+                ph.gm = a.gm_f;
+                ph.gm1 = a.gm1_f;
+                ph.gh = a.gh_f;
+                ph.theta = a.theta_f;
+                const double dr = B.rv[i + 1] - B.rv[i];
+                const double dq = B.qv[j + 1] - B.qv[j];
+                const double dl = fmin(dr, dq * B.rv[i]);
+                const double amax = (double)max_signal_speed(ph, P) * a.cflux;
+                st.dtz = fmin(st.dtz, dl / amax);
+            }
         }
     }
 };
@@ -201,7 +217,7 @@ __global__ void __launch_bounds__(TILE_THREADS, 3) c2p_mixed_kernel(StageArgs a)
         const int j = t.z + threadIdx.x % TILE_Q;
         MixedC2p<MLP>::zone(a, t.x, B, i, j, i < B.nr && j < B.nq, W, act, st);
     }
-    warp_reduce_stats(a.status, st.zones, st.it64, st.it32, st.fbs, 0.0, false);
+    warp_reduce_stats(a.status, st.zones, st.it64, st.it32, st.fbs, st.dtz, a.compute_dt != 0);
 }
 
 // ---- the fused stage (mixed) -------------------------------------------------

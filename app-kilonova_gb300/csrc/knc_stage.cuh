@@ -88,6 +88,17 @@ __device__ __forceinline__ R stage_plm(R theta, R a, R b, R c) {
     else return plm_gradient(theta, a, b, c);
 }
 
+// The stage's time step: the host's dt, or (adaptive dt found on the device)
+// the reduced dl / a_max times the CFL number, formed like the host would.
+template <class R>
+__device__ __forceinline__ R stage_dt(const StageArgs& a) {
+    if (a.dt_bits) {
+        const double d = __dmul_rn(__longlong_as_double((long long)*(volatile unsigned long long*)a.dt_bits), a.cfl);
+        return (R)d;
+    }
+    return sizeof(R) == 4 ? (R)a.dt_f : (R)a.dt;
+}
+
 template <class R, bool MIXED, int TR_, bool BOX = false>
 __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, unsigned char* smem_raw,
                                             const R* boxP = nullptr, const double* boxU = nullptr,
@@ -255,7 +266,7 @@ __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, un
                 sources(ph, Pc, (R)B.rc[i], (R)B.cot[j], src);
                 dV = (R)B.dv[z];
             }
-            const R dt = sizeof(R) == 4 ? (R)a.dt_f : (R)a.dt;
+            const R dt = stage_dt<R>(a);
             const double* Uin = B.buf[a.sel_in];
             double* Uout = B.buf[a.sel_out];
             const double* U0 = a.sel_base >= 0 ? B.buf[a.sel_base] : nullptr;
@@ -376,7 +387,7 @@ __device__ __forceinline__ void update_strip(const StageArgs& a, const int4 it, 
     const int64_t n = (int64_t)nr * nq;
     const R th = ph.theta;
     const R cflux = sizeof(R) == 4 ? (R)a.cflux_f : (R)a.cflux;
-    const R dt = sizeof(R) == 4 ? (R)a.dt_f : (R)a.dt;
+    const R dt = stage_dt<R>(a);
     const double* Uin = B.buf[a.sel_in];
     double* Uout = B.buf[a.sel_out];
     const double* U0 = a.sel_base >= 0 ? B.buf[a.sel_base] : nullptr;

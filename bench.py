@@ -39,16 +39,17 @@ sys.path.insert(0, str(ROOT / "app-kilonova_gb300"))
 
 METRIC = "zone-updates/s per GB300: mixed+learned vs plain FP64 GPU at L1<1e-6; HBM %"
 UNIT = "zone-updates/s"
-# Algorithmic HBM bytes per zone of the mixed RK2 step (5 fields; state FP64,
-# primitives FP32):
-#   recovery launch  reads U (40 B), writes P (20 B)                 60 B
-#   update, stage 1  reads P (20 B) and U (40 B), writes U1 (40 B)  100 B
-#   update, stage 2  also reads the RK base U0 (40 B)               140 B
-# so one update launch averages 120 B per zone and a whole step moves
-# 2 x 60 + 100 + 140 = 360 B per zone-update.
-ALG_BYTES_UPDATE_LAUNCH = 120.0
-ALG_BYTES_RECOVERY_LAUNCH = 60.0
-ALG_BYTES_PER_ZONE_UPDATE = 360.0
+# Algorithmic HBM bytes per zone (5 fields, FP64 conserved state): an RK2
+# zone-update reads U and writes U1 (80 B), then reads U1 and U0 and writes
+# (120 B): 200 B. Geometry counts 0 (recomputable) and halo re-reads are not
+# algorithmic. The update launch carries the stage's state traffic, 80 or
+# 120 B, on average 100 B per zone. The primitives this design keeps between
+# the recovery and the update (FP32, written once and read once per stage:
+# 40 B per stage) are an intermediate of the implementation, reported apart.
+ALG_BYTES_UPDATE_LAUNCH = 100.0
+ALG_BYTES_RECOVERY_LAUNCH = 40.0
+ALG_BYTES_PER_ZONE_UPDATE = 200.0
+INTERMEDIATE_BYTES_PER_ZONE_UPDATE = 2 * 40.0 + 2 * 20.0 + 2 * 20.0   # U re-read by the recovery, P written and read
 
 
 def load_peaks():
@@ -206,7 +207,8 @@ def run_reference(args):
 
 
 # ncu summaries of the mixed-stage kernels on this workload (one capture each)
-PROFILE_OF = {"update": "update_kernel_mixed_wind_4096x1024.md", "c2p": "c2p_mixed_wind_4096x1024.md"}
+# (captured on the strip form of the update, the shape the autotuner picks there)
+PROFILE_OF = {"update": "update_strip_mixed_wind_4096x1024.md", "c2p": "c2p_mixed_wind_4096x1024.md"}
 
 
 def profiled_traffic(kernel: str):
@@ -281,7 +283,7 @@ def run_knc(args):
         return ms, s.launch_count() - l0
 
     # ---- plain FP64 path
-    fp64 = make(False, False, False)
+    fp64 = make(False, False, False, tune=True)
     fp64.reset_c2p_stats()
     ms64, _ = timed(fp64, args.steps, args.fold)
     st64 = fp64.c2p_stats()
@@ -318,7 +320,7 @@ def run_knc(args):
     per_zone = {"update": ALG_BYTES_UPDATE_LAUNCH, "c2p": ALG_BYTES_RECOVERY_LAUNCH}.get(dom, 0.0)
     alg_bytes = per_zone * zones
     achieved = alg_bytes / (dom_ms * 1e-3) / 1e9
-    traffic = profiled_traffic(dom)
+    traffic = profiled_traffic(dom) if (dom != "update" or tuning.get("strip")) else None
 
     # ---- end to end through the C ABI with host buffers
     nb = w.num_blocks
@@ -346,7 +348,7 @@ def run_knc(args):
     un = None
     if not args.no_uneven:
         wu = workloads.uneven(seed=1 + rank)
-        u64 = make(False, False, False, workload=wu)
+        u64 = make(False, False, False, workload=wu, tune=True)
         ms_u64, _ = timed(u64, args.steps, args.fold)
         zu64 = timed.zone_updates
         uh = make(True, True, True, workload=wu, tune=True)
@@ -385,7 +387,7 @@ def run_knc(args):
                                                "learned c2p guess, CUDA graph per fold",
                        "fold": args.fold, "l2": "state 168 MB per buffer > 129 MB L2 (no flush needed)",
                        "parallelism": f"replicas x{world}", "tuning": tuning},
-            "fp64": {"value": v64, "ms_per_step": ms64 / args.steps,
+            "fp64": {"value": v64, "ms_per_step": ms64 / args.steps, "tuning": fp64.tuning(),
                      "newton_iters_per_zone": st64["iters_fp64"] / max(st64["zones"], 1),
                      "fp64_peak_gflops": fp64_peak},
             "speedup_vs_fp64": value / v64,
@@ -400,7 +402,10 @@ def run_knc(args):
                          "alg_bytes_per_zone_launch": per_zone,
                          "step": {"alg_bytes_per_zone_update": ALG_BYTES_PER_ZONE_UPDATE,
                                   "achieved": ALG_BYTES_PER_ZONE_UPDATE * value / 1e9,
-                                  "frac": ALG_BYTES_PER_ZONE_UPDATE * value / 1e9 / hbm_peak}},
+                                  "frac": ALG_BYTES_PER_ZONE_UPDATE * value / 1e9 / hbm_peak,
+                                  "with_intermediates_frac": (ALG_BYTES_PER_ZONE_UPDATE +
+                                                              INTERMEDIATE_BYTES_PER_ZONE_UPDATE) * value / 1e9 /
+                                                             hbm_peak}},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d},
             "gpu_launches": launches,
             "clocks": clk,
@@ -422,7 +427,8 @@ def run_only(args):
     w = workloads.WORKLOADS[args.workload]()
     s = knc.build_solver(w)
     if args.tile_rows:
-        s.set_tuning(tile_rows=args.tile_rows, fused=args.fused, tma=args.tma, strip=args.strip)
+        s.set_tuning(tile_rows=args.tile_rows, fused=args.fused, tma=args.tma, strip=args.strip,
+                     ctas_per_sm=args.ctas_per_sm)
     if args.only == "mixed":
         s.set_precision(abi.KNC_PRECISION_MIXED)
         s.set_mixed_w_split(args.w_split)
@@ -461,6 +467,7 @@ def main():
     ap.add_argument("--fused", action="store_true")
     ap.add_argument("--tma", action="store_true")
     ap.add_argument("--strip", action="store_true")
+    ap.add_argument("--ctas-per-sm", type=int, default=0)
     ap.add_argument("--only", choices=["fp64", "mixed"], default=None,
                     help="run one path alone (profiler captures)")
     args = ap.parse_args()

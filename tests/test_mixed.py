@@ -95,3 +95,25 @@ def test_fp64_graph_bitwise():
     g.advance(5)
     o.advance(5)
     assert max(field_errors(g.state(), o.state())) == 0.0
+
+
+def test_mixed_adaptive_dt_in_the_fold():
+    """Mixed precision with adaptive dt: the fold's first (mixed) recovery
+    finds dt from FP32 signal speeds; the time stays within 1e-5 of the FP64
+    path's and the state stays close."""
+    import knc
+    from helpers import field_errors, make_pair
+    from knc import workloads
+    w = workloads.wind_small()
+    w.hydro.adaptive_time_step = True
+    g64, _ = make_pair(w, gpu=True)
+    gm, _ = make_pair(w, gpu=True)
+    gm.set_precision(knc.abi.KNC_PRECISION_MIXED)
+    gm.set_batched(True)
+    for _ in range(3):
+        g64.advance(5)
+        gm.advance(5)
+    t64, tm = g64.time()[0], gm.time()[0]
+    assert abs(tm - t64) <= 1e-5 * t64
+    errs = field_errors(gm.state(), g64.state())
+    assert errs[0] <= 1e-4, errs

@@ -135,3 +135,26 @@ def test_state_roundtrip():
     st2 = g.state()
     for i in st:
         assert np.array_equal(st[i][0], st2[i][0])
+
+
+def test_adaptive_dt_found_in_the_fold():
+    """Adaptive dt: the fold's first recovery finds dt on the device (no
+    separate pass); states and times equal the oracle's, which runs the
+    separate time_step pass, for both the stream and the graph path."""
+    import knc
+    from knc import workloads
+    for riemann, batched in (("HLLE", False), ("HLLC", True)):
+        w = workloads.sphere_small(riemann=riemann)
+        g, o = make_pair(w)
+        g.set_batched(batched)
+        n0 = g.launch_count()
+        g.advance(5)
+        o.advance(5)
+        # 5 RK2 steps, 3 launches per stage, no extra recovery pass
+        assert g.launch_count() - n0 == 5 * 2 * 3
+        assert g.time() == o.time()
+        assert max(zone_relative_errors(g.state(), o.state())) == 0.0
+        g.advance(3)
+        o.advance(3)
+        assert g.time() == o.time()
+        assert max(field_errors(g.state(), o.state())) <= TOL
