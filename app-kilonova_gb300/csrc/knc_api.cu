@@ -1765,7 +1765,19 @@ void finish_fold(knc_ctx* c) {
 
 }  // namespace
 
-int knc_advance(knc_ctx* c, int32_t fold) {
+namespace {
+int advance_impl(knc_ctx* c, int32_t fold, const double* dt_given);
+}
+
+int knc_advance(knc_ctx* c, int32_t fold) { return advance_impl(c, fold, nullptr); }
+
+int knc_advance_dt(knc_ctx* c, int32_t fold, double dt) {
+    if (!c || !(dt > 0.0)) return KNC_ERR_INVALID_ARGUMENT;
+    return advance_impl(c, fold, &dt);
+}
+
+namespace {
+int advance_impl(knc_ctx* c, int32_t fold, const double* dt_given) {
     if (!c || fold < 0) return KNC_ERR_INVALID_ARGUMENT;
     int r = KNC_OK;
     if ((r = check_ready(c))) return r;
@@ -1779,10 +1791,12 @@ int knc_advance(knc_ctx* c, int32_t fold) {
     // dt = min x cfl from the device, ghost rows form their stage times there,
     // and the host learns dt (and advances the time) when the fold is done.
     const bool adaptive = !(c->hp.system == KNC_SYSTEM_RELATIVISTIC && !c->hp.adaptive_time_step);
-    const bool ddt = adaptive && !c->mesh.moving() && c->model.kind != KNC_MODEL_HOST && fold > 0 &&
+    const bool ddt = !dt_given && adaptive && !c->mesh.moving() && c->model.kind != KNC_MODEL_HOST && fold > 0 &&
                      (int64_t)fold * per_step < 0xffff;
     double dt = 0.0;
-    if (ddt) {
+    if (dt_given) {
+        dt = *dt_given;
+    } else if (ddt) {
         c->ddt = true;
         c->ddt_t0 = c->time;
         c->ddt_step = 0;
@@ -1868,6 +1882,7 @@ int knc_advance(knc_ctx* c, int32_t fold) {
     }
     return finish_ddt(check_status(c));
 }
+}  // namespace
 
 int knc_set_profiling(knc_ctx* c, int32_t on) {
     if (!c) return KNC_ERR_INVALID_ARGUMENT;

@@ -232,8 +232,12 @@ class Solver:
         self._check(self.lib.knc_time_step(self.h, C.byref(dt)), "time_step")
         return dt.value
 
-    def advance(self, fold: int = 1):
-        self._check(self.lib.knc_advance(self.h, int(fold)), "advance")
+    def advance(self, fold: int = 1, dt=None):
+        """scheme::advance; with dt given, that time step instead of time_step()."""
+        if dt is None:
+            self._check(self.lib.knc_advance(self.h, int(fold)), "advance")
+        else:
+            self._check(self.lib.knc_advance_dt(self.h, int(fold), float(dt)), "advance_dt")
 
     def try_advance(self, fold: int = 1) -> int:
         return self.lib.knc_advance(self.h, int(fold))

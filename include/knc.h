@@ -222,6 +222,12 @@ int knc_time_step(knc_ctx* ctx, double* dt);
 /* scheme::advance (src/scheme.rs:212-240): dt once, then `fold` times
  * {add_remove_blocks if the excision surfaces move; one RK step}. */
 int knc_advance(knc_ctx* ctx, int32_t fold);
+/* scheme::advance with the time step given by the caller instead of
+ * State::time_step: a driver that splits the mesh into radial slabs (one
+ * context per slab) passes the minimum of every slab's knc_time_step, the
+ * one reduction the decomposition needs per advance. No counterpart in the
+ * reference, which always advances the whole state. */
+int knc_advance_dt(knc_ctx* ctx, int32_t fold, double dt);
 
 /* Chosen forms. */
 int knc_set_precision(knc_ctx* ctx, int32_t precision);          /* KNC_PRECISION_* */

@@ -1275,6 +1275,13 @@ int oracle_advance(oracle_ctx* c, int32_t fold) {
     double dt;
     const int r = oracle_time_step(c, &dt);
     if (r != KNC_OK) return r;
+    return oracle_advance_dt(c, fold, dt);
+}
+
+// scheme::advance with the time step given by the caller (a multi-domain
+// driver passes the minimum of every domain's time_step).
+int oracle_advance_dt(oracle_ctx* c, int32_t fold, double dt) {
+    if (!c || fold < 0 || c->blocks.empty() || !(dt > 0.0)) return KNC_ERR_INVALID_ARGUMENT;
     for (int32_t k = 0; k < fold; ++k) {
         if (c->mesh.moving()) add_remove_blocks(c);
         if (!rk_step(c, dt)) return KNC_ERR_HYDRO;

@@ -50,6 +50,7 @@ int oracle_set_time(oracle_ctx* ctx, double time, int64_t num, int64_t den);
 int oracle_get_time(const oracle_ctx* ctx, double* time, int64_t* num, int64_t* den);
 int oracle_time_step(oracle_ctx* ctx, double* dt);
 int oracle_advance(oracle_ctx* ctx, int32_t fold);
+int oracle_advance_dt(oracle_ctx* ctx, int32_t fold, double dt);
 int oracle_last_error(const oracle_ctx* ctx, knc_error* out);
 /* Newton iterations summed since creation (c2p calls on live and ghost blocks). */
 int oracle_c2p_stats(const oracle_ctx* ctx, int64_t* zones, int64_t* iters);

@@ -55,6 +55,7 @@ def load():
         "oracle_get_time": (C.c_int, [P, DP, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
         "oracle_time_step": (C.c_int, [P, DP]),
         "oracle_advance": (C.c_int, [P, C.c_int32]),
+        "oracle_advance_dt": (C.c_int, [P, C.c_int32, C.c_double]),
         "oracle_last_error": (C.c_int, [P, C.POINTER(abi.Error)]),
         "oracle_c2p_stats": (C.c_int, [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
         "oracle_prim_to_cons": (None, [C.POINTER(abi.HydroParams), DP, DP]),
@@ -174,8 +175,11 @@ class Oracle:
         self._check(self.lib.oracle_time_step(self.h, C.byref(dt)), "time_step")
         return dt.value
 
-    def advance(self, fold: int = 1):
-        self._check(self.lib.oracle_advance(self.h, fold), "advance")
+    def advance(self, fold: int = 1, dt=None):
+        if dt is None:
+            self._check(self.lib.oracle_advance(self.h, fold), "advance")
+        else:
+            self._check(self.lib.oracle_advance_dt(self.h, fold, float(dt)), "advance_dt")
 
     def last_error(self):
         e = self._abi.Error()
