@@ -64,7 +64,7 @@ class SlabDomain:
 
 
 def advance_slabs(domains: Sequence[SlabDomain], fold: int,
-                  allreduce_min: Callable[[float], float] = min,
+                  allreduce_min: Callable[[float], float] = None,
                   allgather: Callable[[dict], List[dict]] = None):
     """One fold on every local domain: global dt, advance, exchange owned
     blocks. With one process holding all domains the defaults suffice; ranks
@@ -73,7 +73,7 @@ def advance_slabs(domains: Sequence[SlabDomain], fold: int,
         if fold > d.max_fold():
             raise ValueError(f"fold {fold} exceeds what the overlap covers ({d.max_fold()})")
     local_dt = min(d.engine.time_step() for d in domains)
-    dt = allreduce_min(local_dt)
+    dt = allreduce_min(local_dt) if allreduce_min else local_dt
     for d in domains:
         d.engine.advance(fold, dt)
     mine = {}
