@@ -94,6 +94,16 @@ float2 split_df(double x) {
     return make_float2(hi, (float)(x - (double)hi));
 }
 
+// Length unit L = 2^e of the mixed stage's FP32 geometry: the power of two at
+// or below the reference radius, so FP32 radii stay near 1 whatever the
+// units (code units: e = 0; the reference's cgs setups: r ~ 1e8-1e19 cm, where
+// c r^3 in cm^3 cm/s would overflow FP32).
+int length_exponent(const knc_mesh_params& p) {
+    int e = 0;
+    std::frexp(p.reference_radius, &e);
+    return e - 1;
+}
+
 GeomH make_geometry(const MeshH& M, int32_t index, bool with_faces = true, double cflux = 1.0, int64_t nr = 0,
                     int64_t nq = 0) {   // mesh.rs:246-264
     GeomH G;
@@ -127,20 +137,22 @@ GeomH make_geometry(const MeshH& M, int32_t index, bool with_faces = true, doubl
     for (int64_t i = 0; i < nr; ++i)
         for (int64_t j = 0; j <= nq; ++j)
             G.aq[i * (nq + 1) + j] = face_area(G.rv[i], G.qv[j], G.rv[i + 1], G.qv[j]);
-    // separable factors for the mixed path (double-float pairs, c folded in)
+    // separable factors for the mixed path (double-float pairs, c folded in),
+    // lengths in units of L = 2^e (exact power-of-two scalings)
+    const int le = length_exponent(M.p);
     G.ar_r.resize(nr + 1);
     G.aq_r.resize(nr);
     G.dv_r.resize(nr);
     G.dv_r32.resize(nr);
     G.rc32.resize(nr);
-    for (int64_t i = 0; i <= nr; ++i) G.ar_r[i] = split_df(cflux * (G.rv[i] * G.rv[i]));
+    for (int64_t i = 0; i <= nr; ++i) G.ar_r[i] = split_df(std::ldexp(cflux * (G.rv[i] * G.rv[i]), -2 * le));
     for (int64_t i = 0; i < nr; ++i) {
         const double a = G.rv[i], b = G.rv[i + 1];
-        G.aq_r[i] = split_df(cflux * (PI_H * (b * b - a * a)));
+        G.aq_r[i] = split_df(std::ldexp(cflux * (PI_H * (b * b - a * a)), -2 * le));
         const double v = (b * b * b - a * a * a) * 2.0 * PI_H / 3.0;
-        G.dv_r[i] = split_df(cflux * v);
-        G.dv_r32[i] = (float)v;
-        G.rc32[i] = (float)G.rc[i];
+        G.dv_r[i] = split_df(std::ldexp(cflux * v, -3 * le));
+        G.dv_r32[i] = (float)std::ldexp(v, -3 * le);
+        G.rc32[i] = (float)std::ldexp(G.rc[i], -le);
     }
     G.ar_q.resize(nq);
     G.aq_q.resize(nq + 1);
@@ -860,6 +872,10 @@ StageArgs base_args(knc_ctx* c) {
     a.theta_f = (float)a.plm_theta;
     a.cflux_f = (float)a.cflux;
     a.high_thr_f = (float)(1.0 - 1.0 / (c->w_split * c->w_split));
+    const int le = length_exponent(c->mesh.p);
+    a.lscale2 = 2 * le;
+    a.lscale3 = 3 * le;
+    a.lscale3_d = std::ldexp(1.0, -3 * le);
     a.mlp = c->guess == KNC_GUESS_MLP ? c->d_mlp : nullptr;
     a.status = c->d_status;
     a.sel_base = -1;

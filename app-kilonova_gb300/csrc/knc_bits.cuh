@@ -51,6 +51,44 @@ __device__ __forceinline__ double f2d(float x) {
     return __longlong_as_double((long long)(((unsigned long long)hi << 32) | lo));
 }
 
+// d2f_rn(x * 2^de) and x * 2^de exactly as a double (de small; the mixed
+// stage's length scale): the power of two enters the exponent field, so the
+// scaled value is formed without an FP64 multiply.
+__device__ __forceinline__ float d2f_rn_exp(double x, int de) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
+    const uint32_t sign = hi & 0x80000000u;
+    const uint32_t ex = (hi >> 20) & 0x7ffu;
+    const int e32 = (int)ex - 1023 + 127 + (ex ? de : 0);
+    const uint32_t m23 = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const uint32_t rest = lo & 0x1fffffffu;
+    uint32_t r = ((uint32_t)e32 << 23) + m23;
+    r += (rest > 0x10000000u) || (rest == 0x10000000u && (m23 & 1u));
+    r = e32 <= 0 ? 0u : r;
+    r = (e32 >= 255 || ex == 0x7ffu) ? 0x7f800000u : r;
+    r = r > 0x7f800000u ? 0x7f800000u : r;
+    return __uint_as_float(sign | r);
+}
+
+__device__ __forceinline__ double f2d_exp(float x, int de) {
+    const uint32_t f = __float_as_uint(x);
+    const uint32_t sign = f & 0x80000000u;
+    const uint32_t e = (f >> 23) & 0xffu;
+    const uint32_t m = f & 0x7fffffu;
+    uint32_t hi, lo;
+    if (e == 0u) {
+        hi = sign;
+        lo = 0u;
+    } else if (e == 0xffu) {
+        hi = sign | 0x7ff00000u | (m >> 3);
+        lo = m << 29;
+    } else {
+        hi = sign | ((uint32_t)((int)e - 127 + 1023 + de) << 20) | (m >> 3);
+        lo = m << 29;
+    }
+    return __longlong_as_double((long long)(((unsigned long long)hi << 32) | lo));
+}
+
 // True when x < 0 (a negative number, not -0), from the high word alone.
 __device__ __forceinline__ bool is_negative(double x) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);

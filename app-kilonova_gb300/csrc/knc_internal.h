@@ -123,6 +123,11 @@ struct StageArgs {
     // in FP64 for them (on GB300 the FP64 pipe is the narrow one)
     float gm_f, gm1_f, gh_f, theta_f, dt_f, cflux_f;
     float high_thr_f;       // 1 - 1 / w_split^2: |S| / (D + tau) squared above it means W > w_split
+    // mixed stage length unit L = 2^e: its FP32 geometry is in units of L
+    // (areas 2^(-2e), volumes 2^(-3e)), so increments scale back by 2^(2e)
+    // and recovered densities use volumes in L^3
+    int32_t lscale2, lscale3;   // 2e, 3e
+    double lscale3_d;           // 2^(-3e)
     int32_t avg_half;       // w1 == bf == 1/2 (the RK2 average, halved exactly on the integer pipe)
     const float* mlp;       // packed MLP weights (device) or null
     DevStatus* status;

@@ -99,20 +99,28 @@ struct MixedC2p {
         int kind = HYDRO_NONE;
         if (active && is_negative(m)) kind = HYDRO_NEGATIVE_DENSITY;
         else if (active && is_negative(tau)) kind = HYDRO_NEGATIVE_ENERGY_DENSITY;
-        // FP32 copies by integer conversion (no FP64-pipe instructions)
-        const float mf = d2f_rn(m), tauf = d2f_rn(tau), s1f = d2f_rn(U[1]), s2f = d2f_rn(U[2]);
-        const float ssf = s1f * s1f + s2f * s2f;
-        const float sf = sqrtf(ssf);
-        const float x1 = __fdividef(sf, mf + tauf);
+        // FP32 copies by integer conversion (no FP64-pipe instructions), in
+        // the stage's length units: volumes (and so the volume integrals)
+        // carry 2^(-3 e) with L = 2^e near the reference radius
+        const int de = -a.lscale3;
+        const float mf = d2f_rn_exp(m, de), tauf = d2f_rn_exp(tau, de);
+        const float s1f = d2f_rn_exp(U[1], de), s2f = d2f_rn_exp(U[2], de);
+        // the FP32 iteration runs on the state per unit mass (O(1) numbers,
+        // no overflow or underflow of the squares whatever the units); the
+        // recovery is scale-invariant, p = (p / m) m
+        const float im = 1.0f / mf;
+        const float s1n = s1f * im, s2n = s2f * im, taun = tauf * im;
+        const float ssn = s1n * s1n + s2n * s2n;
+        const float x1 = __fdividef(sqrtf(ssn), 1.0f + taun);   // |S| / (D + tau)
         const bool high = active && kind == HYDRO_NONE && x1 * x1 > high_thr;
-        float guess = 0.0f;
+        float guess = 0.0f;   // p / m
         if (MLP) {
             if (__any_sync(0xffffffffu, high)) {
                 float x[3];
                 const bool ok = mlp_features(m, U[1] * U[1] + U[2] * U[2], tau, x);
                 const float y = mlp_guess_call(W, act, x[0], x[1], x[2]);
-                const float gsv = mf * __expf(y);
-                guess = (ok && gsv > 0.0f) ? fminf(gsv, (gmf - 1.0f) * tauf) : 0.0f;
+                const float gsv = __expf(y);
+                guess = (ok && gsv > 0.0f) ? fminf(gsv, (gmf - 1.0f) * taun) : 0.0f;
             }
         }
         float P[4] = {0.f, 0.f, 0.f, 0.f};
@@ -121,22 +129,22 @@ struct MixedC2p {
             ++st.zones;
             float p32 = 0.f, w32 = 1.f;
             int it32 = 0;
-            const bool ok32 = newton_fast<float>(mf, ssf, tauf, gmf, guess, 1e-30f, 1e-6f, 16, p32, w32, it32);
+            const bool ok32 = newton_fast<float>(1.0f, ssn, taun, gmf, guess, 1e-30f, 1e-6f, 16, p32, w32, it32);
             st.it32 += (unsigned long long)it32;
             if (!high && ok32) {
                 const float inv_dv = 1.0f / dV;
-                const float inv_et = 1.0f / (tauf + mf + p32);
+                const float inv_et = 1.0f / (taun + 1.0f + p32);
                 P[0] = mf / w32 * inv_dv;
-                P[1] = w32 * s1f * inv_et;
-                P[2] = w32 * s2f * inv_et;
-                P[3] = p32 * inv_dv;
+                P[1] = w32 * s1n * inv_et;
+                P[2] = w32 * s2n * inv_et;
+                P[3] = p32 * mf * inv_dv;
                 if (p32 < 0.f) P[3] = (float)PRESSURE_FLOOR * P[0];
             } else {
                 const double ss = U[1] * U[1] + U[2] * U[2];
                 const double tol = NEWTON_TOLERANCE * (m + tau);
                 double p64 = 0.0, w64 = 1.0;
                 int it64 = 0;
-                bool ok = newton_fast<double>(m, ss, tau, gm, ok32 ? (double)p32 : 0.0, tol, 0.0, NEWTON_ITER_MAX,
+                bool ok = newton_fast<double>(m, ss, tau, gm, ok32 ? (double)p32 * m : 0.0, tol, 0.0, NEWTON_ITER_MAX,
                                               p64, w64, it64);
                 st.it64 += (unsigned long long)it64;
                 if (!ok) {
@@ -151,15 +159,16 @@ struct MixedC2p {
                     if (kf == HYDRO_ROOT_FINDER_FAILED) {
                         kind = kf;
                     } else {
-                        // Pd is the (floored) primitive of the volume-integrated state
-                        const double inv_dv = 1.0 / (double)dV;
+                        // Pd is the (floored) primitive of the volume-integrated
+                        // state; dV is in the stage's length units
+                        const double inv_dv = a.lscale3_d / (double)dV;
                         P[0] = (float)(Pd[0] * inv_dv);
                         P[1] = (float)Pd[1];
                         P[2] = (float)Pd[2];
                         P[3] = (float)(Pd[3] * inv_dv);
                     }
                 } else {
-                    const double inv_dv = 1.0 / (double)dV;
+                    const double inv_dv = a.lscale3_d / (double)dV;
                     const double inv_et = 1.0 / (tau + m + p64);
                     const double rho = m / w64 * inv_dv;
                     P[0] = (float)rho;
@@ -175,7 +184,7 @@ struct MixedC2p {
                 a.status->err_sel = a.sel_in;
             }
             wz = sqrtf(1.0f + P[1] * P[1] + P[2] * P[2]);
-            const float v[NFIELD] = {P[0], P[1], P[2], P[3], d2f_rn(U[4]) / dV / wz};
+            const float v[NFIELD] = {P[0], P[1], P[2], P[3], d2f_rn_exp(U[4], de) / dV / wz};
             store_prim<float>(B, i, j, v);
             if (a.compute_dt && kind == HYDRO_NONE) {
                 // State::time_step (src/state.rs:151-160) on this stage's

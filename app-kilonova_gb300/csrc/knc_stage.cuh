@@ -287,7 +287,7 @@ __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, un
                     du = (sc - (fb - fa) - (fd - fc)) * dt;
                 }
                 const double uin = BOX ? boxU[(q * TR + r) * TQ + c] : Uin[q * n + z];
-                res[q] = uin + (MIXED ? f2d((float)du) : (double)du);
+                res[q] = uin + (MIXED ? f2d_exp((float)du, a.lscale2) : (double)du);
             }
             {
                 const R fa = sFr[(4 * (TR + 1) + r) * TQ + c];
@@ -301,7 +301,7 @@ __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, un
                     ds = ((fb - fa) + (fd - fc)) * -dt;
                 }
                 const double uin = BOX ? boxU[(4 * TR + r) * TQ + c] : Uin[4 * n + z];
-                res[4] = uin + (MIXED ? f2d((float)ds) : (double)ds);
+                res[4] = uin + (MIXED ? f2d_exp((float)ds, a.lscale2) : (double)ds);
             }
             if (U0) {
                 if (MIXED && a.avg_half) {
@@ -465,11 +465,11 @@ __device__ __forceinline__ void update_strip(const StageArgs& a, const int4 it, 
                 if constexpr (MIXED) sc = df_scale(src[q], cdV);
                 else sc = src[q] * cflux * dV;
                 const R du = (sc - (Fhi[q] - Flo[q]) - (Fq1[q] - Fq[q])) * dt;
-                res[q] = Uin[q * n + z] + (MIXED ? f2d((float)du) : (double)du);
+                res[q] = Uin[q * n + z] + (MIXED ? f2d_exp((float)du, a.lscale2) : (double)du);
             }
             {
                 const R ds = ((Fhi[4] - Flo[4]) + (Fq1[4] - Fq[4])) * -dt;
-                res[4] = Uin[4 * n + z] + (MIXED ? f2d((float)ds) : (double)ds);
+                res[4] = Uin[4 * n + z] + (MIXED ? f2d_exp((float)ds, a.lscale2) : (double)ds);
             }
             if (U0) {
                 if (MIXED && a.avg_half) {

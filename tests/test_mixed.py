@@ -117,3 +117,28 @@ def test_mixed_adaptive_dt_in_the_fold():
     assert abs(tm - t64) <= 1e-5 * t64
     errs = field_errors(gm.state(), g64.state())
     assert errs[0] <= 1e-4, errs
+
+
+def test_mixed_in_cgs_units():
+    """The reference's setups are in cgs (radii 1e8-1e19 cm, densities down to
+    1e-20 g/cm^3): the mixed stage works in a power-of-two length unit near
+    the reference radius and recovers per unit mass, so the same wind at
+    r ~ 1e18 cm and rho ~ 1e-20 stays as close to the FP64 path as in code
+    units."""
+    import dataclasses
+    import knc
+    from helpers import field_errors, make_pair
+    from knc import workloads
+    w = workloads.wind_small()
+    w.mesh = dataclasses.replace(w.mesh, reference_radius=1e18, inner_radius=1e18, outer_radius=1e19)
+    w.model = dataclasses.replace(w.model, rho0=1e16)
+    g64, _ = make_pair(w, gpu=True)
+    gm, _ = make_pair(w, gpu=True)
+    gm.set_precision(knc.abi.KNC_PRECISION_MIXED)
+    for _ in range(4):
+        g64.advance(5)
+        gm.advance(5)
+    st = gm.state()
+    assert all(np.isfinite(c).all() and np.isfinite(s).all() for c, s in st.values())
+    errs = field_errors(st, g64.state(), momentum_scale=True)
+    assert max(errs) <= 1e-5, errs
