@@ -236,6 +236,8 @@ struct Layout {
     int utr = 0;
     int uform = -1;
     int64_t nzones = 0;         // zones of the block set
+    int2* d_high = nullptr;     // mixed recovery: zones deferred to the dense FP64 pass
+    int64_t high_cap = 0;
     TmaMaps* d_tmaps = nullptr; // tensor maps per slot (tiles of `utr` rows), when every block allows them
     int tmaps_cap = 0;
     bool tma_ok = false;
@@ -271,6 +273,7 @@ void free_layout(Layout& l) {
     cudaFree(l.d_tiles);
     cudaFree(l.d_utiles);
     cudaFree(l.d_chunks);
+    cudaFree(l.d_high);
     cudaFree(l.d_strips);
     cudaFree(l.d_tmaps);
     cudaFree(l.d_remap);
@@ -331,6 +334,7 @@ struct knc_ctx {
     int32_t utr = 8;   // update tile rows (4, 8 or 16)
     int32_t fused = 0;         // one cooperative launch per stage
     int32_t uform = KNC_UPDATE_TILE;   // update form of the separate stage
+    int32_t rform = KNC_RECOVERY_INLINE;   // mixed recovery form of the separate stage
     int32_t ctas_per_sm = 0;   // fused grid: CTAs per SM (0: the occupancy bound)
     int32_t sms = 0;
     bool coop = false;         // the device supports cooperative launches
@@ -691,6 +695,12 @@ int rebuild_table(knc_ctx* c) {
     L(c).nstrips = (int)strips.size();
     L(c).uform = c->uform;
     L(c).nzones = zoff;
+    if (zoff > L(c).high_cap) {
+        cudaFree(L(c).d_high);
+        L(c).d_high = nullptr;
+        CK(dalloc(&L(c).d_high, (size_t)zoff));
+        L(c).high_cap = zoff;
+    }
     L(c).tma_ok = false;
     if (tma_ok) {
         if (nb > L(c).tmaps_cap) {
@@ -970,6 +980,12 @@ int run_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, doub
     a.dt = dt;
     a.dt_f = (float)dt;
     a.avg_half = w1 == 0.5 && bf == 0.5 ? 1 : 0;
+    if (mixed(c) && !c->fused && c->rform == KNC_RECOVERY_DEFERRED && L(c).d_high) {
+        a.high = L(c).d_high;
+        a.high_count = &c->d_status->high_count[stage & 1];
+        a.high_count_next = &c->d_status->high_count[(stage + 1) & 1];
+        a.high_cap = (unsigned)L(c).high_cap;
+    }
     if (c->ddt) {
         a.dt_bits = &c->d_status->dt_bits;
         a.cfl = c->hp.cfl_number;
@@ -1171,6 +1187,8 @@ int reset_status(knc_ctx* c, bool keep_stats) {
     s.dt_bits = ~0ull;
     s.bar_count = 0;
     s.bar_abort = 0;
+    s.high_count[0] = 0;
+    s.high_count[1] = 0;
     c->bar_epoch = 0;
     CK(cudaMemcpyAsync(c->d_status, &s, sizeof(s), cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -1972,6 +1990,8 @@ int knc_set_tuning(knc_ctx* c, const knc_tuning* t) {
     if (strip && c->mesh.p.num_polar_zones == 1)
         return set_msg(c, KNC_ERR_UNSUPPORTED, "warp strips need num_polar_zones > 1");
     if (t->ctas_per_sm < 0) return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "ctas_per_sm must be >= 0");
+    if (t->recovery_form != KNC_RECOVERY_INLINE && t->recovery_form != KNC_RECOVERY_DEFERRED)
+        return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "unknown recovery form %d", t->recovery_form);
     if (t->fused && !c->coop)
         return set_msg(c, KNC_ERR_UNSUPPORTED, "the device has no cooperative launch (fused stage)");
     c->utr = t->tile_rows;
@@ -1979,6 +1999,7 @@ int knc_set_tuning(knc_ctx* c, const knc_tuning* t) {
     c->ctas_per_sm = t->ctas_per_sm;
     // the fused stage stages its tiles itself (no tensor-copy form)
     c->uform = t->fused && t->update_form == KNC_UPDATE_TILE_TMA ? KNC_UPDATE_TILE : t->update_form;
+    c->rform = t->recovery_form;
     return KNC_OK;
 }
 
@@ -1988,6 +2009,7 @@ int knc_get_tuning(const knc_ctx* c, knc_tuning* t) {
     t->fused = c->fused;
     t->ctas_per_sm = c->ctas_per_sm;
     t->update_form = c->uform;
+    t->recovery_form = c->rform;
     return KNC_OK;
 }
 
@@ -2002,7 +2024,7 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
     if ((r = time_step_impl(c, &dt))) return r;
     DevStatus saved;
     CK(cudaMemcpy(&saved, c->d_status, sizeof(saved), cudaMemcpyDeviceToHost));
-    const knc_tuning keep = {c->utr, c->fused, c->ctas_per_sm, c->uform};
+    const knc_tuning keep = {c->utr, c->fused, c->ctas_per_sm, c->uform, c->rform};
     std::vector<knc_tuning> cands;
     if (c->mesh.p.num_polar_zones > 1)
         for (int sr : {4, 8, 16, 32, 64})
@@ -2036,11 +2058,17 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
     double best_ms = -1.0;
     const bool prof = c->profiling;
     c->profiling = false;
-    for (const knc_tuning& t : cands) {
+    // the launch shapes with inline recovery, then (mixed, separate) the best
+    // of them with the deferred dense recovery
+    for (size_t ci = 0; ci < cands.size(); ++ci) {
+        const knc_tuning t = cands[ci];
         c->utr = t.tile_rows;
         c->fused = t.fused;
         c->ctas_per_sm = t.ctas_per_sm;
         c->uform = t.update_form;
+        c->rform = t.recovery_form;
+        // a fresh start for the deferred-recovery counters of every candidate
+        CK(cudaMemsetAsync(c->d_status->high_count, 0, sizeof(c->d_status->high_count), c->stream));
         if ((r = rebuild_table(c))) break;
         if (t.update_form == KNC_UPDATE_TILE_TMA && !L(c).tma_ok) continue;
         // the first stage reads buf[cur] and writes buf[1 - cur]: the state stays
@@ -2059,12 +2087,19 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
             best = t;
         }
         c->stage_counter = 0;
+        if (ci + 1 == cands.size() && mixed(c) && !best.fused && best.recovery_form == KNC_RECOVERY_INLINE) {
+            knc_tuning d = best;
+            d.recovery_form = KNC_RECOVERY_DEFERRED;
+            cands.push_back(d);
+        }
     }
     c->profiling = prof;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     saved.bar_count = 0;
     saved.bar_abort = 0;
+    saved.high_count[0] = 0;
+    saved.high_count[1] = 0;
     CK(cudaMemcpy(c->d_status, &saved, sizeof(saved), cudaMemcpyHostToDevice));
     c->stage_counter = 0;
     c->bar_epoch = 0;
@@ -2072,6 +2107,7 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
     c->fused = best.fused;
     c->ctas_per_sm = best.ctas_per_sm;
     c->uform = best.update_form;
+    c->rform = best.recovery_form;
     if (r) {
         c->failed = false;
         return r;

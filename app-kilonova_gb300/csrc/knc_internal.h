@@ -89,6 +89,7 @@ struct DevStatus {
     unsigned long long bar_count;   // grid-barrier arrivals of fused launches since the last reset
     int32_t bar_abort;              // a grid barrier gave up waiting
     int32_t pad2;
+    unsigned high_count[2];         // deferred FP64 recoveries, by stage parity
 };
 
 struct StageArgs {
@@ -128,6 +129,11 @@ struct StageArgs {
     // and recovered densities use volumes in L^3
     int32_t lscale2, lscale3;   // 2e, 3e
     double lscale3_d;           // 2^(-3e)
+    // mixed recovery, separate form: zones deferred to the dense FP64 pass
+    int2* high;                 // {slot, z}, capacity = zones of the layout, or null
+    unsigned* high_count;       // this stage's count (status word, by stage parity)
+    unsigned* high_count_next;  // the next stage's, cleared by the dense pass
+    unsigned high_cap;          // entries a.high holds
     int32_t avg_half;       // w1 == bf == 1/2 (the RK2 average, halved exactly on the integer pipe)
     const float* mlp;       // packed MLP weights (device) or null
     DevStatus* status;

@@ -75,8 +75,11 @@ static __device__ __noinline__ float mlp_guess_call(const MlpWeights& W, __nv_bf
 constexpr int TMA_WAIT_LIMIT = 1 << 22;   // mbarrier polls before a copy counts as lost
 
 // Recovery of one zone; every thread of a warp calls zone() together (the
-// learned guess is a warp-wide inference).
-template <bool MLP>
+// learned guess is a warp-wide inference). DEFER: zones whose Lorentz factor
+// needs the FP64 recovery are appended to the stage's list (a.high) and left
+// to c2p_high_kernel, which runs them densely with the learned guess; every
+// zone still meets the same arithmetic.
+template <bool MLP, bool DEFER = false>
 struct MixedC2p {
     static constexpr bool mlp = MLP;
     __device__ static void zone(const StageArgs& a, int slot, const DevBlock& B, int i, int j, bool active,
@@ -113,6 +116,22 @@ struct MixedC2p {
         const float ssn = s1n * s1n + s2n * s2n;
         const float x1 = __fdividef(sqrtf(ssn), 1.0f + taun);   // |S| / (D + tau)
         const bool high = active && kind == HYDRO_NONE && x1 * x1 > high_thr;
+        if (DEFER) {
+            const unsigned full = 0xffffffffu;
+            const unsigned mask = __ballot_sync(full, high);
+            if (mask) {
+                const int lane = threadIdx.x & 31;
+                unsigned base = 0;
+                if (lane == __ffs(mask) - 1) base = atomicAdd(a.high_count, (unsigned)__popc(mask));
+                base = __shfl_sync(full, base, __ffs(mask) - 1);
+                const unsigned slot_k = base + __popc(mask & ((1u << lane) - 1u));
+                // a full list (never reached: capacity = zones) keeps the zone here
+                if (high && slot_k < a.high_cap) {
+                    a.high[slot_k] = make_int2(slot, (int)z);
+                    return;
+                }
+            }
+        }
         float guess = 0.0f;   // p / m
         if (MLP) {
             if (__any_sync(0xffffffffu, high)) {
@@ -120,7 +139,9 @@ struct MixedC2p {
                 const bool ok = mlp_features(m, U[1] * U[1] + U[2] * U[2], tau, x);
                 const float y = mlp_guess_call(W, act, x[0], x[1], x[2]);
                 const float gsv = __expf(y);
-                guess = (ok && gsv > 0.0f) ? fminf(gsv, (gmf - 1.0f) * taun) : 0.0f;
+                // the learned start is for the zones that go on to the FP64
+                // recovery; the others start from the plain guess
+                guess = (high && ok && gsv > 0.0f) ? fminf(gsv, (gmf - 1.0f) * taun) : 0.0f;
             }
         }
         float P[4] = {0.f, 0.f, 0.f, 0.f};
@@ -206,7 +227,7 @@ struct MixedC2p {
     }
 };
 
-template <bool MLP>
+template <bool MLP, bool DEFER = false>
 __global__ void __launch_bounds__(TILE_THREADS, 3) c2p_mixed_kernel(StageArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
@@ -224,7 +245,41 @@ __global__ void __launch_bounds__(TILE_THREADS, 3) c2p_mixed_kernel(StageArgs a)
         const DevBlock& B = a.blocks[t.x];
         const int i = t.y + threadIdx.x / TILE_Q;
         const int j = t.z + threadIdx.x % TILE_Q;
-        MixedC2p<MLP>::zone(a, t.x, B, i, j, i < B.nr && j < B.nq, W, act, st);
+        MixedC2p<MLP, DEFER>::zone(a, t.x, B, i, j, i < B.nr && j < B.nq, W, act, st);
+    }
+    warp_reduce_stats(a.status, st.zones, st.it64, st.it32, st.fbs, st.dtz, a.compute_dt != 0);
+}
+
+// The deferred zones of this stage ({slot, z} in a.high, *a.high_count of
+// them): warps take 32 at a time, so the learned guess and the FP64 recovery
+// run on full warps. Clears the other stage parity's counter for the next
+// stage (its last reader finished before this launch).
+template <bool MLP>
+__global__ void __launch_bounds__(TILE_THREADS, 2) c2p_high_kernel(StageArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.high_count_next = 0u;
+    if (ek != NO_ERROR && (uint32_t)(ek >> 48) < (uint32_t)a.stage) return;
+    const unsigned count = min(*(volatile unsigned*)a.high_count, a.high_cap);
+    if (count == 0u) return;
+    MlpWeights& W = *reinterpret_cast<MlpWeights*>(smem_raw);
+    __nv_bfloat16* act = reinterpret_cast<__nv_bfloat16*>(smem_raw + sizeof(MlpWeights)) +
+                         (threadIdx.x >> 5) * MLP_ACT_ELEMS;
+    if (MLP) {
+        mlp_load(W, a.mlp);
+        __syncthreads();
+    }
+    C2pStats st;
+    const unsigned warps = gridDim.x * (TILE_THREADS / 32);
+    const unsigned lane = threadIdx.x & 31;
+    for (unsigned base = (blockIdx.x * (TILE_THREADS / 32) + (threadIdx.x >> 5)) * 32; base < count;
+         base += warps * 32) {
+        const unsigned k = base + lane;
+        const bool active = k < count;
+        const int2 e = a.high[active ? k : base];
+        const DevBlock& B = a.blocks[e.x];
+        const int i = e.y / B.nq, j = e.y - i * B.nq;
+        MixedC2p<MLP>::zone(a, e.x, B, i, j, active, W, act, st);
     }
     warp_reduce_stats(a.status, st.zones, st.it64, st.it32, st.fbs, st.dtz, a.compute_dt != 0);
 }
@@ -266,6 +321,18 @@ static int resident_grid(K kernel, int threads, size_t smem) {
 
 cudaError_t launch_c2p_mixed(const StageArgs& a, cudaStream_t s) {
     if (a.ntiles <= 0) return cudaSuccess;
+    if (a.high) {
+        // every zone in FP32; the ones that need the FP64 recovery, densely after
+        const int grid = std::min(a.ntiles, resident_grid(c2p_mixed_kernel<false, true>, TILE_THREADS, 0));
+        c2p_mixed_kernel<false, true><<<grid, TILE_THREADS, 0, s>>>(a);
+        if (a.mlp) {
+            const size_t bytes = sizeof(MlpWeights) + 8 * MLP_ACT_ELEMS * sizeof(__nv_bfloat16);
+            c2p_high_kernel<true><<<num_sms(), TILE_THREADS, bytes, s>>>(a);
+        } else {
+            c2p_high_kernel<false><<<num_sms(), TILE_THREADS, 0, s>>>(a);
+        }
+        return cudaGetLastError();
+    }
     if (a.mlp) {
         const size_t bytes = sizeof(MlpWeights) + 8 * MLP_ACT_ELEMS * sizeof(__nv_bfloat16);
         const int grid = std::min(a.ntiles, resident_grid(c2p_mixed_kernel<true>, TILE_THREADS, bytes));
@@ -469,6 +536,9 @@ cudaError_t configure_kernels() {
     if (e == cudaSuccess) e = configure_update_mixed<4>();
     if (e == cudaSuccess) e = configure_update_mixed<8>();
     if (e == cudaSuccess) e = configure_update_mixed<16>();
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(c2p_high_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(MlpWeights) + 8 * MLP_ACT_ELEMS * sizeof(__nv_bfloat16)));
     if (e == cudaSuccess) e = configure_fused_mixed<4, false>();
     if (e == cudaSuccess) e = configure_fused_mixed<8, false>();
     if (e == cudaSuccess) e = configure_fused_mixed<16, false>();

@@ -55,6 +55,8 @@ KNC_KERNEL_FUSED = 3
 KNC_UPDATE_TILE = 0
 KNC_UPDATE_TILE_TMA = 1
 KNC_UPDATE_STRIP = 2
+KNC_RECOVERY_INLINE = 0
+KNC_RECOVERY_DEFERRED = 1
 KNC_KERNEL_KINDS = 4
 
 KNC_MLP_HIDDEN = 64
@@ -130,7 +132,7 @@ class Error(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("tile_rows", C.c_int32), ("fused", C.c_int32), ("ctas_per_sm", C.c_int32),
-                ("update_form", C.c_int32)]
+                ("update_form", C.c_int32), ("recovery_form", C.c_int32)]
 
 
 class MlpTrainParams(C.Structure):

@@ -106,19 +106,20 @@ class Solver:
         self._check(self.lib.knc_set_batched(self.h, int(bool(graph))), "set_batched")
 
     def set_tuning(self, tile_rows: int = 8, fused: bool = False, ctas_per_sm: int = 0, tma: bool = False,
-                   strip: bool = False):
+                   strip: bool = False, deferred: bool = False):
         """Launch shape: update tiles of tile_rows rows (tma: staged by tensor
         copies), warp strips of tile_rows rows (strip), or the fused stage."""
         form = abi.KNC_UPDATE_STRIP if strip else abi.KNC_UPDATE_TILE_TMA if tma else abi.KNC_UPDATE_TILE
         t = abi.Tuning(tile_rows=int(tile_rows), fused=int(bool(fused)), ctas_per_sm=int(ctas_per_sm),
-                       update_form=form)
+                       update_form=form, recovery_form=int(bool(deferred)))
         self._check(self.lib.knc_set_tuning(self.h, C.byref(t)), "set_tuning")
 
     def tuning(self) -> dict:
         t = abi.Tuning()
         self._check(self.lib.knc_get_tuning(self.h, C.byref(t)), "get_tuning")
         return {"tile_rows": t.tile_rows, "fused": bool(t.fused), "ctas_per_sm": t.ctas_per_sm,
-                "tma": t.update_form == abi.KNC_UPDATE_TILE_TMA, "strip": t.update_form == abi.KNC_UPDATE_STRIP}
+                "tma": t.update_form == abi.KNC_UPDATE_TILE_TMA, "strip": t.update_form == abi.KNC_UPDATE_STRIP,
+                "deferred": t.recovery_form == abi.KNC_RECOVERY_DEFERRED}
 
     def autotune(self, reps: int = 5):
         """Time every launch shape on the live state, keep the fastest; returns
@@ -127,7 +128,8 @@ class Solver:
         ms = C.c_double()
         self._check(self.lib.knc_autotune(self.h, int(reps), C.byref(t), C.byref(ms)), "autotune")
         return {"tile_rows": t.tile_rows, "fused": bool(t.fused), "ctas_per_sm": t.ctas_per_sm,
-                "tma": t.update_form == abi.KNC_UPDATE_TILE_TMA, "strip": t.update_form == abi.KNC_UPDATE_STRIP}, ms.value
+                "tma": t.update_form == abi.KNC_UPDATE_TILE_TMA, "strip": t.update_form == abi.KNC_UPDATE_STRIP,
+                "deferred": t.recovery_form == abi.KNC_RECOVERY_DEFERRED}, ms.value
 
     def zone_updates(self) -> int:
         n = C.c_int64()

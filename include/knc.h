@@ -262,7 +262,13 @@ typedef struct knc_tuning {
     int32_t fused;
     int32_t ctas_per_sm;
     int32_t update_form;
+    int32_t recovery_form;   /* mixed, separate form: KNC_RECOVERY_* */
 } knc_tuning;
+/* KNC_RECOVERY_INLINE: each warp recovers its zones, the FP64 ones among
+ * them in place; KNC_RECOVERY_DEFERRED: zones that need the FP64 recovery
+ * are listed and recovered afterwards on full warps (with the learned guess)
+ * by a second launch. Same bits either way. */
+enum { KNC_RECOVERY_INLINE = 0, KNC_RECOVERY_DEFERRED = 1 };
 int knc_set_tuning(knc_ctx* ctx, const knc_tuning* tuning);
 int knc_get_tuning(const knc_ctx* ctx, knc_tuning* tuning);
 /* Autotuner: times every candidate shape (tile rows x separate / fused x CTAs

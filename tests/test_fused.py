@@ -253,3 +253,31 @@ def test_fused_strips_match(rows):
     for _ in range(2):
         m.advance(3)
     assert _same(m.state(), ref.state())
+
+
+@pytest.mark.parametrize("learned", [False, True])
+def test_mixed_deferred_recovery_matches_inline(learned):
+    """Zones that need the FP64 recovery, listed and recovered on full warps by
+    a second launch, give the bits of the in-place recovery (the W = 100 jet
+    has such zones in its nozzle)."""
+    import knc
+    from knc import learned as L, workloads
+    wts = None
+    if learned:
+        wts = L.init_weights(seed=3)
+        wts[-6:-3] = 0.0
+        wts[-3:] = 1.0
+    w = workloads.jet_small()
+    runs = []
+    for deferred in (False, True):
+        g, _ = make_pair(w, gpu=True)
+        g.set_precision(knc.abi.KNC_PRECISION_MIXED)
+        if wts is not None:
+            g.set_c2p_guess(knc.abi.KNC_GUESS_MLP, wts)
+        g.set_tuning(tile_rows=8, strip=True, deferred=deferred)
+        g.reset_c2p_stats()
+        g.advance(6)
+        runs.append(g)
+    assert runs[1].c2p_stats()["iters_fp64"] > 0
+    assert runs[0].c2p_stats() == runs[1].c2p_stats()
+    assert _same(runs[0].state(), runs[1].state())
