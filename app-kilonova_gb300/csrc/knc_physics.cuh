@@ -332,14 +332,104 @@ __device__ __forceinline__ void srhd_side_f32(const PhysT<float>& ph, float rho,
     S.pre = pre;
 }
 
+// Both sides of a face at once, on Blackwell's paired FP32 units: every
+// product, sum and fused multiply-add of srhd_side_f32 runs on the (left,
+// right) pair as one instruction (__fmul2_rn / __fadd2_rn / __ffma2_rn, each
+// lane rounded like its scalar form); reciprocals and square roots stay
+// per lane.
+__device__ __forceinline__ float2 pair(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 bcast(float a) { return make_float2(a, a); }
+
+template <int AXIS>
+__device__ __forceinline__ void srhd_sides_f32x2(const PhysT<float>& ph, const float* pl, const float* pr, float sl,
+                                                 float sr, Side<float>& L, Side<float>& R) {
+    const float2 one = bcast(1.0f), mone = bcast(-1.0f);
+    const float2 rho = pair(pl[0], pr[0]), ur = pair(pl[1], pr[1]), uq = pair(pl[2], pr[2]);
+    const float2 pre = pair(pl[3], pr[3]), s = pair(sl, sr);
+    const float2 uu = __ffma2_rn(ur, ur, __fmul2_rn(uq, uq));
+    const float2 w2 = __fadd2_rn(one, uu);
+    const float2 iw = pair(rsqrtf(w2.x), rsqrtf(w2.y));
+    const float2 w = __fmul2_rn(w2, iw);
+    const float2 prr = __fmul2_rn(pre, pair(1.0f / rho.x, 1.0f / rho.y));   // p / rho
+    const float2 h = __ffma2_rn(prr, bcast(ph.gh), one);
+    const float2 d = __fmul2_rn(rho, w);
+    const float2 m = __fmul2_rn(d, h);
+    const float2 un = AXIS == 0 ? ur : uq;
+    const float2 ut = AXIS == 0 ? uq : ur;
+    const float2 vn = __fmul2_rn(un, iw);
+    const float2 U1 = __fmul2_rn(m, ur), U2 = __fmul2_rn(m, uq);
+    const float2 cs2 = __fmul2_rn(__fmul2_rn(bcast(ph.gm), prr), pair(1.0f / h.x, 1.0f / h.y));
+    const float2 omv2 = __fmul2_rn(iw, iw);                                  // 1 - v^2
+    const float2 v2 = __fmul2_rn(uu, omv2);
+    const float2 k = __ffma2_rn(cs2, mone, one);                            // 1 - cs^2
+    const float2 a = __fmul2_rn(vn, k);
+    const float2 wp1 = __fadd2_rn(w, one);
+    // tau without cancellation: p (gh W^2 - 1) + D u^2 / (W + 1)
+    const float2 U3 = __ffma2_rn(pre, __ffma2_rn(bcast(ph.gh), w2, mone),
+                                 __fmul2_rn(__fmul2_rn(d, uu), pair(1.0f / wp1.x, 1.0f / wp1.y)));
+    const float2 inner = __ffma2_rn(__fmul2_rn(__fmul2_rn(ut, ut), omv2), k, omv2);
+    const float2 barg = __fmul2_rn(__fmul2_rn(cs2, omv2), inner);
+    const float2 b = pair(sqrtf(barg.x), sqrtf(barg.y));
+    const float2 F0 = __fmul2_rn(d, vn);
+    const float2 F1 = AXIS == 0 ? __ffma2_rn(U1, vn, pre) : __fmul2_rn(U1, vn);
+    const float2 F2 = AXIS == 1 ? __ffma2_rn(U2, vn, pre) : __fmul2_rn(U2, vn);
+    const float2 F3 = __fmul2_rn(__fadd2_rn(U3, pre), vn);
+    const float2 den = __ffma2_rn(__fmul2_rn(v2, cs2), mone, one);           // 1 - v^2 cs^2
+    const float2 inv = pair(1.0f / den.x, 1.0f / den.y);
+    const float2 lm = __fmul2_rn(__ffma2_rn(b, mone, a), inv);
+    const float2 lp = __fmul2_rn(__fadd2_rn(a, b), inv);
+    const float2 sU = __fmul2_rn(s, w), sF = __fmul2_rn(s, un);
+    L.U[0] = d.x; R.U[0] = d.y;
+    L.U[1] = U1.x; R.U[1] = U1.y;
+    L.U[2] = U2.x; R.U[2] = U2.y;
+    L.U[3] = U3.x; R.U[3] = U3.y;
+    L.F[0] = F0.x; R.F[0] = F0.y;
+    L.F[1] = F1.x; R.F[1] = F1.y;
+    L.F[2] = F2.x; R.F[2] = F2.y;
+    L.F[3] = F3.x; R.F[3] = F3.y;
+    L.lm = lm.x; R.lm = lm.y;
+    L.lp = lp.x; R.lp = lp.y;
+    L.sU = sU.x; R.sU = sU.y;
+    L.sF = sF.x; R.sF = sF.y;
+    L.vn = vn.x; R.vn = vn.y;
+    L.pre = pre.x; R.pre = pre.y;
+}
+
+// HLLE on paired fields (D, S_r), (S_theta, tau) and the scalar alone.
+__device__ __forceinline__ void hlle_f32x2(const Side<float>& L, const Side<float>& R, float out[5]) {
+    const float am = fminf(L.lm, R.lm);
+    const float ap = fmaxf(L.lp, R.lp);
+    if (am >= 0.0f) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) out[q] = L.F[q];
+        out[4] = L.sF;
+    } else if (ap <= 0.0f) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) out[q] = R.F[q];
+        out[4] = R.sF;
+    } else {
+        const float inv = 1.0f / (ap - am);
+        const float apam = ap * am;
+        const float2 AP = bcast(ap), MAM = bcast(-am), APAM = bcast(apam), INV = bcast(inv);
+#pragma unroll
+        for (int q = 0; q < 4; q += 2) {
+            const float2 fl = pair(L.F[q], L.F[q + 1]), fr = pair(R.F[q], R.F[q + 1]);
+            const float2 du = __fadd2_rn(pair(R.U[q], R.U[q + 1]), __fmul2_rn(pair(L.U[q], L.U[q + 1]), bcast(-1.0f)));
+            const float2 o = __fmul2_rn(__ffma2_rn(APAM, du, __ffma2_rn(MAM, fr, __fmul2_rn(AP, fl))), INV);
+            out[q] = o.x;
+            out[q + 1] = o.y;
+        }
+        out[4] = (ap * L.sF - am * R.sF + apam * (R.sU - L.sU)) * inv;
+    }
+}
+
 template <int AXIS>
 __device__ __forceinline__ void riemann_srhd_f32(const PhysT<float>& ph, const float* pl, const float* pr,
                                                  float sl, float sr, float out[5]) {
     Side<float> L, Rr;
-    srhd_side_f32<AXIS>(ph, pl[0], pl[1], pl[2], pl[3], sl, L);
-    srhd_side_f32<AXIS>(ph, pr[0], pr[1], pr[2], pr[3], sr, Rr);
+    srhd_sides_f32x2<AXIS>(ph, pl, pr, sl, sr, L, Rr);
     if (ph.hllc) srhd_hllc(L, Rr, AXIS, out);
-    else hlle(L, Rr, out);
+    else hlle_f32x2(L, Rr, out);
 }
 
 // Geometric sources per unit volume for the FP32 relativistic stage: the
