@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -1648,40 +1649,58 @@ int knc_block_shape_of(const knc_ctx* c, int32_t index, int64_t* nr, int64_t* nq
     return KNC_OK;
 }
 
+// The device address of host memory the GPU can read and write directly
+// (page-locked or registered; over NVLink-C2C on a Grace host), else null.
+const void* device_view(const void* p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type == cudaMemoryTypeHost && at.devicePointer) return at.devicePointer;
+    if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) return p;
+    return nullptr;
+}
+
 int knc_set_state(knc_ctx* c, const double* cons, const double* scalar) {
     if (!c || !cons || !scalar) return KNC_ERR_INVALID_ARGUMENT;
+    int r;
+    if ((r = rebuild_table(c))) return r;
     int64_t total = 0;
     for (auto& kv : c->blocks) total += kv.second.nr * kv.second.nq;
-    int r;
-    if ((r = ensure_stage(c, 5 * (size_t)total))) return r;
-    CK(cudaMemcpyAsync(c->d_stage, cons, 4 * total * 8, cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemcpyAsync(c->d_stage + 4 * total, scalar, total * 8, cudaMemcpyHostToDevice, c->stream));
-    int64_t off = 0;
-    for (auto& kv : c->blocks) {
-        BlockH& b = kv.second;
-        CK(launch_aos_to_soa(c->d_stage + 4 * off, c->d_stage + 4 * total + off, b.buf[c->cur], b.nr, b.nq,
-                             c->stream));
-        ++c->launches;
-        off += b.nr * b.nq;
+    const double* dc = static_cast<const double*>(device_view(cons));
+    const double* ds = static_cast<const double*>(device_view(scalar));
+    if (!dc || !ds) {
+        // pageable host memory: through a device staging copy
+        if ((r = ensure_stage(c, 5 * (size_t)total))) return r;
+        CK(cudaMemcpyAsync(c->d_stage, cons, 4 * total * 8, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(c->d_stage + 4 * total, scalar, total * 8, cudaMemcpyHostToDevice, c->stream));
+        dc = c->d_stage;
+        ds = c->d_stage + 4 * total;
     }
+    // one launch reads the arrays (directly from page-locked host memory when
+    // it can: on GB300 that beat a DMA copy plus transpose, 0.81 vs 0.87 ms
+    // for 168 MB) and writes every block's SoA state
+    CK(launch_state_in(L(c).d_table, L(c).d_tiles, L(c).ntiles, c->cur, dc, ds, c->stream));
+    ++c->launches;
+    // the caller's buffers are free again when the call returns
+    CK(cudaStreamSynchronize(c->stream));
     c->failed = false;
     return KNC_OK;
 }
 
 int knc_get_state(knc_ctx* c, double* cons, double* scalar) {
     if (!c || !cons || !scalar) return KNC_ERR_INVALID_ARGUMENT;
+    int r;
+    if ((r = rebuild_table(c))) return r;
     int64_t total = 0;
     for (auto& kv : c->blocks) total += kv.second.nr * kv.second.nq;
-    int r;
+    // transposed on the device, then one DMA copy per array: measured on
+    // GB300, writing host memory from a kernel is slower than the copy engines
     if ((r = ensure_stage(c, 5 * (size_t)total))) return r;
-    int64_t off = 0;
-    for (auto& kv : c->blocks) {
-        BlockH& b = kv.second;
-        CK(launch_soa_to_aos(b.buf[c->cur], c->d_stage + 4 * off, c->d_stage + 4 * total + off, b.nr, b.nq,
-                             c->stream));
-        ++c->launches;
-        off += b.nr * b.nq;
-    }
+    CK(launch_state_out(L(c).d_table, L(c).d_tiles, L(c).ntiles, c->cur, c->d_stage, c->d_stage + 4 * total,
+                        c->stream));
+    ++c->launches;
     CK(cudaMemcpyAsync(cons, c->d_stage, 4 * total * 8, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(scalar, c->d_stage + 4 * total, total * 8, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));

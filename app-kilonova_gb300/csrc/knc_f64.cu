@@ -199,6 +199,45 @@ __global__ void soa_to_aos_kernel(const double* __restrict__ soa, double* __rest
     scalar[z] = soa[4 * n + z];
 }
 
+// The whole state <-> the ABI's arrays (blocks in slot order, each
+// [nr][nq][4] then [nr][nq] scalar mass), one launch over the recovery tiles
+// (t.w = the block's first zone in the whole-state arrays). The host arrays
+// may be page-locked host memory read or written directly over the
+// CPU-GPU link, or a device staging copy.
+__global__ void __launch_bounds__(TILE_THREADS) state_in_kernel(const DevBlock* __restrict__ blocks,
+                                                               const int4* __restrict__ tiles, int sel,
+                                                               const double* __restrict__ cons,
+                                                               const double* __restrict__ scalar) {
+    const int4 t = tiles[blockIdx.x];
+    const DevBlock& B = blocks[t.x];
+    const int i = t.y + threadIdx.x / TILE_Q, j = t.z + threadIdx.x % TILE_Q;
+    if (i >= B.nr || j >= B.nq) return;
+    const int64_t n = (int64_t)B.nr * B.nq, z = (int64_t)i * B.nq + j, g = (int64_t)t.w + z;
+    const double2 a = reinterpret_cast<const double2*>(cons)[2 * g];
+    const double2 b = reinterpret_cast<const double2*>(cons)[2 * g + 1];
+    double* U = B.buf[sel];
+    U[z] = a.x;
+    U[n + z] = a.y;
+    U[2 * n + z] = b.x;
+    U[3 * n + z] = b.y;
+    U[4 * n + z] = scalar[g];
+}
+
+__global__ void __launch_bounds__(TILE_THREADS) state_out_kernel(const DevBlock* __restrict__ blocks,
+                                                                const int4* __restrict__ tiles, int sel,
+                                                                double* __restrict__ cons,
+                                                                double* __restrict__ scalar) {
+    const int4 t = tiles[blockIdx.x];
+    const DevBlock& B = blocks[t.x];
+    const int i = t.y + threadIdx.x / TILE_Q, j = t.z + threadIdx.x % TILE_Q;
+    if (i >= B.nr || j >= B.nq) return;
+    const int64_t n = (int64_t)B.nr * B.nq, z = (int64_t)i * B.nq + j, g = (int64_t)t.w + z;
+    const double* U = B.buf[sel];
+    reinterpret_cast<double2*>(cons)[2 * g] = make_double2(U[z], U[n + z]);
+    reinterpret_cast<double2*>(cons)[2 * g + 1] = make_double2(U[2 * n + z], U[3 * n + z]);
+    scalar[g] = U[4 * n + z];
+}
+
 // Interior rows of a padded double primitive array -> [nr][nq][5], with the
 // scalar density divided by rho into a concentration.
 __global__ void prims_to_aos_kernel(const double* __restrict__ P, double* __restrict__ out, int64_t nr,
@@ -343,6 +382,20 @@ cudaError_t launch_aos_to_soa(const double* aos, const double* scalar, double* s
                               cudaStream_t s) {
     const int64_t n = nr * nq;
     aos_to_soa_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(aos, scalar, soa, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_state_in(const DevBlock* blocks, const int4* tiles, int ntiles, int sel, const double* cons,
+                            const double* scalar, cudaStream_t s) {
+    if (ntiles <= 0) return cudaSuccess;
+    state_in_kernel<<<ntiles, TILE_THREADS, 0, s>>>(blocks, tiles, sel, cons, scalar);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_state_out(const DevBlock* blocks, const int4* tiles, int ntiles, int sel, double* cons,
+                             double* scalar, cudaStream_t s) {
+    if (ntiles <= 0) return cudaSuccess;
+    state_out_kernel<<<ntiles, TILE_THREADS, 0, s>>>(blocks, tiles, sel, cons, scalar);
     return cudaGetLastError();
 }
 

@@ -226,6 +226,12 @@ inline int stage_threads(int utr) { return (utr + 1) * TILE_Q; }
 // Tile rows the fused kernel is instantiated for: utr when it is a tile
 // size, else 8 (warp strips of other lengths run in a CTA of 9 warps).
 inline int fused_tr(int utr) { return utr == 4 || utr == 16 ? utr : 8; }
+// Whole state <-> ABI arrays over the recovery tiles (cons/scalar: device or
+// device-accessible host pointers).
+cudaError_t launch_state_in(const DevBlock* blocks, const int4* tiles, int ntiles, int sel, const double* cons,
+                            const double* scalar, cudaStream_t s);
+cudaError_t launch_state_out(const DevBlock* blocks, const int4* tiles, int ntiles, int sel, double* cons,
+                             double* scalar, cudaStream_t s);
 cudaError_t launch_prims_to_aos(const void* P, double* out, int64_t nr, int64_t nq, cudaStream_t s);
 cudaError_t launch_soa_to_aos(const double* soa, double* aos, double* scalar, int64_t nr, int64_t nq,
                               cudaStream_t s);

@@ -158,3 +158,31 @@ def test_adaptive_dt_found_in_the_fold():
         o.advance(3)
         assert g.time() == o.time()
         assert max(field_errors(g.state(), o.state())) <= TOL
+
+
+@pytest.mark.parametrize("name", ["wind_small", "uneven_small"])
+def test_state_roundtrip_page_locked(name):
+    """Whole-state copies through page-locked host memory, which the
+    library reads and writes directly from the device (uneven blocks: flat
+    arrays, blocks in index order with their own shapes)."""
+    import knc
+    from knc import workloads
+    w = workloads.wind_small() if name == "wind_small" else workloads.uneven_small(moving=False)
+    g, _ = make_pair(w, gpu=True)
+    idx = g.block_indexes()
+    zones = sum(int(np.prod(g.shape_of(i))) for i in idx)
+    cons = knc.solver.PinnedArray((zones, 4))
+    scal = knc.solver.PinnedArray((zones,))
+    g.get_state(cons.array, scal.array)
+    st = g.state()
+    off = 0
+    for i in idx:
+        n = int(np.prod(g.shape_of(i)))
+        assert np.array_equal(cons.array[off:off + n].reshape(st[i][0].shape), st[i][0])
+        assert np.array_equal(scal.array[off:off + n].reshape(st[i][1].shape), st[i][1])
+        off += n
+    g.advance(2)
+    g.set_state(cons.array, scal.array)     # back to the saved state
+    st2 = g.state()
+    for i in idx:
+        assert np.array_equal(st[i][0], st2[i][0]) and np.array_equal(st[i][1], st2[i][1])
