@@ -1176,23 +1176,24 @@ int check_status(knc_ctx* c) {
 }
 
 int reset_status(knc_ctx* c, bool keep_stats) {
-    DevStatus s;
+    DevStatus* d = c->d_status;
     if (keep_stats) {
-        CK(cudaMemcpyAsync(&s, c->d_status, sizeof(s), cudaMemcpyDeviceToHost, c->stream));
-        CK(cudaStreamSynchronize(c->stream));
+        // stream-ordered field writes, no round trip: the error key and dt
+        // minimum to all-ones, the barrier and deferral counters to zero
+        CK(cudaMemsetAsync(&d->err_key, 0xff, sizeof(d->err_key), c->stream));
+        CK(cudaMemsetAsync(&d->err_sel, 0, sizeof(d->err_sel), c->stream));
+        CK(cudaMemsetAsync(&d->dt_bits, 0xff, sizeof(d->dt_bits), c->stream));
+        CK(cudaMemsetAsync(&d->bar_count, 0, sizeof(d->bar_count) + sizeof(d->bar_abort), c->stream));
+        CK(cudaMemsetAsync(d->high_count, 0, sizeof(d->high_count), c->stream));
     } else {
+        DevStatus s;
         std::memset(&s, 0, sizeof(s));
+        s.err_key = NO_ERROR;
+        s.dt_bits = ~0ull;
+        CK(cudaMemcpyAsync(d, &s, sizeof(s), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
     }
-    s.err_key = NO_ERROR;
-    s.err_sel = 0;
-    s.dt_bits = ~0ull;
-    s.bar_count = 0;
-    s.bar_abort = 0;
-    s.high_count[0] = 0;
-    s.high_count[1] = 0;
     c->bar_epoch = 0;
-    CK(cudaMemcpyAsync(c->d_status, &s, sizeof(s), cudaMemcpyHostToDevice, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
     c->stage_counter = 0;
     return KNC_OK;
 }
