@@ -245,6 +245,7 @@ struct Layout {
     int4* d_strips = nullptr;   // warp strips {slot, i0, j0, rows} of `utr` rows (strip form)
     int strips_cap = 0;
     int nstrips = 0;
+    int chunk_nt = 0;           // zones per fused recovery chunk (= fused CTA threads)
     int4* d_chunks = nullptr;   // fused recovery chunks {slot, z0, nz, 0} of <= stage_threads(utr) zones
     int chunks_cap = 0;
     int nchunks = 0;
@@ -565,15 +566,23 @@ bool encode_block_maps(const BlockH& b, int tr, TmaMaps* m) {
     return true;
 }
 
+// Threads of a fused-stage CTA (and zones of its recovery chunks): the mixed
+// strip-only kernel runs CTAs of STRIP_WARPS warps, the others (TR+1) warps.
+int fused_threads(const knc_ctx* c) {
+    return c->precision == KNC_PRECISION_MIXED && c->uform == KNC_UPDATE_STRIP ? STRIP_WARPS * 32
+                                                                              : stage_threads(fused_tr(c->utr));
+}
+
 // Rebuild the device block table and the tile list after the block set changed.
 int rebuild_table(knc_ctx* c) {
-    if (!c->dirty && L(c).utr == c->utr && L(c).uform == c->uform) return KNC_OK;
+    if (!c->dirty && L(c).utr == c->utr && L(c).uform == c->uform && L(c).chunk_nt == fused_threads(c))
+        return KNC_OK;
     const int nb = (int)c->blocks.size();
     std::vector<DevBlock> tab(nb);
     std::vector<int4> tiles, utiles, chunks, strips;
     std::vector<TmaMaps> maps(nb);
     bool tma_ok = nb > 0;
-    const int nt = stage_threads(fused_tr(c->utr));
+    const int nt = fused_threads(c);
     L(c).slot_index.clear();
     int slot = 0;
     int64_t zoff = 0;
@@ -684,6 +693,7 @@ int rebuild_table(knc_ctx* c) {
         CK(cudaMemcpyAsync(L(c).d_chunks, chunks.data(), chunks.size() * sizeof(int4), cudaMemcpyHostToDevice,
                            c->stream));
     L(c).nchunks = (int)chunks.size();
+    L(c).chunk_nt = nt;
     if ((int)strips.size() > L(c).strips_cap) {
         cudaFree(L(c).d_strips);
         L(c).d_strips = nullptr;
@@ -916,12 +926,14 @@ int launch_update(knc_ctx* c, const StageArgs& a) {
 int fused_grid(knc_ctx* c) {
     int per_sm = 1;
     const bool mlp = c->guess == KNC_GUESS_MLP && c->d_mlp;
-    const cudaError_t e = mixed(c) ? fused_max_ctas_mixed(mlp, c->utr, &per_sm)
-                                   : fused_max_ctas_f64(mlp && c->hp.system == KNC_SYSTEM_RELATIVISTIC, c->utr, &per_sm);
+    const bool strip_only = mixed(c) && c->uform == KNC_UPDATE_STRIP;
+    const cudaError_t e = strip_only ? fused_strip_max_ctas_mixed(mlp, &per_sm)
+                          : mixed(c) ? fused_max_ctas_mixed(mlp, c->utr, &per_sm)
+                                     : fused_max_ctas_f64(mlp && c->hp.system == KNC_SYSTEM_RELATIVISTIC, c->utr, &per_sm);
     if (e != cudaSuccess || per_sm < 1) per_sm = 1;
     if (c->ctas_per_sm > 0 && c->ctas_per_sm < per_sm) per_sm = c->ctas_per_sm;
     const Layout& l = L(c);
-    const int nt = stage_threads(fused_tr(c->utr));
+    const int nt = fused_threads(c);
     const int need_a = (int)(2 * l.nq_edge[0] + nt - 1) / nt + (int)(2 * l.nq_edge[1] + nt - 1) / nt + l.nchunks;
     const int need_b = (int)(((int64_t)l.nremap * 2 * l.max_nq + nt - 1) / nt);
     const int need_c = l.uform == KNC_UPDATE_STRIP ? (l.nstrips + nt / 32 - 1) / (nt / 32) : l.nutiles;
@@ -2066,7 +2078,7 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
         // the fused stage with warp strips in its update phase (CTAs of 9 warps)
         int per_sm = 1;
         const bool mlp = c->guess == KNC_GUESS_MLP && c->d_mlp;
-        CK(mixed(c) ? fused_max_ctas_mixed(mlp, 8, &per_sm)
+        CK(mixed(c) ? fused_strip_max_ctas_mixed(mlp, &per_sm)
                     : fused_max_ctas_f64(mlp && c->hp.system == KNC_SYSTEM_RELATIVISTIC, 8, &per_sm));
         for (int sr : {8, 16, 32})
             for (int k = 1; k <= per_sm && k <= 8; ++k) cands.push_back({sr, 1, k, KNC_UPDATE_STRIP});

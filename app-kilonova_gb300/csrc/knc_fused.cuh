@@ -63,6 +63,11 @@ struct C2pStats {
 
 // Shared memory of the fused kernel: the update tile's arrays, then (with the
 // learned guess) the MLP weights and one activation tile per warp.
+template <bool MLP>
+constexpr size_t fused_strip_smem_bytes() {
+    return MLP ? sizeof(MlpWeights) + STRIP_WARPS * MLP_ACT_ELEMS * sizeof(__nv_bfloat16) : 0;
+}
+
 template <class R, int TR, bool MLP>
 constexpr size_t fused_smem_bytes() {
     return ((StageSmem<R, TR>::bytes + 15) / 16) * 16 +
@@ -74,12 +79,16 @@ constexpr size_t fused_smem_bytes() {
 //                               MlpWeights&, __nv_bfloat16* act, C2pStats&)
 // which every thread of a warp calls together (the learned guess is a
 // warp-wide tensor-core inference).
-template <class R, bool MIXED, int TR, class C2P>
+//
+// NT threads per CTA (the tile form needs update_threads<TR>()); STRIPS_ONLY:
+// the update phase runs warp strips only and the CTA keeps no tile arrays,
+// so small CTAs (4 warps) fit many to an SM.
+template <class R, bool MIXED, int TR, class C2P, int NT = update_threads<TR>(), bool STRIPS_ONLY = false>
 __device__ __forceinline__ void stage_fused_body(const StageArgs& a, const GhostArgs& g, const FusedArgs& f) {
-    constexpr int NT = update_threads<TR>();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int run_update;
-    MlpWeights& W = *reinterpret_cast<MlpWeights*>(smem_raw + ((StageSmem<R, TR>::bytes + 15) / 16) * 16);
+    constexpr size_t W_OFF = STRIPS_ONLY ? 0 : ((StageSmem<R, TR>::bytes + 15) / 16) * 16;
+    MlpWeights& W = *reinterpret_cast<MlpWeights*>(smem_raw + W_OFF);
     __nv_bfloat16* act = reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<unsigned char*>(&W) + sizeof(MlpWeights)) +
                          (threadIdx.x >> 5) * MLP_ACT_ELEMS;
     if (C2P::mlp) {
@@ -139,13 +148,13 @@ __device__ __forceinline__ void stage_fused_body(const StageArgs& a, const Ghost
                      *(volatile int32_t*)&a.status->bar_abort == 0;
     __syncthreads();
     if (run_update) {
-        if (a.strips) {
+        if (STRIPS_ONLY || a.strips) {
             // warp strips: every warp of the grid takes strips on its own
             constexpr int WPC = NT / 32;
             const PhysT<R> ph = make_phys<R>(a);
             for (int k = blockIdx.x * WPC + (int)(threadIdx.x >> 5); k < a.nstrips; k += gridDim.x * WPC)
                 update_strip<R, MIXED>(a, a.strips[k], ph);
-        } else {
+        } else if constexpr (!STRIPS_ONLY) {
             for (int tile = blockIdx.x; tile < a.nutiles; tile += gridDim.x) {
                 update_tile<R, MIXED, TR>(a, a.utiles[tile], smem_raw);
                 __syncthreads();

@@ -221,6 +221,8 @@ cudaError_t launch_stage_fused_mixed(const StageArgs& a, const GhostArgs& g, con
 // Resident CTAs per SM of the fused kernel for (precision, learned guess, tile rows).
 cudaError_t fused_max_ctas_f64(bool mlp, int utr, int* per_sm);
 cudaError_t fused_max_ctas_mixed(bool mlp, int utr, int* per_sm);
+// The mixed fused stage with warp strips only (CTAs of STRIP_WARPS warps).
+cudaError_t fused_strip_max_ctas_mixed(bool mlp, int* per_sm);
 // Threads of a fused / update CTA for tile rows utr.
 inline int stage_threads(int utr) { return (utr + 1) * TILE_Q; }
 // Tile rows the fused kernel is instantiated for: utr when it is a tile

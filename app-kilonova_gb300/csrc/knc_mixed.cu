@@ -497,9 +497,41 @@ static cudaError_t fused_mixed(const StageArgs& a, const GhostArgs& g, const Fus
     return cudaLaunchKernelEx(&cfg, stage_fused_mixed_kernel<TR, MLP>, a, g, f);
 }
 
+// The fused stage with warp strips only: CTAs of 4 warps, recovery chunks of
+// 128 zones.
+template <bool MLP>
+__global__ void __launch_bounds__(STRIP_WARPS * 32, 5)
+    stage_fused_strip_mixed_kernel(StageArgs a, GhostArgs g, FusedArgs f) {
+    stage_fused_body<float, true, 8, MixedC2p<MLP>, STRIP_WARPS * 32, true>(a, g, f);
+}
+
+template <bool MLP>
+static cudaError_t fused_strip_mixed(const StageArgs& a, const GhostArgs& g, const FusedArgs& f, int grid,
+                                     cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(STRIP_WARPS * 32);
+    cfg.dynamicSmemBytes = fused_strip_smem_bytes<MLP>();
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, stage_fused_strip_mixed_kernel<MLP>, a, g, f);
+}
+
+cudaError_t fused_strip_max_ctas_mixed(bool mlp, int* n) {
+    return mlp ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, stage_fused_strip_mixed_kernel<true>,
+                                                               STRIP_WARPS * 32, fused_strip_smem_bytes<true>())
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, stage_fused_strip_mixed_kernel<false>,
+                                                               STRIP_WARPS * 32, fused_strip_smem_bytes<false>());
+}
+
 cudaError_t launch_stage_fused_mixed(const StageArgs& a, const GhostArgs& g, const FusedArgs& f, int grid,
                                      cudaStream_t s) {
     const bool mlp = a.mlp != nullptr;
+    if (a.strips) return mlp ? fused_strip_mixed<true>(a, g, f, grid, s) : fused_strip_mixed<false>(a, g, f, grid, s);
     switch (fused_tr(a.utr)) {
     case 4: return mlp ? fused_mixed<4, true>(a, g, f, grid, s) : fused_mixed<4, false>(a, g, f, grid, s);
     case 16: return mlp ? fused_mixed<16, true>(a, g, f, grid, s) : fused_mixed<16, false>(a, g, f, grid, s);
@@ -539,6 +571,9 @@ cudaError_t configure_kernels() {
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(c2p_high_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(sizeof(MlpWeights) + 8 * MLP_ACT_ELEMS * sizeof(__nv_bfloat16)));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(stage_fused_strip_mixed_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)fused_strip_smem_bytes<true>());
     if (e == cudaSuccess) e = configure_fused_mixed<4, false>();
     if (e == cudaSuccess) e = configure_fused_mixed<8, false>();
     if (e == cudaSuccess) e = configure_fused_mixed<16, false>();
