@@ -421,6 +421,15 @@ __device__ __forceinline__ void update_strip(const StageArgs& a, const int4 it, 
         // the next row, one step ahead
         R Pn[NFIELD];
         load_prim_row(P, pn, nq, nr, j, jin, i + 3, Pn);
+        // this row's state and RK base towards L1 (read at the end of the step)
+        if (MIXED && writes) {
+            const int64_t z = (int64_t)i * nq + j;
+#pragma unroll
+            for (int q = 0; q < NFIELD; ++q) {
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(Uin + q * n + z));
+                if (U0) asm volatile("prefetch.global.L1 [%0];" ::"l"(U0 + q * n + z));
+            }
+        }
         // ---- polar: slopes of row i, the face j - 1 | j, its right neighbour's
         R gq[NFIELD], plq[NFIELD], prq[NFIELD], Fq[NFIELD], Fq1[NFIELD];
 #pragma unroll
