@@ -364,16 +364,23 @@ __device__ __forceinline__ void srhd_sides_f32x2(const PhysT<float>& ph, const f
     const float2 k = __ffma2_rn(cs2, mone, one);                            // 1 - cs^2
     const float2 a = __fmul2_rn(vn, k);
     const float2 wp1 = __fadd2_rn(w, one);
-    // tau without cancellation: p (gh W^2 - 1) + D u^2 / (W + 1)
-    const float2 U3 = __ffma2_rn(pre, __ffma2_rn(bcast(ph.gh), w2, mone),
-                                 __fmul2_rn(__fmul2_rn(d, uu), pair(1.0f / wp1.x, 1.0f / wp1.y)));
+    const float2 t = __fmul2_rn(__fmul2_rn(rho, uu), pair(1.0f / wp1.x, 1.0f / wp1.y));   // rho u^2 / (W + 1)
+    // tau without cancellation: p (gh W^2 - 1) + W rho u^2 / (W + 1)
+    const float2 U3 = __ffma2_rn(pre, __ffma2_rn(bcast(ph.gh), w2, mone), __fmul2_rn(w, t));
     const float2 inner = __ffma2_rn(__fmul2_rn(__fmul2_rn(ut, ut), omv2), k, omv2);
     const float2 barg = __fmul2_rn(__fmul2_rn(cs2, omv2), inner);
     const float2 b = pair(sqrtf(barg.x), sqrtf(barg.y));
-    const float2 F0 = __fmul2_rn(d, vn);
-    const float2 F1 = AXIS == 0 ? __ffma2_rn(U1, vn, pre) : __fmul2_rn(U1, vn);
-    const float2 F2 = AXIS == 1 ? __ffma2_rn(U2, vn, pre) : __fmul2_rn(U2, vn);
-    const float2 F3 = __fmul2_rn(__fadd2_rn(U3, pre), vn);
+    // fluxes in the forms with the fewest roundings (all equal to U v_n + p e_n
+    // in exact arithmetic): D v_n = rho u_n, S v_n = rho h u u_n,
+    // (tau + p) v_n = u_n (rho u^2 / (W + 1) + gh p W); the density flux then
+    // carries one rounding instead of three, which is what the density error
+    // of a near-steady flow accumulates from
+    const float2 rhoh = __ffma2_rn(bcast(ph.gh), pre, rho);
+    const float2 rhohun = __fmul2_rn(rhoh, un);
+    const float2 F0 = __fmul2_rn(rho, un);
+    const float2 F1 = AXIS == 0 ? __ffma2_rn(rhohun, ur, pre) : __fmul2_rn(rhohun, ur);
+    const float2 F2 = AXIS == 1 ? __ffma2_rn(rhohun, uq, pre) : __fmul2_rn(rhohun, uq);
+    const float2 F3 = __fmul2_rn(un, __ffma2_rn(__fmul2_rn(bcast(ph.gh), pre), w, t));
     const float2 den = __ffma2_rn(__fmul2_rn(v2, cs2), mone, one);           // 1 - v^2 cs^2
     const float2 inv = pair(1.0f / den.x, 1.0f / den.y);
     const float2 lm = __fmul2_rn(__ffma2_rn(b, mone, a), inv);
