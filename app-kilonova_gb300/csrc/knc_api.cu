@@ -908,7 +908,8 @@ bool mixed(const knc_ctx* c) { return c->precision == KNC_PRECISION_MIXED; }
 int launch_c2p(knc_ctx* c, const StageArgs& a) {
     ProfScope ps(c, KNC_KERNEL_C2P);
     cudaError_t e = mixed(c) ? launch_c2p_mixed(a, c->stream) : launch_c2p_f64(a, c->stream);
-    ++c->launches;
+    // the deferring form is two kernels: every zone, then the deferred ones
+    c->launches += mixed(c) && a.high && a.ntiles > 0 ? 2 : 1;
     CK(e);
     return KNC_OK;
 }

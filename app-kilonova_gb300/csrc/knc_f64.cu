@@ -67,7 +67,7 @@ struct F64C2p {
             kind = newt_c2p(a.gm - 1.0, u, P, bad);
         }
         ++st.zones;
-        st.it64 += (unsigned long long)iters;
+        st.it64 += (unsigned)iters;
         if (kind != HYDRO_NONE && kind != HYDRO_NEGATIVE_PRESSURE) {
             atomicMin(&a.status->err_key, error_key(a.stage, slot, i, j, kind));
             a.status->err_sel = a.sel_in;

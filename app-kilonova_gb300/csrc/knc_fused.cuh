@@ -55,9 +55,11 @@ __device__ __forceinline__ void grid_barrier(DevStatus* st, unsigned long long t
     __syncthreads();
 }
 
-// Per-thread recovery statistics (summed into DevStatus at the end).
+// Per-thread recovery statistics (summed into DevStatus at the end). 32-bit
+// per thread (a thread recovers far fewer than 2^28 zones of at most 16
+// iterations each), widened for the warp sums.
 struct C2pStats {
-    unsigned long long zones = 0, it64 = 0, it32 = 0, fbs = 0;
+    unsigned zones = 0, it64 = 0, it32 = 0, fbs = 0;
     double dtz = 1.7976931348623157e308;
 };
 

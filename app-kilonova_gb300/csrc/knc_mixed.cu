@@ -74,30 +74,107 @@ static __device__ __noinline__ float mlp_guess_call(const MlpWeights& W, __nv_bf
 
 constexpr int TMA_WAIT_LIMIT = 1 << 22;   // mbarrier polls before a copy counts as lost
 
+// The FP64 recovery of one zone (volume-integrated state m, S_r, S_theta,
+// tau; cell volume dV in the stage's length units) from the FP32 root p32 / m
+// when the FP32 iteration converged (ok32), else from the plain guess; the
+// reference's iteration from the plain guess is the fallback.
+struct Fp64Recovery {
+    float P[4];
+    int kind;
+    int it64;
+    int fbs;
+    int it32;
+};
+
+__device__ __forceinline__ Fp64Recovery recover_fp64(const StageArgs& a, double m, double s1, double s2, double tau,
+                                                     float dV, bool ok32, float p32) {
+    Fp64Recovery r = {{0.f, 0.f, 0.f, 0.f}, HYDRO_NONE, 0, 0, 0};
+    const double ss = s1 * s1 + s2 * s2;
+    const double tol = NEWTON_TOLERANCE * (m + tau);
+    double p64 = 0.0, w64 = 1.0;
+    const bool ok = newton_fast<double>(m, ss, tau, a.gm, ok32 ? (double)p32 * m : 0.0, tol, 0.0, NEWTON_ITER_MAX,
+                                        p64, w64, r.it64);
+    if (!ok) {
+        // fallback: the reference's iteration from the plain guess
+        r.fbs = 1;
+        const double u[4] = {m, s1, s2, tau};
+        double Pd[4] = {0.0, 0.0, 0.0, 0.0};
+        double bad;
+        int itf = 0;
+        const int kf = srhd_c2p_newton(a.gm, u, 0.0, Pd, itf, bad);
+        r.it64 += itf;
+        if (kf == HYDRO_ROOT_FINDER_FAILED) {
+            r.kind = kf;
+        } else {
+            // Pd is the (floored) primitive of the volume-integrated state
+            const double inv_dv = a.lscale3_d / (double)dV;
+            r.P[0] = (float)(Pd[0] * inv_dv);
+            r.P[1] = (float)Pd[1];
+            r.P[2] = (float)Pd[2];
+            r.P[3] = (float)(Pd[3] * inv_dv);
+        }
+    } else {
+        const double inv_dv = a.lscale3_d / (double)dV;
+        const double inv_et = 1.0 / (tau + m + p64);
+        const double rho = m / w64 * inv_dv;
+        r.P[0] = (float)rho;
+        r.P[1] = (float)(w64 * s1 * inv_et);
+        r.P[2] = (float)(w64 * s2 * inv_et);
+        r.P[3] = p64 < 0.0 ? (float)(PRESSURE_FLOOR * rho) : (float)(p64 * inv_dv);
+    }
+    return r;
+}
+
+// Out of line, for the recovery form that defers these zones: there it runs
+// only if the deferral list were full, so it reads the zone's state again
+// rather than keep the FP64 values live, and its registers stay out of the
+// common path. run32: the FP32 iteration (per unit mass: ssn, taun, from
+// guess) has not run yet.
+static __device__ __noinline__ Fp64Recovery recover_fp64_call(const StageArgs& a, const DevBlock& B, int i, int j,
+                                                              float dV, bool ok32, float p32, bool run32, float ssn,
+                                                              float taun, float guess) {
+    int it32 = 0;
+    if (run32) {
+        float w32 = 1.f;
+        ok32 = newton_fast<float>(1.0f, ssn, taun, a.gm_f, guess, 2e-7f * taun, 1e-6f, 16, p32, w32, it32);
+    }
+    const int64_t n = (int64_t)B.nr * B.nq;
+    const double* Ub = B.buf[a.sel_in] + (int64_t)i * B.nq + j;
+    Fp64Recovery r = recover_fp64(a, Ub[0], Ub[n], Ub[2 * n], Ub[3 * n], dV, ok32, p32);
+    r.it32 = it32;
+    return r;
+}
+
 // Recovery of one zone; every thread of a warp calls zone() together (the
-// learned guess is a warp-wide inference). DEFER: zones whose Lorentz factor
-// needs the FP64 recovery are appended to the stage's list (a.high) and left
-// to c2p_high_kernel, which runs them densely with the learned guess; every
-// zone still meets the same arithmetic.
+// learned guess is a warp-wide inference).
+//
+// DEFER: the zones that need the FP64 recovery (Lorentz factor above the
+// split, or an FP32 iteration that did not converge) are appended to the
+// stage's list (a.high) and left to c2p_high_kernel, which recovers them
+// densely, with the learned guess, through the inline form: every zone meets
+// the same arithmetic in both forms.
 template <bool MLP, bool DEFER = false>
 struct MixedC2p {
     static constexpr bool mlp = MLP;
     __device__ static void zone(const StageArgs& a, int slot, const DevBlock& B, int i, int j, bool active,
                                 MlpWeights& W, __nv_bfloat16* act, C2pStats& st) {
-        const double gm = a.gm;
+        double U[5] = {1.0, 0.0, 0.0, 1.0, 0.0};
+        if (active) {
+            const int64_t n = (int64_t)B.nr * B.nq;
+            const double* Ub = B.buf[a.sel_in] + (int64_t)i * B.nq + j;
+#pragma unroll
+            for (int q = 0; q < 5; ++q) U[q] = Ub[q * n];
+        }
+        zone_state(a, slot, B, i, j, active, U, W, act, st);
+    }
+
+    // The same with the zone's state U (D, S_r, S_theta, tau, scalar mass)
+    // already loaded.
+    __device__ static void zone_state(const StageArgs& a, int slot, const DevBlock& B, int i, int j, bool active,
+                                      const double (&U)[5], MlpWeights& W, __nv_bfloat16* act, C2pStats& st) {
         const float gmf = a.gm_f;
         const float high_thr = a.high_thr_f;
-        const int nr = B.nr, nq = B.nq;
-        const int64_t n = (int64_t)nr * nq;
-        const int64_t z = (int64_t)i * nq + j;
-        double U[5] = {1.0, 0.0, 0.0, 1.0, 0.0};
-        float dV = 1.0f;
-        if (active) {
-            const double* Ub = B.buf[a.sel_in];
-#pragma unroll
-            for (int q = 0; q < 5; ++q) U[q] = Ub[q * n + z];
-            dV = B.dv_r32[i] * B.dv_q[j].x;
-        }
+        const float dV = active ? B.dv_r32[i] * B.dv_q[j].x : 1.0f;
         const double m = U[0], tau = U[3];
         int kind = HYDRO_NONE;
         if (active && is_negative(m)) kind = HYDRO_NEGATIVE_DENSITY;
@@ -108,6 +185,7 @@ struct MixedC2p {
         const int de = -a.lscale3;
         const float mf = d2f_rn_exp(m, de), tauf = d2f_rn_exp(tau, de);
         const float s1f = d2f_rn_exp(U[1], de), s2f = d2f_rn_exp(U[2], de);
+        const float scalf = d2f_rn_exp(U[4], de);
         // the FP32 iteration runs on the state per unit mass (O(1) numbers,
         // no overflow or underflow of the squares whatever the units); the
         // recovery is scale-invariant, p = (p / m) m
@@ -115,23 +193,8 @@ struct MixedC2p {
         const float s1n = s1f * im, s2n = s2f * im, taun = tauf * im;
         const float ssn = s1n * s1n + s2n * s2n;
         const float x1 = __fdividef(sqrtf(ssn), 1.0f + taun);   // |S| / (D + tau)
-        const bool high = active && kind == HYDRO_NONE && x1 * x1 > high_thr;
-        if (DEFER) {
-            const unsigned full = 0xffffffffu;
-            const unsigned mask = __ballot_sync(full, high);
-            if (mask) {
-                const int lane = threadIdx.x & 31;
-                unsigned base = 0;
-                if (lane == __ffs(mask) - 1) base = atomicAdd(a.high_count, (unsigned)__popc(mask));
-                base = __shfl_sync(full, base, __ffs(mask) - 1);
-                const unsigned slot_k = base + __popc(mask & ((1u << lane) - 1u));
-                // a full list (never reached: capacity = zones) keeps the zone here
-                if (high && slot_k < a.high_cap) {
-                    a.high[slot_k] = make_int2(slot, (int)z);
-                    return;
-                }
-            }
-        }
+        const bool valid = active && kind == HYDRO_NONE;
+        const bool high = valid && x1 * x1 > high_thr;
         float guess = 0.0f;   // p / m
         if (MLP) {
             if (__any_sync(0xffffffffu, high)) {
@@ -144,20 +207,38 @@ struct MixedC2p {
                 guess = (high && ok && gsv > 0.0f) ? fminf(gsv, (gmf - 1.0f) * taun) : 0.0f;
             }
         }
+        float p32 = 0.f, w32 = 1.f;
+        int it32 = 0;
+        bool ok32 = false;
+        // stop once the residual is at the rounding level of the energy
+        // (|f| < 2e-7 tau / m, about 3 FP32 ulps of tau): further steps move p
+        // by rounding noise only (5.6 -> 2.1 iterations per zone on the wind,
+        // density L1 unchanged). The deferring form leaves the high zones'
+        // iteration to the dense pass.
+        if (valid && !(DEFER && high))
+            ok32 = newton_fast<float>(1.0f, ssn, taun, gmf, guess, 2e-7f * taun, 1e-6f, 16, p32, w32, it32);
+        bool fp64 = valid && (high || !ok32);
+        if (DEFER) {
+            const unsigned full = 0xffffffffu;
+            const unsigned mask = __ballot_sync(full, fp64);
+            if (mask) {
+                const int lane = threadIdx.x & 31;
+                unsigned base = 0;
+                if (lane == __ffs(mask) - 1) base = atomicAdd(a.high_count, (unsigned)__popc(mask));
+                base = __shfl_sync(full, base, __ffs(mask) - 1);
+                const unsigned slot_k = base + __popc(mask & ((1u << lane) - 1u));
+                // a full list (never reached: capacity = zones) keeps the zone here
+                if (fp64 && slot_k < a.high_cap) {
+                    a.high[slot_k] = make_int2(slot, (int)((int64_t)i * B.nq + j));
+                    return;
+                }
+            }
+        }
         float P[4] = {0.f, 0.f, 0.f, 0.f};
-        float wz = 1.0f;
-        if (active && kind == HYDRO_NONE) {
+        if (valid) {
             ++st.zones;
-            float p32 = 0.f, w32 = 1.f;
-            int it32 = 0;
-            // stop once the residual is at the rounding level of the energy
-            // (|f| < 2e-7 tau / m, about 3 FP32 ulps of tau): further steps
-            // move p by rounding noise only (5.6 -> 2.1 iterations per zone
-            // on the wind, density L1 unchanged)
-            const bool ok32 =
-                newton_fast<float>(1.0f, ssn, taun, gmf, guess, 2e-7f * taun, 1e-6f, 16, p32, w32, it32);
-            st.it32 += (unsigned long long)it32;
-            if (!high && ok32) {
+            st.it32 += (unsigned)it32;
+            if (!fp64) {
                 const float inv_dv = 1.0f / dV;
                 const float inv_et = 1.0f / (taun + 1.0f + p32);
                 P[0] = mf / w32 * inv_dv;
@@ -166,42 +247,17 @@ struct MixedC2p {
                 P[3] = p32 * mf * inv_dv;
                 if (p32 < 0.f) P[3] = (float)PRESSURE_FLOOR * P[0];
             } else {
-                const double ss = U[1] * U[1] + U[2] * U[2];
-                const double tol = NEWTON_TOLERANCE * (m + tau);
-                double p64 = 0.0, w64 = 1.0;
-                int it64 = 0;
-                bool ok = newton_fast<double>(m, ss, tau, gm, ok32 ? (double)p32 * m : 0.0, tol, 0.0, NEWTON_ITER_MAX,
-                                              p64, w64, it64);
-                st.it64 += (unsigned long long)it64;
-                if (!ok) {
-                    // fallback: the reference's iteration from the plain guess
-                    ++st.fbs;
-                    const double u[4] = {m, U[1], U[2], tau};
-                    double Pd[4] = {0.0, 0.0, 0.0, 0.0};
-                    double bad;
-                    int itf = 0;
-                    const int kf = srhd_c2p_newton(gm, u, 0.0, Pd, itf, bad);
-                    st.it64 += (unsigned long long)itf;
-                    if (kf == HYDRO_ROOT_FINDER_FAILED) {
-                        kind = kf;
-                    } else {
-                        // Pd is the (floored) primitive of the volume-integrated
-                        // state; dV is in the stage's length units
-                        const double inv_dv = a.lscale3_d / (double)dV;
-                        P[0] = (float)(Pd[0] * inv_dv);
-                        P[1] = (float)Pd[1];
-                        P[2] = (float)Pd[2];
-                        P[3] = (float)(Pd[3] * inv_dv);
-                    }
-                } else {
-                    const double inv_dv = a.lscale3_d / (double)dV;
-                    const double inv_et = 1.0 / (tau + m + p64);
-                    const double rho = m / w64 * inv_dv;
-                    P[0] = (float)rho;
-                    P[1] = (float)(w64 * U[1] * inv_et);
-                    P[2] = (float)(w64 * U[2] * inv_et);
-                    P[3] = p64 < 0.0 ? (float)(PRESSURE_FLOOR * rho) : (float)(p64 * inv_dv);
-                }
+                // (deferring form: kept here, a high zone has not run the
+                // FP32 iteration yet)
+                const Fp64Recovery r =
+                    DEFER ? recover_fp64_call(a, B, i, j, dV, ok32, p32, high, ssn, taun, guess)
+                          : recover_fp64(a, m, U[1], U[2], tau, dV, ok32, p32);
+                st.it32 += (unsigned)r.it32;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) P[q] = r.P[q];
+                kind = r.kind;
+                st.it64 += (unsigned)r.it64;
+                st.fbs += (unsigned)r.fbs;
             }
         }
         if (active) {
@@ -209,8 +265,8 @@ struct MixedC2p {
                 atomicMin(&a.status->err_key, error_key(a.stage, slot, i, j, kind));
                 a.status->err_sel = a.sel_in;
             }
-            wz = sqrtf(1.0f + P[1] * P[1] + P[2] * P[2]);
-            const float v[NFIELD] = {P[0], P[1], P[2], P[3], d2f_rn_exp(U[4], de) / dV / wz};
+            const float wz = sqrtf(1.0f + P[1] * P[1] + P[2] * P[2]);
+            const float v[NFIELD] = {P[0], P[1], P[2], P[3], scalf / dV / wz};
             store_prim<float>(B, i, j, v);
             if (a.compute_dt && kind == HYDRO_NONE) {
                 // State::time_step (src/state.rs:151-160) on this stage's
@@ -232,7 +288,7 @@ struct MixedC2p {
     }
 };
 
-template <bool MLP, bool DEFER = false>
+template <bool MLP>
 __global__ void __launch_bounds__(TILE_THREADS, 3) c2p_mixed_kernel(StageArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
@@ -250,8 +306,73 @@ __global__ void __launch_bounds__(TILE_THREADS, 3) c2p_mixed_kernel(StageArgs a)
         const DevBlock& B = a.blocks[t.x];
         const int i = t.y + threadIdx.x / TILE_Q;
         const int j = t.z + threadIdx.x % TILE_Q;
-        MixedC2p<MLP, DEFER>::zone(a, t.x, B, i, j, i < B.nr && j < B.nq, W, act, st);
+        MixedC2p<MLP>::zone(a, t.x, B, i, j, i < B.nr && j < B.nq, W, act, st);
     }
+    warp_reduce_stats(a.status, st.zones, st.it64, st.it32, st.fbs, st.dtz, a.compute_dt != 0);
+}
+
+// ---- recovery by warps walking the rows of a tile -----------------------------
+// The recovery's arithmetic between its loads and its stores is long and
+// serial, so a zone-per-thread loop keeps few loads in flight and runs
+// latency-bound. Here a warp takes a whole recovery tile (TILE_R rows of 32
+// zones): the tile's descriptor and block fields are read once instead of once
+// per zone, and each lane copies its column's state of the rows C2P_DEPTH - 1
+// ahead into shared memory with cp.async (8-byte, L1-allocating) while it
+// recovers the current row, so the copies hold no registers. A lane reads
+// only the slots it filled (no barrier); cp.async.wait_group orders its own
+// copies, and the slot it refills is the one it read a row earlier.
+constexpr int C2P_DEPTH = 3;
+
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+__global__ void __launch_bounds__(TILE_THREADS, 3) c2p_rows_kernel(StageArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int WPC = TILE_THREADS / 32;
+    __shared__ __align__(16) double sU[WPC][C2P_DEPTH][NFIELD][32];
+    const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
+    if (ek != NO_ERROR && (uint32_t)(ek >> 48) < (uint32_t)a.stage) return;
+    MlpWeights& W = *reinterpret_cast<MlpWeights*>(smem_raw);   // unused without the learned guess
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    C2pStats st;
+    for (int tile = blockIdx.x * WPC + w; tile < a.ntiles; tile += gridDim.x * WPC) {
+        const int4 t = a.tiles[tile];
+        const DevBlock& B = a.blocks[t.x];
+        const int j = t.z + lane;
+        const bool jin = j < B.nq;
+        const int rows = min(TILE_R, B.nr - t.y);
+        const int64_t n = (int64_t)B.nr * B.nq;
+        const double* Ub = B.buf[a.sel_in] + (int64_t)t.y * B.nq + j;
+        auto issue = [&](int r) {
+            if (jin && r < rows) {
+#pragma unroll
+                for (int q = 0; q < NFIELD; ++q) cp_async8(&sU[w][r % C2P_DEPTH][q][lane], Ub + q * n + (int64_t)r * B.nq);
+            }
+            cp_async_commit();
+        };
+#pragma unroll
+        for (int r = 0; r < C2P_DEPTH - 1; ++r) issue(r);
+        for (int r = 0; r < rows; ++r) {
+            issue(r + C2P_DEPTH - 1);
+            cp_async_wait<C2P_DEPTH - 1>();
+            double U[5] = {1.0, 0.0, 0.0, 1.0, 0.0};
+            if (jin) {
+#pragma unroll
+                for (int q = 0; q < NFIELD; ++q) U[q] = sU[w][r % C2P_DEPTH][q][lane];
+            }
+            MixedC2p<false, true>::zone_state(a, t.x, B, t.y + r, j, jin, U, W, nullptr, st);
+        }
+    }
+    cp_async_wait<0>();
     warp_reduce_stats(a.status, st.zones, st.it64, st.it32, st.fbs, st.dtz, a.compute_dt != 0);
 }
 
@@ -328,8 +449,10 @@ cudaError_t launch_c2p_mixed(const StageArgs& a, cudaStream_t s) {
     if (a.ntiles <= 0) return cudaSuccess;
     if (a.high) {
         // every zone in FP32; the ones that need the FP64 recovery, densely after
-        const int grid = std::min(a.ntiles, resident_grid(c2p_mixed_kernel<false, true>, TILE_THREADS, 0));
-        c2p_mixed_kernel<false, true><<<grid, TILE_THREADS, 0, s>>>(a);
+        // one warp per recovery tile
+        const int wt = (a.ntiles + TILE_THREADS / 32 - 1) / (TILE_THREADS / 32);
+        const int grid = std::min(wt, resident_grid(c2p_rows_kernel, TILE_THREADS, 0));
+        c2p_rows_kernel<<<grid, TILE_THREADS, 0, s>>>(a);
         if (a.mlp) {
             const size_t bytes = sizeof(MlpWeights) + 8 * MLP_ACT_ELEMS * sizeof(__nv_bfloat16);
             c2p_high_kernel<true><<<num_sms(), TILE_THREADS, bytes, s>>>(a);
@@ -365,7 +488,7 @@ struct TmaSmem {
 template <int TR>
 __global__ void __launch_bounds__(update_threads<TR>(), 1) update_tma_kernel(StageArgs a) {
     using L = TmaSmem<TR>;
-    extern __shared__ __align__(128) unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned char* base = smem_raw + ((128 - (smem_u32(smem_raw) & 127)) & 127);
     unsigned char* work = base + 2 * L::BUF;
     uint64_t* bar = reinterpret_cast<uint64_t*>(work + L::WORK);

@@ -428,7 +428,7 @@ def run_only(args):
     s = knc.build_solver(w)
     if args.tile_rows:
         s.set_tuning(tile_rows=args.tile_rows, fused=args.fused, tma=args.tma, strip=args.strip,
-                     ctas_per_sm=args.ctas_per_sm)
+                     ctas_per_sm=args.ctas_per_sm, deferred=args.deferred)
     if args.only == "mixed":
         s.set_precision(abi.KNC_PRECISION_MIXED)
         s.set_mixed_w_split(args.w_split)
@@ -468,6 +468,7 @@ def main():
     ap.add_argument("--tma", action="store_true")
     ap.add_argument("--strip", action="store_true")
     ap.add_argument("--ctas-per-sm", type=int, default=0)
+    ap.add_argument("--deferred", action="store_true", help="mixed recovery with the FP64 zones deferred")
     ap.add_argument("--only", choices=["fp64", "mixed"], default=None,
                     help="run one path alone (profiler captures)")
     args = ap.parse_args()

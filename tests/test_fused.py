@@ -137,6 +137,21 @@ def test_fused_counts_one_launch_per_stage():
     assert n1.value - n0.value == 3 * 2      # RK2: two stages per step, one launch each
 
 
+def test_launch_count_counts_every_kernel():
+    """Launches per stage as counted by knc_launch_count: ghost rows,
+    recovery, update; the deferring recovery adds its dense FP64 pass."""
+    import knc
+    from knc import workloads
+    w = workloads.wind_small()
+    g, _ = make_pair(w, gpu=True)
+    g.set_precision(knc.abi.KNC_PRECISION_MIXED)
+    for deferred, per_stage in ((False, 3), (True, 4)):
+        g.set_tuning(tile_rows=8, strip=True, deferred=deferred)
+        n0 = g.launch_count()
+        g.advance(2)
+        assert g.launch_count() - n0 == 2 * 2 * per_stage
+
+
 @pytest.mark.parametrize("tile_rows", [4, 8, 16])
 def test_mixed_tma_staging_matches(tile_rows):
     """The tensor-copy staged update reads the same values from shared
