@@ -224,6 +224,9 @@ void free_block(BlockH& b) {
     b = BlockH();
 }
 
+// Rows of the warp strips the host-state advance updates chunks with.
+constexpr int STREAM_STRIP_ROWS = 4;
+
 // One block set's device view.
 struct Layout {
     DevBlock* d_table = nullptr;
@@ -255,6 +258,16 @@ struct Layout {
     int nremap = 0;
     int max_nq = 0;
     std::vector<int32_t> slot_index;   // slot -> block index
+    // per slot (and one past the last): its first recovery tile, update tile,
+    // warp strip and zone in the flat whole-state order; the lists hold the
+    // blocks in slot order, so a run of slots is a run of each list
+    std::vector<int> tile_off, utile_off, strip_off, sstrip_off;
+    std::vector<int64_t> zone_off;
+    // warp strips of STREAM_STRIP_ROWS rows for the host-state advance, whose
+    // launches each cover one chunk of blocks: short strips keep enough
+    // warps per SM on a chunk
+    int4* d_sstrips = nullptr;
+    int sstrips_cap = 0;
     // edge blocks, whose outer halo rows the ghost launch writes
     void* P_edge[2] = {nullptr, nullptr};
     int32_t nr_edge[2] = {0, 0}, nq_edge[2] = {0, 0};
@@ -277,6 +290,7 @@ void free_layout(Layout& l) {
     cudaFree(l.d_chunks);
     cudaFree(l.d_high);
     cudaFree(l.d_strips);
+    cudaFree(l.d_sstrips);
     cudaFree(l.d_tmaps);
     cudaFree(l.d_remap);
     cudaFree(l.d_ghost_rc);
@@ -298,6 +312,10 @@ struct knc_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;        // ghost rows run here, beside the recovery
+    // host-state advance: uploads and downloads of block chunks, beside the stages
+    cudaStream_t h2d = nullptr, d2h = nullptr;
+    std::vector<cudaStream_t> kstreams;   // one per kind of chunk launch (recovery / update of each stage)
+    std::vector<cudaEvent_t> ev_chunk;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::map<int32_t, BlockH> blocks;
     std::map<std::pair<int64_t, int64_t>, std::vector<BlockH>> pool;   // freed block storage by shape
@@ -584,6 +602,12 @@ int rebuild_table(knc_ctx* c) {
     bool tma_ok = nb > 0;
     const int nt = fused_threads(c);
     L(c).slot_index.clear();
+    L(c).tile_off.clear();
+    L(c).utile_off.clear();
+    L(c).strip_off.clear();
+    L(c).sstrip_off.clear();
+    L(c).zone_off.clear();
+    std::vector<int4> sstrips;
     int slot = 0;
     int64_t zoff = 0;
     const BlockH* prev = nullptr;
@@ -637,6 +661,15 @@ int rebuild_table(knc_ctx* c) {
                 remaps.push_back(make_int4(k - 1, k, 1, 0));
             }
         }
+        L(c).tile_off.push_back((int)tiles.size());
+        L(c).utile_off.push_back((int)utiles.size());
+        L(c).strip_off.push_back((int)strips.size());
+        L(c).sstrip_off.push_back((int)sstrips.size());
+        L(c).zone_off.push_back(zoff);
+        for (int64_t j0 = 0; j0 < b.nq; j0 += STRIP_OUT)
+            for (int64_t i0 = 0; i0 < b.nr; i0 += STREAM_STRIP_ROWS)
+                sstrips.push_back(
+                    make_int4(slot, (int)i0, (int)j0, (int)std::min<int64_t>(STREAM_STRIP_ROWS, b.nr - i0)));
         for (int64_t i0 = 0; i0 < b.nr; i0 += TILE_R)
             for (int64_t j0 = 0; j0 < b.nq; j0 += TILE_Q)
                 tiles.push_back(make_int4(slot, (int)i0, (int)j0, (int)zoff));
@@ -657,6 +690,20 @@ int rebuild_table(knc_ctx* c) {
         prev = &b;
         ++slot;
     }
+    L(c).tile_off.push_back((int)tiles.size());
+    L(c).utile_off.push_back((int)utiles.size());
+    L(c).strip_off.push_back((int)strips.size());
+    L(c).sstrip_off.push_back((int)sstrips.size());
+    L(c).zone_off.push_back(zoff);
+    if ((int)sstrips.size() > L(c).sstrips_cap) {
+        cudaFree(L(c).d_sstrips);
+        L(c).d_sstrips = nullptr;
+        CK(dalloc(&L(c).d_sstrips, sstrips.size()));
+        L(c).sstrips_cap = (int)sstrips.size();
+    }
+    if (!sstrips.empty())
+        CK(cudaMemcpyAsync(L(c).d_sstrips, sstrips.data(), sstrips.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                           c->stream));
     if (nb > L(c).table_cap) {
         cudaFree(L(c).d_table);
         L(c).d_table = nullptr;
@@ -943,13 +990,14 @@ int fused_grid(knc_ctx* c) {
 }
 
 // One Euler stage U_out = avg(U_in + dt L(U_in), U_base), src/scheme.rs:16-173.
-int run_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, double bf, double t_stage,
-              double dt, int sub) {
+// The arguments of one RK stage's launches (ghost rows, recovery, remaps,
+// update); takes the next stage number.
+int prepare_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, double bf, double t_stage,
+                  double dt, int sub, GhostArgs& g, StageArgs& a) {
     int r;
     if (c->stage_counter >= 0xffff) return set_msg(c, KNC_ERR_INVALID_ARGUMENT, "too many stages in one call");
     const int32_t stage = c->stage_counter++;
     // ghost rows at the stage time
-    GhostArgs g;
     std::memset(&g, 0, sizeof(g));
     const Layout& lay = L(c);
     for (int end = 0; end < 2; ++end) {
@@ -984,7 +1032,7 @@ int run_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, doub
         g.host_prim[0] = c->d_host_prim;
         g.host_prim[1] = c->d_host_prim + 2 * L(c).ghost_nq[0] * 5;
     }
-    StageArgs a = base_args(c);
+    a = base_args(c);
     a.stage = stage;
     a.sel_in = sel_in;
     a.sel_out = sel_out;
@@ -1005,6 +1053,16 @@ int run_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, doub
         a.cfl = c->hp.cfl_number;
         a.compute_dt = c->ddt_step == 0 && sub == 0 ? 1 : 0;   // the fold's first recovery finds dt
     }
+    return KNC_OK;
+}
+
+int run_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, double bf, double t_stage,
+              double dt, int sub) {
+    int r;
+    GhostArgs g;
+    StageArgs a;
+    if ((r = prepare_stage(c, sel_in, sel_out, sel_base, w1, bf, t_stage, dt, sub, g, a))) return r;
+    const Layout& lay = L(c);
     if (c->fused) {
         // the whole stage in one cooperative launch (grid barriers between phases)
         FusedArgs f;
@@ -1078,9 +1136,34 @@ StepTimes step_times(int order, double t0, double dt) {
     return s;
 }
 
-// godunov_core::runge_kutta::try_advance_async restated (SSP RK1/RK2/RK3).
-int rk_step(knc_ctx* c, double dt) {
+// The stages of one SSP RK step (godunov_core::runge_kutta::try_advance_async
+// restated, RK1/RK2/RK3): the input, output and base buffers of each stage,
+// its averaging weights (1 - b) and b, and its start time.
+struct StagePlan {
+    int sel_in, sel_out, sel_base;
+    double w1, bf, t;
+    int sub;
+};
+
+int step_plan(const knc_ctx* c, double dt, StagePlan p[3]) {
     const int A = c->cur, B = 1 - c->cur;
+    const int order = c->hp.runge_kutta_order;
+    const StepTimes T = step_times(order, c->time, dt);
+    p[0] = {A, B, -1, 1.0, 0.0, T.stage[0], 0};
+    if (order == 1) return 1;
+    if (order == 2) {
+        const double bf = 0.5;
+        p[1] = {B, A, A, -bf + 1.0, bf, T.stage[1], 1};
+        return 2;
+    }
+    const double b2 = 0.75, b3 = 1.0 / 3.0;
+    p[1] = {B, B, A, -b2 + 1.0, b2, T.stage[1], 1};
+    p[2] = {B, A, A, -b3 + 1.0, b3, T.stage[2], 2};
+    return 3;
+}
+
+// Time, iteration and current buffer after a step's stages ran.
+void finish_step(knc_ctx* c, double dt) {
     const double t0 = c->time;
     const Rational it0 = c->iteration;
     Rational one;
@@ -1092,40 +1175,36 @@ int rk_step(knc_ctx* c, double dt) {
         mbr.n = -mbr.n;
         return i1.mul(mbr.add(one)).add(it0.mul(br));
     };
-    int r;
-    c->zone_updates += L(c).nzones;
-    if ((r = run_stage(c, A, B, -1, 1.0, 0.0, T.stage[0], dt, 0))) return r;
-    Rational i1 = it0.add(one);
+    const Rational i1 = it0.add(one);
+    if (!c->ddt) c->time = T.end;
     if (order == 1) {
-        c->cur = B;
-        if (!c->ddt) c->time = T.end;
+        c->cur = 1 - c->cur;
         c->iteration = i1;
-        return KNC_OK;
-    }
-    if (order == 2) {
-        const double bf = 0.5;
-        if ((r = run_stage(c, B, A, A, -bf + 1.0, bf, T.stage[1], dt, 1))) return r;
+    } else if (order == 2) {
         Rational half;
         half.n = 1;
         half.d = 2;
-        if (!c->ddt) c->time = T.end;
         c->iteration = avg_iter(i1.add(one), half);
-        return KNC_OK;
+    } else {
+        Rational q34, q13;
+        q34.n = 3;
+        q34.d = 4;
+        q13.n = 1;
+        q13.d = 3;
+        const Rational i2 = avg_iter(i1.add(one), q34);
+        c->iteration = avg_iter(i2.add(one), q13);
     }
-    // RK3
-    const double b2 = 0.75;
-    if ((r = run_stage(c, B, B, A, -b2 + 1.0, b2, T.stage[1], dt, 1))) return r;
-    Rational q34;
-    q34.n = 3;
-    q34.d = 4;
-    const Rational i2 = avg_iter(i1.add(one), q34);
-    const double b3 = 1.0 / 3.0;
-    if ((r = run_stage(c, B, A, A, -b3 + 1.0, b3, T.stage[2], dt, 2))) return r;
-    Rational q13;
-    q13.n = 1;
-    q13.d = 3;
-    if (!c->ddt) c->time = T.end;
-    c->iteration = avg_iter(i2.add(one), q13);
+}
+
+int rk_step(knc_ctx* c, double dt) {
+    StagePlan p[3];
+    const int n = step_plan(c, dt, p);
+    c->zone_updates += L(c).nzones;
+    int r;
+    for (int s = 0; s < n; ++s)
+        if ((r = run_stage(c, p[s].sel_in, p[s].sel_out, p[s].sel_base, p[s].w1, p[s].bf, p[s].t, dt, p[s].sub)))
+            return r;
+    finish_step(c, dt);
     return KNC_OK;
 }
 
@@ -1373,6 +1452,8 @@ int create_device_side(knc_ctx* c) {
     CK(cudaGetDevice(&c->device));
     CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c->h2d, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c->d2h, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
     {
@@ -1468,6 +1549,16 @@ void knc_destroy(knc_ctx* c) {
         cudaStreamSynchronize(c->side);
         cudaStreamDestroy(c->side);
     }
+    for (cudaStream_t st : {c->h2d, c->d2h})
+        if (st) {
+            cudaStreamSynchronize(st);
+            cudaStreamDestroy(st);
+        }
+    for (cudaStream_t st : c->kstreams) {
+        cudaStreamSynchronize(st);
+        cudaStreamDestroy(st);
+    }
+    for (cudaEvent_t e : c->ev_chunk) cudaEventDestroy(e);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -1950,6 +2041,240 @@ int advance_impl(knc_ctx* c, int32_t fold, const double* dt_given) {
     return finish_ddt(check_status(c));
 }
 }  // namespace
+
+namespace {
+
+// Chunks of consecutive slots for the host-state advance, about equal in
+// zones, at most HOST_CHUNKS and at least one slot each: bounds[k] ..
+// bounds[k + 1] - 1 are chunk k's slots.
+constexpr int HOST_CHUNKS = 16;
+
+std::vector<int> chunk_bounds(const Layout& l) {
+    const int nb = (int)l.slot_index.size();
+    const int G = std::min(HOST_CHUNKS, nb);
+    std::vector<int> b{0};
+    const int64_t total = l.zone_off[nb];
+    for (int g = 1; g < G; ++g) {
+        const int64_t target = total * g / G;
+        int s = b.back() + 1;
+        while (s < nb - (G - g) && l.zone_off[s] < target) ++s;   // a slot left for every later chunk
+        b.push_back(s);
+    }
+    b.push_back(nb);
+    return b;
+}
+
+int ensure_chunk_events(knc_ctx* c, size_t n) {
+    while (c->ev_chunk.size() < n) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        c->ev_chunk.push_back(e);
+    }
+    return KNC_OK;
+}
+
+// One RK step with the state streamed between page-locked host memory and
+// the device by chunks of blocks: hc_in / hs_in are uploaded before the
+// step's first stage reads them, hc_out / hs_out downloaded after its last
+// stage (either pair may be null). Uploads (one copy direction), downloads
+// (the other) and the stages of the chunks in between run at the same time.
+//
+// Stage s recovers chunk g (R_s(g)) and updates it (X_s(g)). X_s(g) reads the
+// halo rows that R_s(g - 1) and R_s(g + 1) push into g's primitives, and
+// R_{s+1}(g) overwrites the halo rows that X_s(g - 1) and X_s(g + 1) read and
+// the state X_s(g) wrote. Each of the 2S kinds R_0, X_0, R_1, X_1, ... runs in
+// chunk order on a stream of its own, so these orders reduce to
+//   X_s(g)     after R_s(min(g + 1, G - 1)),
+//   R_{s+1}(g) after X_s(min(g + 1, G - 1)),
+// one event wait each; chunks of different kinds then overlap on the GPU
+// (a chunk's launch alone does not fill it). Launches are issued in waves
+// (R_s(g) in wave g + 2s, X_s(g) in wave g + 2s + 1, kinds in that order
+// within a wave), so every event is recorded before it is waited on. The
+// ghost rows of stage s at the inner (outer) mesh end go on X_s's stream just
+// before X_s of the first (last) chunk, which runs after X_{s-1} of that
+// chunk read the previous stage's. Recoveries run in the inline form (the
+// deferred list is per stage, not per chunk) and updates as short warp
+// strips. Every zone meets the arithmetic of rk_step, so states are bitwise
+// those of knc_set_state + knc_advance + knc_get_state.
+int stream_step(knc_ctx* c, double dt, const double* hc_in, const double* hs_in, double* hc_out,
+                double* hs_out) {
+    int r;
+    const Layout& lay = L(c);
+    const std::vector<int> cb = chunk_bounds(lay);
+    const int G = (int)cb.size() - 1;
+    const int64_t total = lay.zone_off.back();
+    StagePlan p[3];
+    const int S = step_plan(c, dt, p);
+    const int K = 2 * S;
+    GhostArgs g[3];
+    StageArgs a[3];
+    for (int s = 0; s < S; ++s)
+        if ((r = prepare_stage(c, p[s].sel_in, p[s].sel_out, p[s].sel_base, p[s].w1, p[s].bf, p[s].t, dt, p[s].sub,
+                               g[s], a[s])))
+            return r;
+    if ((r = ensure_stage(c, 5 * (size_t)total))) return r;
+    // events: uploads [0, G), kinds [G, G + K G), downloads ready [G + K G, 2 G + K G), start
+    const size_t ev_start = (size_t)(2 + K) * G;
+    if ((r = ensure_chunk_events(c, ev_start + 1))) return r;
+    while ((int)c->kstreams.size() < K) {
+        cudaStream_t st;
+        CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        c->kstreams.push_back(st);
+    }
+    auto evH = [&](int k) { return c->ev_chunk[k]; };
+    auto evK = [&](int kind, int k) { return c->ev_chunk[G + (size_t)kind * G + k]; };
+    auto evO = [&](int k) { return c->ev_chunk[(size_t)(1 + K) * G + k]; };
+    double* sc = c->d_stage;               // whole-state layout: cons [total][4], then scalar [total]
+    double* ss = c->d_stage + 4 * total;
+    auto zlo = [&](int k) { return lay.zone_off[cb[k]]; };
+    auto nz = [&](int k) { return lay.zone_off[cb[k + 1]] - lay.zone_off[cb[k]]; };
+    auto tiles_of = [&](int k) { return lay.d_tiles + lay.tile_off[cb[k]]; };
+    auto ntiles_of = [&](int k) { return lay.tile_off[cb[k + 1]] - lay.tile_off[cb[k]]; };
+    auto chunk_args = [&](const StageArgs& x, int k) {
+        StageArgs y = x;
+        const int s0 = cb[k], s1 = cb[k + 1];
+        y.tiles = lay.d_tiles + lay.tile_off[s0];
+        y.ntiles = lay.tile_off[s1] - lay.tile_off[s0];
+        // the update as warp strips of STREAM_STRIP_ROWS rows, whatever the
+        // tuned form (every form gives the same state)
+        y.strips = lay.d_sstrips + lay.sstrip_off[s0];
+        y.nstrips = lay.sstrip_off[s1] - lay.sstrip_off[s0];
+        y.tma = 0;
+        y.high = nullptr;
+        y.high_count = nullptr;
+        y.high_count_next = nullptr;
+        y.high_cap = 0;
+        return y;
+    };
+    // every stream starts after the work already on the library's stream
+    CK(cudaEventRecord(c->ev_chunk[ev_start], c->stream));
+    for (int k = 0; k < K; ++k) CK(cudaStreamWaitEvent(c->kstreams[k], c->ev_chunk[ev_start], 0));
+    if (hc_in) {
+        CK(cudaStreamWaitEvent(c->h2d, c->ev_chunk[ev_start], 0));
+        for (int k = 0; k < G; ++k) {
+            CK(cudaMemcpyAsync(sc + 4 * zlo(k), hc_in + 4 * zlo(k), 4 * nz(k) * sizeof(double),
+                               cudaMemcpyHostToDevice, c->h2d));
+            CK(cudaMemcpyAsync(ss + zlo(k), hs_in + zlo(k), nz(k) * sizeof(double), cudaMemcpyHostToDevice, c->h2d));
+            CK(cudaEventRecord(evH(k), c->h2d));
+        }
+    }
+    auto recover = [&](int s, int k) -> int {
+        cudaStream_t st = c->kstreams[2 * s];
+        if (s == 0 && hc_in) {
+            CK(cudaStreamWaitEvent(st, evH(k), 0));
+            CK(launch_state_in(lay.d_table, tiles_of(k), ntiles_of(k), p[0].sel_in, sc, ss, st));
+            ++c->launches;
+        }
+        if (s > 0) CK(cudaStreamWaitEvent(st, evK(2 * s - 1, std::min(k + 1, G - 1)), 0));
+        const StageArgs y = chunk_args(a[s], k);
+        CK(mixed(c) ? launch_c2p_mixed(y, st) : launch_c2p_f64(y, st));
+        ++c->launches;
+        CK(cudaEventRecord(evK(2 * s, k), st));
+        return KNC_OK;
+    };
+    auto update = [&](int s, int k) -> int {
+        cudaStream_t st = c->kstreams[2 * s + 1];
+        CK(cudaStreamWaitEvent(st, evK(2 * s, std::min(k + 1, G - 1)), 0));
+        for (int end = 0; end < 2; ++end) {
+            if (k != (end ? G - 1 : 0)) continue;
+            GhostArgs ge = g[s];
+            ge.P[1 - end] = nullptr;   // this end only
+            CK(mixed(c) ? launch_ghost_mixed(ge, st) : launch_ghost_f64(ge, st));
+            ++c->launches;
+        }
+        const StageArgs y = chunk_args(a[s], k);
+        CK(mixed(c) ? launch_update_mixed(y, st) : launch_update_f64(y, st));
+        ++c->launches;
+        CK(cudaEventRecord(evK(2 * s + 1, k), st));
+        if (s == S - 1 && hc_out) {
+            CK(launch_state_out(lay.d_table, tiles_of(k), ntiles_of(k), p[S - 1].sel_out, sc, ss, st));
+            ++c->launches;
+            CK(cudaEventRecord(evO(k), st));
+            CK(cudaStreamWaitEvent(c->d2h, evO(k), 0));
+            CK(cudaMemcpyAsync(hc_out + 4 * zlo(k), sc + 4 * zlo(k), 4 * nz(k) * sizeof(double),
+                               cudaMemcpyDeviceToHost, c->d2h));
+            CK(cudaMemcpyAsync(hs_out + zlo(k), ss + zlo(k), nz(k) * sizeof(double), cudaMemcpyDeviceToHost,
+                               c->d2h));
+        }
+        return KNC_OK;
+    };
+    for (int w = 0; w < G + 2 * S - 1; ++w) {
+        if (w < G && (r = recover(0, w))) return r;
+        for (int s = 0; s < S; ++s) {
+            const int gx = w - 2 * s - 1;
+            if (gx >= 0 && gx < G && (r = update(s, gx))) return r;
+            const int gr = w - 2 * s - 2;
+            if (s + 1 < S && gr >= 0 && gr < G && (r = recover(s + 1, gr))) return r;
+        }
+    }
+    // the library's stream continues after every kind's last chunk and the downloads
+    for (int k = 0; k < K; ++k) CK(cudaStreamWaitEvent(c->stream, evK(k, G - 1), 0));
+    if (hc_out) {
+        CK(cudaEventRecord(c->ev_chunk[ev_start], c->d2h));
+        CK(cudaStreamWaitEvent(c->stream, c->ev_chunk[ev_start], 0));
+    }
+    c->zone_updates += lay.nzones;
+    finish_step(c, dt);
+    return KNC_OK;
+}
+
+int advance_host_streamed(knc_ctx* c, const double* cons_in, const double* scalar_in, double* cons_out,
+                          double* scalar_out, int32_t fold) {
+    int r;
+    if ((r = update_ghost_geometry(c))) return r;
+    if ((r = reset_status(c, true))) return r;
+    double dt = 0.0;
+    if ((r = time_step_impl(c, &dt))) return r;
+    c->failed = false;
+    const int per_step = c->hp.runge_kutta_order;
+    for (int32_t k = 0; k < fold; ++k) {
+        if (c->stage_counter + per_step >= 0xffff) {
+            if ((r = check_status(c))) return r;
+            if ((r = reset_status(c, true))) return r;
+        }
+        const bool first = k == 0, last = k == fold - 1;
+        if (first || last)
+            r = stream_step(c, dt, first ? cons_in : nullptr, first ? scalar_in : nullptr, last ? cons_out : nullptr,
+                            last ? scalar_out : nullptr);
+        else
+            r = rk_step(c, dt);
+        if (r) return r;
+    }
+    return check_status(c);
+}
+
+}  // namespace
+
+int knc_advance_host(knc_ctx* c, const double* cons_in, const double* scalar_in, double* cons_out,
+                     double* scalar_out, int32_t fold) {
+    if (!c || !cons_in || !scalar_in || !cons_out || !scalar_out || fold < 0) return KNC_ERR_INVALID_ARGUMENT;
+    int r;
+    if ((r = check_ready(c))) return r;
+    if (c->mesh.moving())
+        return set_msg(c, KNC_ERR_INVALID_ARGUMENT,
+                       "advance_host: moving excision surfaces change the block set inside the fold; "
+                       "use knc_advance and knc_get_block");
+    if ((r = rebuild_table(c))) return r;
+    const bool adaptive = !(c->hp.system == KNC_SYSTEM_RELATIVISTIC && !c->hp.adaptive_time_step);
+    const bool pinned = device_view(cons_in) && device_view(scalar_in) && device_view(cons_out) &&
+                        device_view(scalar_out);
+    const bool streamed = pinned && fold > 0 && !adaptive && !c->fused && L(c).nremap == 0 &&
+                          c->model.kind != KNC_MODEL_HOST;
+    if (!streamed) {
+        // whole-state copies around the fold
+        if ((r = knc_set_state(c, cons_in, scalar_in))) return r;
+        if ((r = advance_impl(c, fold, nullptr))) return r;
+        return knc_get_state(c, cons_out, scalar_out);
+    }
+    r = advance_host_streamed(c, cons_in, scalar_in, cons_out, scalar_out, fold);
+    // the caller's buffers are free again when the call returns, on failure too
+    cudaStreamSynchronize(c->h2d);
+    cudaStreamSynchronize(c->d2h);
+    for (cudaStream_t st : c->kstreams) cudaStreamSynchronize(st);
+    cudaStreamSynchronize(c->stream);
+    if (r) c->failed = true;
+    return r;
+}
 
 int knc_set_profiling(knc_ctx* c, int32_t on) {
     if (!c) return KNC_ERR_INVALID_ARGUMENT;

@@ -185,6 +185,7 @@ SIGNATURES = {
     "knc_set_batched": (C.c_int, [_P, C.c_int32]),
     "knc_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
     "knc_advance_dt": (C.c_int, [_P, C.c_int32, C.c_double]),
+    "knc_advance_host": (C.c_int, [_P, _DP, _DP, _DP, _DP, C.c_int32]),
     "knc_zone_updates": (C.c_int, [_P, _I64P]),
     "knc_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
     "knc_autotune": (C.c_int, [_P, C.c_int32, C.POINTER(Tuning), _DP]),

@@ -241,6 +241,16 @@ class Solver:
         else:
             self._check(self.lib.knc_advance_dt(self.h, int(fold), float(dt)), "advance_dt")
 
+    def advance_host(self, cons, scalar, fold: int = 1, cons_out=None, scalar_out=None):
+        """scheme::advance on a host state (the whole-state arrays of
+        set_state): uploads it, advances `fold` steps, writes the new state to
+        cons_out / scalar_out (default: in place). Page-locked arrays
+        (PinnedArray) let the copies run beside the stages."""
+        co = cons if cons_out is None else cons_out
+        so = scalar if scalar_out is None else scalar_out
+        self._check(self.lib.knc_advance_host(self.h, abi.dptr(cons), abi.dptr(scalar), abi.dptr(co), abi.dptr(so),
+                                              int(fold)), "advance_host")
+
     def try_advance(self, fold: int = 1) -> int:
         return self.lib.knc_advance(self.h, int(fold))
 

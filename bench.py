@@ -17,7 +17,9 @@ Reported (one JSON line from rank 0):
   roofline     the dominant kernel of the headline path: algorithmic bytes per
                launch / its average CUDA-event duration, against measured HBM
   e2e          the same metric through the C ABI with host buffers: every step
-               uploads the state from pinned memory, advances, downloads it
+               is one knc_advance_host call, which takes the whole state from
+               pinned host memory and writes the new state back (uploads and
+               downloads by chunks of blocks, beside the stages)
   cpu_baseline the CPU oracle on this host's cores, bounded sample
 `--impl reference` times the CPU implementation of the path (the C++ oracle
 port; the reference's Rust crate has no toolchain here) on the same workload.
@@ -328,16 +330,12 @@ def run_knc(args):
     scal = knc.solver.PinnedArray((nb, w.mesh.block_size, w.mesh.num_polar_zones))
     head.get_state(cons.array, scal.array)
     for _ in range(args.warmup):
-        head.set_state(cons.array, scal.array)
-        head.advance(1)
-        head.get_state(cons.array, scal.array)
+        head.advance_host(cons.array, scal.array, 1)
     barrier(pg)
     head.mark(2)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        head.set_state(cons.array, scal.array)
-        head.advance(1)
-        head.get_state(cons.array, scal.array)
+        head.advance_host(cons.array, scal.array, 1)
     wall = time.perf_counter() - t0
     head.mark(3)
     e2e_ms = max_over_ranks(pg, max(head.elapsed_ms(2, 3), wall * 1e3))

@@ -228,6 +228,20 @@ int knc_advance(knc_ctx* ctx, int32_t fold);
  * one reduction the decomposition needs per advance. No counterpart in the
  * reference, which always advances the whole state. */
 int knc_advance_dt(knc_ctx* ctx, int32_t fold, double dt);
+/* scheme::advance (src/scheme.rs:212-240) in its own calling convention:
+ * the state goes in and a new state comes out, both in host memory (the
+ * whole-state layout of knc_set_state / knc_get_state; cons_out may alias
+ * cons_in and scalar_out scalar_in). Equivalent to knc_set_state, knc_advance,
+ * knc_get_state, and bitwise equal to them. The mesh must be fixed (moving
+ * excision surfaces change the block set, and so the arrays' size, inside
+ * the fold: KNC_ERR_INVALID_ARGUMENT). With page-locked buffers
+ * (knc_host_alloc or registered), a device model, no remaps, the fixed SRHD
+ * time step and the separate stage form, the first step's upload and the
+ * last step's download run by chunks of blocks beside the stages; otherwise
+ * the three calls run in turn. On failure the output buffers are unspecified
+ * and the state must be set again. */
+int knc_advance_host(knc_ctx* ctx, const double* cons_in, const double* scalar_in, double* cons_out,
+                     double* scalar_out, int32_t fold);
 
 /* Chosen forms. */
 int knc_set_precision(knc_ctx* ctx, int32_t precision);          /* KNC_PRECISION_* */

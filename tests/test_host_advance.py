@@ -1,0 +1,138 @@
+"""knc_advance_host: scheme::advance (src/scheme.rs:212-240) on a state held
+in host memory, the reference's own calling convention (state in, new state
+out).
+
+The streamed form (page-locked buffers) uploads the first step's state and
+downloads the last step's by chunks of blocks while the stages run; it must
+give bitwise the state, time and iteration of knc_set_state + knc_advance +
+knc_get_state, for every RK order, both precisions, each update form, folds
+of one and several steps, in place and into separate buffers, and with more
+blocks than chunks. Pageable buffers and uneven blocks take the whole-copy
+form, with the same result.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _solvers(w, precision, tuning=None):
+    import knc
+    out = []
+    for _ in range(2):
+        s = knc.build_solver(w)
+        s.set_precision(precision)
+        if tuning:
+            s.set_tuning(**tuning)
+        out.append(s)
+    return out
+
+
+def _host_state(s, pinned):
+    import knc
+    zones = sum(int(np.prod(s.shape_of(i))) for i in s.block_indexes())
+    if pinned:
+        keep = (knc.solver.PinnedArray((zones, 4)), knc.solver.PinnedArray((zones,)))
+        cons, scal = keep[0].array, keep[1].array
+    else:
+        keep = None
+        cons, scal = np.empty((zones, 4)), np.empty(zones)
+    s.get_state(cons, scal)
+    return keep, cons, scal
+
+
+def _by_copies(s, cons, scal, fold):
+    s.set_state(cons, scal)
+    s.advance(fold)
+    oc, os_ = np.empty_like(cons), np.empty_like(scal)
+    s.get_state(oc, os_)
+    return oc, os_
+
+
+def _check(w, precision, fold, tuning=None, pinned=True, in_place=True):
+    a, b = _solvers(w, precision, tuning)
+    for s in (a, b):
+        s.advance(2)   # a state with structure, the same on both
+    keep, cons, scal = _host_state(a, pinned)
+    ref_c, ref_s = _by_copies(b, cons.copy(), scal.copy(), fold)
+    if in_place:
+        a.advance_host(cons, scal, fold)
+        out_c, out_s = cons, scal
+    else:
+        import knc
+        in_c, in_s = cons.copy(), scal.copy()
+        outs = (knc.solver.PinnedArray(cons.shape), knc.solver.PinnedArray(scal.shape))
+        out_c, out_s = outs[0].array, outs[1].array
+        a.advance_host(cons, scal, fold, out_c, out_s)
+        assert np.array_equal(cons, in_c) and np.array_equal(scal, in_s)   # inputs untouched
+    assert np.array_equal(out_c, ref_c)
+    assert np.array_equal(out_s, ref_s)
+    assert _time_of(a) == _time_of(b)
+    # the device keeps the returned state
+    st = a.state()
+    off = 0
+    for i in a.block_indexes():
+        n = int(np.prod(a.shape_of(i)))
+        assert np.array_equal(st[i][0].reshape(-1, 4), out_c[off:off + n])
+        assert np.array_equal(st[i][1].reshape(-1), out_s[off:off + n])
+        off += n
+    del keep
+
+
+def _time_of(s):
+    import ctypes as C
+    t, n, d = C.c_double(), C.c_int64(), C.c_int64()
+    s.lib.knc_get_time(s.h, C.byref(t), C.byref(n), C.byref(d))
+    return t.value, n.value, d.value
+
+
+@pytest.mark.parametrize("order", ["RK1", "RK2", "RK3"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("fold", [1, 3])
+def test_streamed_matches_copies(order, precision, fold):
+    import knc
+    from knc import workloads
+    w = workloads.wind_small()
+    w.hydro.runge_kutta_order = order
+    prec = knc.abi.KNC_PRECISION_FP64 if precision == "fp64" else knc.abi.KNC_PRECISION_MIXED
+    _check(w, prec, fold)
+
+
+@pytest.mark.parametrize("tuning", [dict(tile_rows=8), dict(tile_rows=8, tma=True),
+                                    dict(tile_rows=16, strip=True, deferred=True)])
+def test_streamed_many_blocks_per_chunk(tuning):
+    """25 blocks of 8 x 32: chunks of one and two blocks."""
+    import knc
+    from knc import workloads
+    w = workloads.wind_small()
+    w.mesh.block_size = 8
+    w.mesh.num_polar_zones = 32
+    assert w.num_blocks > 16
+    _check(w, knc.abi.KNC_PRECISION_MIXED, 2, tuning)
+
+
+def test_streamed_separate_output():
+    import knc
+    from knc import workloads
+    _check(workloads.wind_small(), knc.abi.KNC_PRECISION_MIXED, 1, in_place=False)
+
+
+def test_whole_copy_forms():
+    """Pageable buffers, and uneven blocks (halo remaps)."""
+    import knc
+    from knc import workloads
+    _check(workloads.wind_small(), knc.abi.KNC_PRECISION_FP64, 2, pinned=False)
+    _check(workloads.uneven_small(moving=False), knc.abi.KNC_PRECISION_FP64, 2)
+
+
+def test_moving_mesh_rejected():
+    """The block set of a moving mesh changes inside the fold, so flat
+    whole-state arrays cannot hold the result: the call refuses."""
+    import knc
+    from knc import workloads
+    w = workloads.uneven_small()
+    a = knc.build_solver(w)
+    keep, cons, scal = _host_state(a, True)
+    with pytest.raises(knc.abi.KncError):
+        a.advance_host(cons, scal, 1)
+    del keep
