@@ -674,9 +674,15 @@ int rebuild_table(knc_ctx* c) {
             for (int64_t j0 = 0; j0 < b.nq; j0 += TILE_Q)
                 tiles.push_back(make_int4(slot, (int)i0, (int)j0, (int)zoff));
         if (c->uform == KNC_UPDATE_STRIP) {
+            // ceil(nr / utr) strips per column, their heights as even as
+            // whole rows allow (64 rows at utr 13: 13, 13, 13, 13, 12)
+            const int64_t per = (b.nr + c->utr - 1) / c->utr;
             for (int64_t j0 = 0; j0 < b.nq; j0 += STRIP_OUT)
-                for (int64_t i0 = 0; i0 < b.nr; i0 += c->utr)
-                    strips.push_back(make_int4(slot, (int)i0, (int)j0, (int)std::min<int64_t>(c->utr, b.nr - i0)));
+                for (int64_t k = 0, i0 = 0; k < per; ++k) {
+                    const int64_t rows = b.nr / per + (k < b.nr % per ? 1 : 0);
+                    strips.push_back(make_int4(slot, (int)i0, (int)j0, (int)rows));
+                    i0 += rows;
+                }
         } else {
             for (int64_t i0 = 0; i0 < b.nr; i0 += c->utr)
                 for (int64_t j0 = 0; j0 < b.nq; j0 += TILE_Q)
@@ -2258,8 +2264,9 @@ int knc_advance_host(knc_ctx* c, const double* cons_in, const double* scalar_in,
     const bool adaptive = !(c->hp.system == KNC_SYSTEM_RELATIVISTIC && !c->hp.adaptive_time_step);
     const bool pinned = device_view(cons_in) && device_view(scalar_in) && device_view(cons_out) &&
                         device_view(scalar_out);
+    // (the chunks update as warp strips, which need a polar grid)
     const bool streamed = pinned && fold > 0 && !adaptive && !c->fused && L(c).nremap == 0 &&
-                          c->model.kind != KNC_MODEL_HOST;
+                          c->model.kind != KNC_MODEL_HOST && c->mesh.p.num_polar_zones > 1;
     if (!streamed) {
         // whole-state copies around the fold
         if ((r = knc_set_state(c, cons_in, scalar_in))) return r;
@@ -2384,8 +2391,11 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
     CK(cudaMemcpy(&saved, c->d_status, sizeof(saved), cudaMemcpyDeviceToHost));
     const knc_tuning keep = {c->utr, c->fused, c->ctas_per_sm, c->uform, c->rform};
     std::vector<knc_tuning> cands;
+    // strip heights: powers of two and some between (the last wave of
+    // resident warps fills differently; measured on the 4096 x 1024 wind the
+    // spread from 8 to 20 rows is within 2%)
     if (c->mesh.p.num_polar_zones > 1)
-        for (int sr : {4, 8, 16, 32, 64})
+        for (int sr : {4, 8, 10, 12, 16, 20, 24, 32, 64})
             for (int mb : {4, 5, 6})
                 if (mixed(c) || mb == 4) cands.push_back({sr, 0, mb, KNC_UPDATE_STRIP});
     for (int tr : {4, 8, 16}) {

@@ -235,8 +235,9 @@ int knc_advance_dt(knc_ctx* ctx, int32_t fold, double dt);
  * knc_get_state, and bitwise equal to them. The mesh must be fixed (moving
  * excision surfaces change the block set, and so the arrays' size, inside
  * the fold: KNC_ERR_INVALID_ARGUMENT). With page-locked buffers
- * (knc_host_alloc or registered), a device model, no remaps, the fixed SRHD
- * time step and the separate stage form, the first step's upload and the
+ * (knc_host_alloc or registered), a device model, no remaps, more than one
+ * polar zone, the fixed SRHD time step and the separate stage form, the
+ * first step's upload and the
  * last step's download run by chunks of blocks beside the stages; otherwise
  * the three calls run in turn. On failure the output buffers are unspecified
  * and the state must be set again. */
