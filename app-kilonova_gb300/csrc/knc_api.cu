@@ -2052,7 +2052,12 @@ namespace {
 
 // Chunks of consecutive slots for the host-state advance, about equal in
 // zones, at most HOST_CHUNKS and at least one slot each: bounds[k] ..
-// bounds[k + 1] - 1 are chunk k's slots.
+// bounds[k + 1] - 1 are chunk k's slots. A chunk's download waits for the
+// upload of the 2S - 1 chunks after it (S stages, halo rows one chunk deep
+// per recovery and update). Measured on the 4096 x 1024 wind (64 blocks):
+// 16 chunks 1.55 ms per step, 8 chunks 1.60, 32 chunks 1.69; single blocks
+// at both ends with 8 larger chunks between 1.62 (the downloads then wait on
+// the larger chunks' uploads).
 constexpr int HOST_CHUNKS = 16;
 
 std::vector<int> chunk_bounds(const Layout& l) {
@@ -2106,11 +2111,11 @@ int stream_step(knc_ctx* c, double dt, const double* hc_in, const double* hs_in,
                 double* hs_out) {
     int r;
     const Layout& lay = L(c);
+    StagePlan p[3];
+    const int S = step_plan(c, dt, p);
     const std::vector<int> cb = chunk_bounds(lay);
     const int G = (int)cb.size() - 1;
     const int64_t total = lay.zone_off.back();
-    StagePlan p[3];
-    const int S = step_plan(c, dt, p);
     const int K = 2 * S;
     GhostArgs g[3];
     StageArgs a[3];
