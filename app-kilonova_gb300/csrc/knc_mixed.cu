@@ -29,6 +29,31 @@
 
 namespace knc {
 
+// Programmatic dependent launch: a kernel launched this way may be scheduled
+// while its predecessor on the stream is still running (after every CTA of
+// the predecessor has started and called launch_dependents); it blocks in
+// dependency_wait() until the predecessor has completed and its writes are
+// visible. The launch latency and the predecessor's tail then overlap.
+__device__ __forceinline__ void dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <class... Params, class... Args>
+static cudaError_t launch_chained(void (*k)(Params...), int grid, int block, size_t smem, cudaStream_t s,
+                                  Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
+
 // Newton-Raphson on the pressure, the reference's iteration rewritten with two
 // divisions: with X = tau + m (1 - W) + p (1 - W^2) and 1 - v^2 = 1/W^2,
 // rho e = X / W^2, f = (gamma - 1) rho e - p, rho h = m / W + rho e + p and
@@ -339,6 +364,8 @@ __global__ void __launch_bounds__(TILE_THREADS, 3) c2p_rows_kernel(StageArgs a) 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int WPC = TILE_THREADS / 32;
     __shared__ __align__(16) double sU[WPC][C2P_DEPTH][NFIELD][32];
+    dependency_wait();
+    launch_dependents();
     const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
     if (ek != NO_ERROR && (uint32_t)(ek >> 48) < (uint32_t)a.stage) return;
     MlpWeights& W = *reinterpret_cast<MlpWeights*>(smem_raw);   // unused without the learned guess
@@ -383,6 +410,8 @@ __global__ void __launch_bounds__(TILE_THREADS, 3) c2p_rows_kernel(StageArgs a) 
 template <bool MLP>
 __global__ void __launch_bounds__(TILE_THREADS, 2) c2p_high_kernel(StageArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    dependency_wait();
+    launch_dependents();
     const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
     if (blockIdx.x == 0 && threadIdx.x == 0) *a.high_count_next = 0u;
     if (ek != NO_ERROR && (uint32_t)(ek >> 48) < (uint32_t)a.stage) return;
@@ -452,14 +481,13 @@ cudaError_t launch_c2p_mixed(const StageArgs& a, cudaStream_t s) {
         // one warp per recovery tile
         const int wt = (a.ntiles + TILE_THREADS / 32 - 1) / (TILE_THREADS / 32);
         const int grid = std::min(wt, resident_grid(c2p_rows_kernel, TILE_THREADS, 0));
-        c2p_rows_kernel<<<grid, TILE_THREADS, 0, s>>>(a);
+        cudaError_t e = launch_chained(c2p_rows_kernel, grid, TILE_THREADS, 0, s, a);
+        if (e != cudaSuccess) return e;
         if (a.mlp) {
             const size_t bytes = sizeof(MlpWeights) + 8 * MLP_ACT_ELEMS * sizeof(__nv_bfloat16);
-            c2p_high_kernel<true><<<num_sms(), TILE_THREADS, bytes, s>>>(a);
-        } else {
-            c2p_high_kernel<false><<<num_sms(), TILE_THREADS, 0, s>>>(a);
+            return launch_chained(c2p_high_kernel<true>, num_sms(), TILE_THREADS, bytes, s, a);
         }
-        return cudaGetLastError();
+        return launch_chained(c2p_high_kernel<false>, num_sms(), TILE_THREADS, 0, s, a);
     }
     if (a.mlp) {
         const size_t bytes = sizeof(MlpWeights) + 8 * MLP_ACT_ELEMS * sizeof(__nv_bfloat16);
@@ -565,7 +593,7 @@ template <int MB>
 static void update_strips(const StageArgs& a, cudaStream_t s) {
     const int want = (a.nstrips + STRIP_WARPS - 1) / STRIP_WARPS;
     const int grid = std::min(want, resident_grid(update_strip_kernel<float, true, MB>, STRIP_WARPS * 32, 0));
-    update_strip_kernel<float, true, MB><<<grid, STRIP_WARPS * 32, 0, s>>>(a);
+    launch_chained(update_strip_kernel<float, true, MB>, grid, STRIP_WARPS * 32, 0, s, a);
 }
 
 cudaError_t launch_update_mixed(const StageArgs& a, cudaStream_t s) {

@@ -509,6 +509,10 @@ __device__ __forceinline__ void update_strip(const StageArgs& a, const int4 it, 
 // against fewer registers).
 template <class R, bool MIXED, int MB>
 __global__ void __launch_bounds__(STRIP_WARPS * 32, MB) update_strip_kernel(StageArgs a) {
+    // launched chained to the recovery (programmatic dependent launch): wait
+    // for it to complete, let the next stage's recovery be scheduled
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (*(volatile unsigned long long*)&a.status->err_key != NO_ERROR) return;
     const PhysT<R> ph = make_phys<R>(a);
     const int warp = blockIdx.x * STRIP_WARPS + (threadIdx.x >> 5);
