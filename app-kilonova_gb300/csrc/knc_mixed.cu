@@ -416,7 +416,8 @@ __global__ void __launch_bounds__(TILE_THREADS, 2) c2p_high_kernel(StageArgs a) 
     if (blockIdx.x == 0 && threadIdx.x == 0) *a.high_count_next = 0u;
     if (ek != NO_ERROR && (uint32_t)(ek >> 48) < (uint32_t)a.stage) return;
     const unsigned count = min(*(volatile unsigned*)a.high_count, a.high_cap);
-    if (count == 0u) return;
+    // CTAs without a group of the list stop before loading the network
+    if ((unsigned)blockIdx.x * TILE_THREADS >= count) return;
     MlpWeights& W = *reinterpret_cast<MlpWeights*>(smem_raw);
     __nv_bfloat16* act = reinterpret_cast<__nv_bfloat16*>(smem_raw + sizeof(MlpWeights)) +
                          (threadIdx.x >> 5) * MLP_ACT_ELEMS;

@@ -20,6 +20,12 @@ Reported (one JSON line from rank 0):
                is one knc_advance_host call, which takes the whole state from
                pinned host memory and writes the new state back (uploads and
                downloads by chunks of blocks, beside the stages)
+  batched_uneven  96 uneven blocks (nr 32..512, nq 64..256), RK3, both
+               excision surfaces at 0.5c: mixed + learned + graph vs FP64
+  learned_jet  the W = 100 jet on 2048 x 512: plain Newton from the
+               reference's guess vs the learned guess, in the mixed path and
+               in the FP64 path (iterations per zone, throughput, density L1
+               against the FP64 path)
   cpu_baseline the CPU oracle on this host's cores, bounded sample
 `--impl reference` times the CPU implementation of the path (the C++ oracle
 port; the reference's Rust crate has no toolchain here) on the same workload.
@@ -369,6 +375,39 @@ def run_knc(args):
         u64.close()
         uh.close()
 
+    # ---- the learned guess inside the W = 100 jet (2048 x 512), against plain
+    # Newton from the reference's guess: FP64 / FP32 iterations per zone and
+    # throughput, each path on its autotuned shape, density L1 against FP64
+    jet = None
+    if not args.no_jet:
+        wj = workloads.jet(seed=1 + rank)
+        j64 = make(False, False, False, workload=wj)
+        timed(j64, args.jet_steps, args.fold)
+        jet = {"workload": f"{wj.name}: relativistic jet, W = 100, theta_j = 0.1, p/rho = 1e-3, through r = 1 "
+                           "into a seeded r^-2 ambient, 2048x512 zones in 32 blocks of 64x512, RK2",
+               "zones": wj.zones, "steps": args.jet_steps}
+        for name, guess, mixed in (("plain_newton", False, True), ("learned_guess", True, True),
+                                   ("fp64_plain_newton", False, False), ("fp64_learned_guess", True, False)):
+            sj = make(mixed, guess, True, workload=wj, tune=True)
+            sj.reset_c2p_stats()
+            ms_j, _ = timed(sj, args.jet_steps, args.fold)
+            ms_j = max_over_ranks(pg, ms_j)
+            st = sj.c2p_stats()
+            jet[name] = {"value": wj.zones * args.jet_steps * world / (ms_j * 1e-3),
+                         "ms_per_step": ms_j / args.jet_steps,
+                         "fp64_iters_per_zone": st["iters_fp64"] / max(st["zones"], 1),
+                         "fp32_iters_per_zone": st["iters_fp32"] / max(st["zones"], 1),
+                         "fallbacks": st["fallbacks"], "l1_density": l1_density(sj, j64),
+                         "tuning": sj.tuning()}
+            sj.close()
+        j64.close()
+        # FP64 Newton iterations the learned start saves: in the mixed path
+        # (FP64 only for the zones above the split, started from the FP32
+        # root) and in the FP64 path (every zone, reference iteration)
+        for key, a_, b_ in (("fp64_iters_saved_mixed", "learned_guess", "plain_newton"),
+                            ("fp64_iters_saved_fp64_path", "fp64_learned_guess", "fp64_plain_newton")):
+            jet[key] = 1.0 - jet[a_]["fp64_iters_per_zone"] / max(jet[b_]["fp64_iters_per_zone"], 1e-30)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(w, args.cpu_blocks, args.cpu_steps)
@@ -410,6 +449,8 @@ def run_knc(args):
         }
         if un:
             line["batched_uneven"] = un
+        if jet:
+            line["learned_jet"] = jet
         if cpu:
             line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
         print(json.dumps(line), flush=True)
@@ -453,13 +494,15 @@ def main():
     ap.add_argument("--impl", default="knc", choices=["knc", "reference"])
     ap.add_argument("--fold", type=int, default=50)
     ap.add_argument("--w-split", type=float, default=2.0)
-    ap.add_argument("--train-pairs", type=int, default=2_000_000)
+    ap.add_argument("--train-pairs", type=int, default=10_000_000)
     ap.add_argument("--train-steps", type=int, default=3000)
     ap.add_argument("--cpu-blocks", type=int, default=16)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--ref-blocks", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-uneven", action="store_true")
+    ap.add_argument("--no-jet", action="store_true")
+    ap.add_argument("--jet-steps", type=int, default=100)
     ap.add_argument("--workload", default="wind_large", help="workload of --only runs")
     ap.add_argument("--tile-rows", type=int, default=0, help="launch shape of --only runs (0: default)")
     ap.add_argument("--fused", action="store_true")
