@@ -2590,7 +2590,12 @@ int knc_get_primitives(knc_ctx* c, int32_t index, double* prim) {
     a.stage = c->stage_counter++;
     a.sel_in = c->cur;
     a.sel_out = c->cur;
-    CK(launch_c2p_f64(a, c->stream));   // FP64 recovery, double primitives
+    // FP64 recovery of this block's tiles only, double primitives
+    const std::vector<int32_t>& si = L(c).slot_index;
+    const int slot = (int)(std::find(si.begin(), si.end(), index) - si.begin());
+    a.tiles = L(c).d_tiles + L(c).tile_off[slot];
+    a.ntiles = L(c).tile_off[slot + 1] - L(c).tile_off[slot];
+    CK(launch_c2p_f64(a, c->stream));
     ++c->launches;
     if ((r = check_status(c))) return r;
     const BlockH& b = it->second;

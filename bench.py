@@ -26,6 +26,9 @@ Reported (one JSON line from rank 0):
                reference's guess vs the learned guess, in the mixed path and
                in the FP64 path (iterations per zone, throughput, density L1
                against the FP64 path)
+  next_rows    the Newtonian sphere on the same grid (FP64, HLLC, adaptive
+               dt found inside the fold vs a separate time-step pass),
+               primitive export and CBOR checkpoint rates of the wind state
   cpu_baseline the CPU oracle on this host's cores, bounded sample
 `--impl reference` times the CPU implementation of the path (the C++ oracle
 port; the reference's Rust crate has no toolchain here) on the same workload.
@@ -240,6 +243,67 @@ def l1_density(a, b) -> float:
     return num / den
 
 
+def next_rows(args, make, timed, head, w):
+    """Measurements of the rows either side of the path (one GPU, rank 0)."""
+    import tempfile
+    import numpy as np
+    from knc import checkpoint, config, workloads
+    out = {}
+    # f4 and the Newtonian variant: sphere on 4096 x 1024, HLLC, FP64
+    ws = workloads.sphere_large(riemann="HLLC")
+    sph = make(False, False, True, workload=ws, tune=True)
+    steps, fold = args.next_steps, args.fold
+    ms_in, _ = timed(sph, steps, fold)
+    # f4 where it matters, folds of one step: dt found in the fold's first
+    # recovery (knc_advance) against the reference's order, a full recovery
+    # pass for State::time_step and then the step (knc_time_step + knc_advance_dt)
+    f4 = {}
+    for name, sep in (("dt_in_fold", False), ("separate_pass", True)):
+        sph.synchronize()
+        sph.mark(0)
+        for _ in range(args.next_steps // 2):
+            if sep:
+                sph.advance(1, sph.time_step())
+            else:
+                sph.advance(1)
+        sph.mark(1)
+        f4[name + "_ms_per_step"] = sph.elapsed_ms(0, 1) / (args.next_steps // 2)
+    out["newtonian_sphere"] = {
+        "workload": f"{ws.name}: Newtonian gamma 5/3 seeded density sphere (rho 10 inside r < 2, 1 outside, "
+                    "p 1e-2), 4096x1024 zones, HLLC, RK2, CFL 0.4, adaptive dt",
+        "path": "FP64, autotuned, CUDA graph per fold", "tuning": sph.tuning(),
+        "value": ws.zones * steps / (ms_in * 1e-3), "unit": UNIT, "ms_per_step": ms_in / steps,
+        "fold": fold, "steps": steps, "adaptive_dt_fold_of_one": f4}
+    sph.close()
+    # f3: primitive export of every block of the wind state (device -> host)
+    idx = head.block_indexes()
+    head.synchronize()
+    t0 = time.perf_counter()
+    prims = [head.get_primitives(i) for i in idx]
+    el = time.perf_counter() - t0
+    nbytes = sum(p.nbytes for p in prims)
+    out["primitive_export"] = {"blocks": len(idx), "bytes": nbytes, "seconds": el,
+                               "GB_per_s": nbytes / el / 1e9}
+    # f1: CBOR checkpoint of the wind state, written and read back (host)
+    ctl = config.Control(start_time=0.0, final_time=1.0, checkpoint_interval=0.1, fold=fold)
+    with tempfile.TemporaryDirectory() as d:
+        path = Path(d) / "chkpt.0000.cbor"
+        t0 = time.perf_counter()
+        checkpoint.write_checkpoint(path, head, w.hydro, "wind", {}, w.mesh, ctl)
+        t_w = time.perf_counter() - t0
+        size = path.stat().st_size
+        t0 = time.perf_counter()
+        ck = checkpoint.read_checkpoint(path)
+        t_r = time.perf_counter() - t0
+        st = head.state()
+        same = all(np.array_equal(ck.blocks[i][0], st[i][0]) and np.array_equal(ck.blocks[i][1], st[i][1])
+                   for i in st)
+    out["checkpoint"] = {"bytes": size, "write_s": t_w, "read_s": t_r, "write_MB_per_s": size / t_w / 1e6,
+                         "read_MB_per_s": size / t_r / 1e6, "round_trip_equal": same,
+                         "note": "state download plus CBOR encoding on the host (numpy), one thread"}
+    return out
+
+
 def run_knc(args):
     import numpy as np
     import knc
@@ -408,6 +472,13 @@ def run_knc(args):
                             ("fp64_iters_saved_fp64_path", "fp64_learned_guess", "fp64_plain_newton")):
             jet[key] = 1.0 - jet[a_]["fp64_iters_per_zone"] / max(jet[b_]["fp64_iters_per_zone"], 1e-30)
 
+    # ---- the rows around the path: the Newtonian sphere of the same grid
+    # (FP64, HLLC, adaptive dt found inside the fold) against the separate
+    # time-step pass, primitive export and CBOR checkpoints of the wind state
+    nxt = None
+    if not args.no_next and rank == 0:
+        nxt = next_rows(args, make, timed, head, w)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(w, args.cpu_blocks, args.cpu_steps)
@@ -451,6 +522,8 @@ def run_knc(args):
             line["batched_uneven"] = un
         if jet:
             line["learned_jet"] = jet
+        if nxt:
+            line["next_rows"] = nxt
         if cpu:
             line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
         print(json.dumps(line), flush=True)
@@ -502,6 +575,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-uneven", action="store_true")
     ap.add_argument("--no-jet", action="store_true")
+    ap.add_argument("--no-next", action="store_true")
+    ap.add_argument("--next-steps", type=int, default=50)
     ap.add_argument("--jet-steps", type=int, default=100)
     ap.add_argument("--workload", default="wind_large", help="workload of --only runs")
     ap.add_argument("--tile-rows", type=int, default=0, help="launch shape of --only runs (0: default)")

@@ -1199,6 +1199,28 @@ int oracle_get_block(oracle_ctx* c, int32_t index, double* cons, double* scalar)
     return KNC_OK;
 }
 
+// The primitive export of one block (Products::try_from_state,
+// src/products.rs:43-66, via BlockState::try_to_primitive, state.rs:76-94):
+// [nr][nq][5] = (rho, u_r, u_theta, p, scalar concentration s / rho).
+int oracle_get_primitives(oracle_ctx* c, int32_t index, double* prim) {
+    if (!c || !prim) return KNC_ERR_INVALID_ARGUMENT;
+    auto it = c->blocks.find(index);
+    if (it == c->blocks.end()) return KNC_ERR_NO_BLOCK;
+    const Geometry& G = geometry_of(c, index);
+    PrimBlock pb;
+    ErrorRec e;
+    if (!block_to_primitive(c, index, it->second, G, pb, e)) {
+        c->err = e;
+        return KNC_ERR_HYDRO;
+    }
+    const int64_t n = G.nr * G.nq;
+    for (int64_t z = 0; z < n; ++z) {
+        for (int q = 0; q < 4; ++q) prim[z * 5 + q] = pb.P[z].v[q];
+        prim[z * 5 + 4] = pb.s[z] / pb.P[z].v[0];
+    }
+    return KNC_OK;
+}
+
 int oracle_num_blocks(const oracle_ctx* c, int32_t* n) {
     if (!c || !n) return KNC_ERR_INVALID_ARGUMENT;
     *n = (int32_t)c->blocks.size();

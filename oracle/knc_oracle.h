@@ -44,6 +44,8 @@ int oracle_set_block_shapes(oracle_ctx* ctx, int32_t first, int32_t count, const
 int oracle_block_shape_of(const oracle_ctx* ctx, int32_t index, int64_t* nr, int64_t* nq);
 int oracle_get_block(oracle_ctx* ctx, int32_t index, double* cons_aos,
                      double* scalar_mass);
+/* [nr][nq][5] = (rho, u_r, u_theta, p, scalar concentration) of a block. */
+int oracle_get_primitives(oracle_ctx* ctx, int32_t index, double* prim);
 int oracle_num_blocks(const oracle_ctx* ctx, int32_t* n);
 int oracle_block_indexes(const oracle_ctx* ctx, int32_t* out, int32_t capacity);
 int oracle_set_time(oracle_ctx* ctx, double time, int64_t num, int64_t den);

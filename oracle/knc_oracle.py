@@ -49,6 +49,7 @@ def load():
         "oracle_set_block_shapes": (C.c_int, [P, C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
         "oracle_block_shape_of": (C.c_int, [P, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
         "oracle_get_block": (C.c_int, [P, C.c_int32, DP, DP]),
+        "oracle_get_primitives": (C.c_int, [P, C.c_int32, DP]),
         "oracle_num_blocks": (C.c_int, [P, C.POINTER(C.c_int32)]),
         "oracle_block_indexes": (C.c_int, [P, C.POINTER(C.c_int32), C.c_int32]),
         "oracle_set_time": (C.c_int, [P, C.c_double, C.c_int64, C.c_int64]),
@@ -159,6 +160,13 @@ class Oracle:
 
     def state(self):
         return {i: self.get_block(i) for i in self.block_indexes()}
+
+    def get_primitives(self, index):
+        """(rho, u_r, u_theta, p, scalar concentration) of a block, [nr, nq, 5]."""
+        nr, nq = self.shape_of(index)
+        out = np.empty((nr, nq, 5))
+        self._check(self.lib.oracle_get_primitives(self.h, index, _d(out)), "get_primitives")
+        return out
 
     def set_time(self, t, num=0, den=1):
         self._check(self.lib.oracle_set_time(self.h, t, num, den), "set_time")

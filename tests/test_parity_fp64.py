@@ -186,3 +186,19 @@ def test_state_roundtrip_page_locked(name):
     st2 = g.state()
     for i in idx:
         assert np.array_equal(st[i][0], st2[i][0]) and np.array_equal(st[i][1], st2[i][1])
+
+
+@pytest.mark.parametrize("name", ["wind_small", "sphere_small", "uneven_small"])
+def test_primitive_export_matches_oracle(name):
+    """knc_get_primitives (the primitive export of Products::try_from_state,
+    src/products.rs:43-66) against the oracle's, block by block, bit for bit;
+    each call recovers only the requested block."""
+    from knc import workloads
+    w = getattr(workloads, name)()
+    g, o = make_pair(w)
+    g.advance(3)
+    o.advance(3)
+    n0 = g.launch_count()
+    for i in o.block_indexes():
+        assert np.array_equal(g.get_primitives(i), o.get_primitives(i)), i
+    assert g.launch_count() - n0 == 2 * len(o.block_indexes())   # recovery + layout change per block
