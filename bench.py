@@ -14,6 +14,7 @@ Reported (one JSON line from rank 0):
   l1_density   L1 error of the comoving density of the mixed path against the
                FP64 path after the same steps (the FP64 path equals the CPU
                oracle to 1e-12, so this is the error against the FP64 oracle)
+  errors_vs_fp64  relative L1 and Linf per conserved field, same comparison
   roofline     the dominant kernel of the headline path: algorithmic bytes per
                launch / its average CUDA-event duration, against measured HBM
   e2e          the same metric through the C ABI with host buffers: every step
@@ -304,6 +305,36 @@ def next_rows(args, make, timed, head, w):
     return out
 
 
+FIELDS = ("D", "S_r", "S_theta", "tau", "scalar_mass")
+
+
+def field_errors(a, b) -> dict:
+    """Per conserved field of solver a against solver b (same blocks):
+    relative L1 = sum |a - b| / sum |b| and relative Linf = max |a - b| / max |b|,
+    with the momentum magnitude |S| as the scale of both momentum components
+    (S_theta of a radial flow is rounding noise around zero)."""
+    import numpy as np
+    num = np.zeros(5)
+    den = np.zeros(5)
+    mx = np.zeros(5)
+    mb = np.zeros(5)
+    for i in b.block_indexes():
+        ca, sa = a.get_block(i)
+        cb, sb = b.get_block(i)
+        smag = np.hypot(cb[..., 1], cb[..., 2])
+        for q in range(5):
+            x = ca[..., q] if q < 4 else sa
+            y = cb[..., q] if q < 4 else sb
+            scale = smag if q in (1, 2) else np.abs(y)
+            d = np.abs(x - y)
+            num[q] += float(d.sum())
+            den[q] += float(scale.sum())
+            mx[q] = max(mx[q], float(d.max()))
+            mb[q] = max(mb[q], float(scale.max()))
+    return {FIELDS[q]: {"l1": num[q] / den[q] if den[q] else 0.0, "linf": mx[q] / mb[q] if mb[q] else 0.0}
+            for q in range(5)}
+
+
 def run_knc(args):
     import numpy as np
     import knc
@@ -375,6 +406,7 @@ def run_knc(args):
     msh = max_over_ranks(pg, msh)
     value = zones * args.steps * world / (msh * 1e-3)
     l1 = l1_density(head, fp64)
+    errs = field_errors(head, fp64)
 
     # ---- same path without the graph, kernels timed with events (roofline)
     prof = make(True, True, False)
@@ -462,6 +494,7 @@ def run_knc(args):
                          "fp64_iters_per_zone": st["iters_fp64"] / max(st["zones"], 1),
                          "fp32_iters_per_zone": st["iters_fp32"] / max(st["zones"], 1),
                          "fallbacks": st["fallbacks"], "l1_density": l1_density(sj, j64),
+                         "errors_vs_fp64": field_errors(sj, j64) if mixed else None,
                          "tuning": sj.tuning()}
             sj.close()
         j64.close()
@@ -500,6 +533,7 @@ def run_knc(args):
                      "fp64_peak_gflops": fp64_peak},
             "speedup_vs_fp64": value / v64,
             "l1_density": l1,
+            "errors_vs_fp64": errs,
             "c2p": {"fp64_iters_per_zone": sth["iters_fp64"] / max(sth["zones"], 1),
                     "fp32_iters_per_zone": sth["iters_fp32"] / max(sth["zones"], 1),
                     "fallbacks": sth["fallbacks"], "mlp_train_loss": train_loss, "mlp_train_s": train_s},
