@@ -136,3 +136,37 @@ def test_moving_mesh_rejected():
     with pytest.raises(knc.abi.KncError):
         a.advance_host(cons, scal, 1)
     del keep
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+@pytest.mark.parametrize("field,value,kind", [(0, -1.0, "NegativeDensity"), (3, -1e-3, "NegativeEnergyDensity")])
+def test_failure_reported_like_the_copies(pinned, field, value, kind):
+    """A poisoned zone in the host state fails the host-state advance at the
+    zone the oracle reports (stage 0), in the streamed and the whole-copy
+    form; the context then refuses to go on until a state is set again."""
+    import knc
+    from helpers import make_pair
+    from knc import workloads
+    w = workloads.wind_small()
+    g, o = make_pair(w)
+    keep, cons, scal = _host_state(g, pinned)
+    nr, nq = g.shape_of(2)
+    z = 2 * nr * nq + 5 * nq + 7          # block 2, zone (5, 7)
+    cons[z, field] = value
+    c2, s2 = o.get_block(2)
+    c2 = c2.copy()
+    c2[5, 7, field] = value
+    o.add_block(2, c2, s2)
+    assert o.try_advance(1) == 5
+    eo = o.last_error()
+    with pytest.raises(knc.HydroError) as exc:
+        g.advance_host(cons, scal, 1)
+    e = exc.value.error
+    assert e["kind"] == kind
+    assert (e["block"], e["i"], e["j"]) == (eo.block, eo.i, eo.j) == (2, 5, 7)
+    assert e["r"] == eo.r and e["theta"] == eo.theta
+    with pytest.raises(knc.HydroError):
+        g.advance(1)
+    g.init_from_model(0.0)
+    g.advance(1)
+    del keep
