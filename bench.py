@@ -12,8 +12,9 @@ Reported (one JSON line from rank 0):
   fp64         the plain FP64 path on the same workload, and the FP64 pipe
                fraction it reaches (against the FP64 FMA rate measured here)
   l1_density   L1 error of the comoving density of the mixed path against the
-               FP64 path after the same steps (the FP64 path equals the CPU
-               oracle to 1e-12, so this is the error against the FP64 oracle)
+               FP64 path after the workload's 200 steps (the FP64 path equals
+               the CPU oracle to 1e-12, so this is the error against the FP64
+               oracle); l1_density_after_run: after this run's steps
   errors_vs_fp64  relative L1 and Linf per conserved field, same comparison
   roofline     the dominant kernel of the headline path: algorithmic bytes per
                launch / its average CUDA-event duration, against measured HBM
@@ -59,6 +60,7 @@ UNIT = "zone-updates/s"
 # the recovery and the update (FP32, written once and read once per stage:
 # 40 B per stage) are an intermediate of the implementation, reported apart.
 ALG_BYTES_UPDATE_LAUNCH = 100.0
+ACCURACY_STEPS = 200   # the wind workload's configured step count
 ALG_BYTES_RECOVERY_LAUNCH = 40.0
 ALG_BYTES_PER_ZONE_UPDATE = 200.0
 INTERMEDIATE_BYTES_PER_ZONE_UPDATE = 2 * 40.0 + 2 * 20.0 + 2 * 20.0   # U re-read by the recovery, P written and read
@@ -405,8 +407,25 @@ def run_knc(args):
     sth = head.c2p_stats()
     msh = max_over_ranks(pg, msh)
     value = zones * args.steps * world / (msh * 1e-3)
-    l1 = l1_density(head, fp64)
-    errs = field_errors(head, fp64)
+    l1_run = l1_density(head, fp64)   # after this run's warm-up + timed steps
+    # the accuracy gate at the workload's own step count (200 RK2 steps),
+    # whatever --steps this run timed: a fresh pair of solvers
+    if args.steps + args.warmup == ACCURACY_STEPS:
+        acc_m, acc_64 = head, fp64
+    else:
+        acc_m, acc_64 = make(True, True, True), make(False, False, True)
+        acc_m.set_tuning(**tuning)
+        for s_ in (acc_m, acc_64):
+            for _ in range(ACCURACY_STEPS // args.fold):
+                s_.advance(args.fold)
+            if ACCURACY_STEPS % args.fold:
+                s_.advance(ACCURACY_STEPS % args.fold)
+    l1 = l1_density(acc_m, acc_64)
+    errs = field_errors(acc_m, acc_64)
+    acc_steps = ACCURACY_STEPS
+    if acc_m is not head:
+        acc_m.close()
+        acc_64.close()
 
     # ---- same path without the graph, kernels timed with events (roofline)
     prof = make(True, True, False)
@@ -534,6 +553,8 @@ def run_knc(args):
             "speedup_vs_fp64": value / v64,
             "l1_density": l1,
             "errors_vs_fp64": errs,
+            "accuracy_steps": acc_steps,
+            "l1_density_after_run": l1_run,
             "c2p": {"fp64_iters_per_zone": sth["iters_fp64"] / max(sth["zones"], 1),
                     "fp32_iters_per_zone": sth["iters_fp32"] / max(sth["zones"], 1),
                     "fallbacks": sth["fallbacks"], "mlp_train_loss": train_loss, "mlp_train_s": train_s},
