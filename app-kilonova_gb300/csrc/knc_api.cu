@@ -2577,6 +2577,49 @@ int knc_elapsed_ms(knc_ctx* c, int32_t a, int32_t b, double* ms) {
     return KNC_OK;
 }
 
+namespace {
+// FP64 recovery of one block's tiles into its (double) primitive array.
+int recover_block_f64(knc_ctx* c, int32_t index) {
+    int r;
+    if ((r = check_ready(c))) return r;
+    if ((r = rebuild_table(c))) return r;
+    if ((r = reset_status(c, true))) return r;
+    StageArgs a = base_args(c);
+    a.mlp = nullptr;
+    a.stage = c->stage_counter++;
+    a.sel_in = c->cur;
+    a.sel_out = c->cur;
+    const std::vector<int32_t>& si = L(c).slot_index;
+    const int slot = (int)(std::find(si.begin(), si.end(), index) - si.begin());
+    a.tiles = L(c).d_tiles + L(c).tile_off[slot];
+    a.ntiles = L(c).tile_off[slot + 1] - L(c).tile_off[slot];
+    CK(launch_c2p_f64(a, c->stream));
+    ++c->launches;
+    return check_status(c);
+}
+}  // namespace
+
+int knc_get_products(knc_ctx* c, int32_t index, double* radial_vertices, double* polar_vertices,
+                     double* primitive, double* scalar) {
+    if (!c) return KNC_ERR_INVALID_ARGUMENT;
+    auto it = c->blocks.find(index);
+    if (it == c->blocks.end()) return set_msg(c, KNC_ERR_NO_BLOCK, "no block %d", index);
+    const BlockH& b = it->second;
+    if (radial_vertices) std::memcpy(radial_vertices, b.geom.rv.data(), b.geom.rv.size() * sizeof(double));
+    if (polar_vertices) std::memcpy(polar_vertices, b.geom.qv.data(), b.geom.qv.size() * sizeof(double));
+    if (!primitive && !scalar) return KNC_OK;
+    int r;
+    if ((r = recover_block_f64(c, index))) return r;
+    const size_t n = (size_t)(b.nr * b.nq);
+    if ((r = ensure_stage(c, 5 * n))) return r;
+    CK(launch_products(b.P, b.buf[c->cur], c->d_stage, c->d_stage + 4 * n, b.nr, b.nq, c->stream));
+    ++c->launches;
+    if (primitive) CK(cudaMemcpyAsync(primitive, c->d_stage, 4 * n * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (scalar) CK(cudaMemcpyAsync(scalar, c->d_stage + 4 * n, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return KNC_OK;
+}
+
 int knc_get_primitives(knc_ctx* c, int32_t index, double* prim) {
     if (!c || !prim) return KNC_ERR_INVALID_ARGUMENT;
     auto it = c->blocks.find(index);

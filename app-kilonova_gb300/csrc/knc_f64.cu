@@ -252,7 +252,32 @@ __global__ void prims_to_aos_kernel(const double* __restrict__ P, double* __rest
     for (int q = 0; q < 5; ++q) out[z * 5 + q] = v[q];
 }
 
+// BlockProducts of a block: the recovered (double) primitives of the padded
+// array in AnyPrimitive order, and scalar_mass / lab_frame_mass from the
+// volume-integrated state U (src/products.rs:50-58).
+__global__ void products_kernel(const double* __restrict__ P, const double* __restrict__ U,
+                                double* __restrict__ prim, double* __restrict__ scalar, int64_t nr, int64_t nq) {
+    const int64_t z = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = nr * nq;
+    if (z >= n) return;
+    const int64_t pn = (nr + 4) * nq;
+    const int64_t off = 2 * nq + z;
+    prim[z * 4 + 0] = P[pn + off];       // velocity_r
+    prim[z * 4 + 1] = P[2 * pn + off];   // velocity_q
+    prim[z * 4 + 2] = P[off];            // mass_density
+    prim[z * 4 + 3] = P[3 * pn + off];   // gas_pressure
+    scalar[z] = U[4 * n + z] / U[z];
+}
+
 // ---- launchers ---------------------------------------------------------------
+cudaError_t launch_products(const void* P, const double* U, double* prim, double* scalar, int64_t nr, int64_t nq,
+                            cudaStream_t s) {
+    const int64_t n = nr * nq;
+    products_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(reinterpret_cast<const double*>(P), U, prim, scalar,
+                                                                  nr, nq);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_prims_to_aos(const void* P, double* out, int64_t nr, int64_t nq, cudaStream_t s) {
     const int64_t n = nr * nq;
     prims_to_aos_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(reinterpret_cast<const double*>(P), out, nr, nq);

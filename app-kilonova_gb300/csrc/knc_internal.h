@@ -235,6 +235,8 @@ cudaError_t launch_state_in(const DevBlock* blocks, const int4* tiles, int ntile
 cudaError_t launch_state_out(const DevBlock* blocks, const int4* tiles, int ntiles, int sel, double* cons,
                              double* scalar, cudaStream_t s);
 cudaError_t launch_prims_to_aos(const void* P, double* out, int64_t nr, int64_t nq, cudaStream_t s);
+cudaError_t launch_products(const void* P, const double* U, double* prim, double* scalar, int64_t nr, int64_t nq,
+                            cudaStream_t s);
 cudaError_t launch_soa_to_aos(const double* soa, double* aos, double* scalar, int64_t nr, int64_t nq,
                               cudaStream_t s);
 cudaError_t launch_sample_pairs(const DevBlock* blocks, const int4* tiles, int ntiles, int sel, int stride, double gm,

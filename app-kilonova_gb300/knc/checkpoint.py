@@ -1,4 +1,5 @@
-"""CBOR checkpoints in the reference's `App` layout.
+"""CBOR checkpoints in the reference's `App` layout, and products files in its
+`Products` layout.
 
 The reference writes `App { state, tasks, config, version }` (src/app.rs:181-186)
 with serde and ciborium 0.1 (src/io.rs:24-35), and restarts from it
@@ -318,6 +319,53 @@ def app_document(blocks: dict, time: float, iteration, hydro, model_name: str, m
             "config": {"hydro": _hydro_doc(hydro), "model": {model_name: dict(model_params)},
                        "mesh": _mesh_doc(mesh), "control": _control_doc(control)},
             "version": version}
+
+
+def _array1(a: np.ndarray):
+    return {"v": 1, "dim": [int(a.size)], "data": F64Array(np.asarray(a, dtype=np.float64).reshape(-1))}
+
+
+def products_document(blocks: dict, time: float, hydro, model_name: str, model_params: dict, mesh: cfg.Mesh,
+                      control: cfg.Control, version: str = VERSION):
+    """Products { time, blocks, config, version } (src/products.rs:30-36).
+    blocks: {index: BlockProducts dict as Solver.get_products returns it}:
+    radial / polar vertices (Array1), primitive (Array2 of AnyPrimitive, which
+    serialises as [velocity_r, velocity_q, mass_density, gas_pressure],
+    physics/mod.rs:36-63) and scalar (Array2)."""
+    out = {}
+    for i, b in sorted(blocks.items()):
+        out[(int(i), 0)] = {"radial_vertices": _array1(b["radial_vertices"]),
+                            "polar_vertices": _array1(b["polar_vertices"]),
+                            "primitive": _ndarray(np.asarray(b["primitive"]), True),
+                            "scalar": _ndarray(np.asarray(b["scalar"]), False)}
+    return {"time": float(time), "blocks": out,
+            "config": {"hydro": _hydro_doc(hydro), "model": {model_name: dict(model_params)},
+                       "mesh": _mesh_doc(mesh), "control": _control_doc(control)},
+            "version": version}
+
+
+def write_products(path, solver, hydro, model_name, model_params, mesh, control):
+    """Products::try_from_state + io::write_cbor (src/main.rs:51-56, the
+    prods.NNNN.cbor files) for a Solver's live state: every block's primitives
+    recovered in FP64 on the device."""
+    t, _ = solver.time()
+    blocks = {i: solver.get_products(i) for i in solver.block_indexes()}
+    Path(path).write_bytes(dumps(products_document(blocks, t, hydro, model_name, model_params, mesh, control)))
+
+
+def read_products(path) -> dict:
+    """A prods file back as {"time", "blocks": {index: BlockProducts arrays},
+    "config", "version"}."""
+    doc = loads(Path(path).read_bytes())
+    blocks = {}
+    for key, b in doc["blocks"].items():
+        index = int(key[0]) if isinstance(key, tuple) else int(key)
+        nr, nq = b["primitive"]["dim"]
+        blocks[index] = {"radial_vertices": np.asarray(b["radial_vertices"]["data"], dtype=np.float64),
+                         "polar_vertices": np.asarray(b["polar_vertices"]["data"], dtype=np.float64),
+                         "primitive": np.asarray(b["primitive"]["data"], dtype=np.float64).reshape(nr, nq, 4),
+                         "scalar": np.asarray(b["scalar"]["data"], dtype=np.float64).reshape(nr, nq)}
+    return {"time": float(doc["time"]), "blocks": blocks, "config": doc["config"], "version": doc["version"]}
 
 
 def write_checkpoint(path, solver, hydro, model_name, model_params, mesh, control, tasks=None):

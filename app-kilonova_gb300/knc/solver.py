@@ -193,6 +193,17 @@ class Solver:
     def get_state(self, cons, scalar):
         self._check(self.lib.knc_get_state(self.h, abi.dptr(cons), abi.dptr(scalar)), "get_state")
 
+    def get_products(self, index: int) -> dict:
+        """BlockProducts::try_from_block_state (src/products.rs:43-66): radial
+        and polar vertices, primitive [nr, nq, 4] in AnyPrimitive order
+        (velocity_r, velocity_q, mass_density, gas_pressure), scalar [nr, nq]."""
+        nr, nq = self.shape_of(index)
+        rv, qv = np.empty(nr + 1), np.empty(nq + 1)
+        prim, scal = np.empty((nr, nq, 4)), np.empty((nr, nq))
+        self._check(self.lib.knc_get_products(self.h, int(index), abi.dptr(rv), abi.dptr(qv), abi.dptr(prim),
+                                              abi.dptr(scal)), "get_products")
+        return {"radial_vertices": rv, "polar_vertices": qv, "primitive": prim, "scalar": scal}
+
     def get_primitives(self, index: int):
         """(rho, u_r, u_theta, p, scalar concentration) of a block, [nr, nq, 5]."""
         out = np.empty(self.shape_of(index) + (5,))

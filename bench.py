@@ -287,6 +287,16 @@ def next_rows(args, make, timed, head, w):
     nbytes = sum(p.nbytes for p in prims)
     out["primitive_export"] = {"blocks": len(idx), "bytes": nbytes, "seconds": el,
                                "GB_per_s": nbytes / el / 1e9}
+    # f3 in the reference's own form: a prods.NNNN.cbor file (Products,
+    # src/main.rs:51-56) of the wind state, BlockProducts recovered on the device
+    ctl_p = config.Control(start_time=0.0, final_time=1.0, checkpoint_interval=0.1, fold=fold)
+    with tempfile.TemporaryDirectory() as d:
+        path = Path(d) / "prods.0000.cbor"
+        t0 = time.perf_counter()
+        checkpoint.write_products(path, head, w.hydro, "wind", {}, w.mesh, ctl_p)
+        t_p = time.perf_counter() - t0
+        out["products_file"] = {"bytes": path.stat().st_size, "seconds": t_p,
+                                "MB_per_s": path.stat().st_size / t_p / 1e6}
     # f1: CBOR checkpoint of the wind state, written and read back (host)
     ctl = config.Control(start_time=0.0, final_time=1.0, checkpoint_interval=0.1, fold=fold)
     with tempfile.TemporaryDirectory() as d:

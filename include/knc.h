@@ -208,6 +208,15 @@ int knc_get_state(knc_ctx* ctx, double* cons_aos, double* scalar_mass);
  * `Products::try_from_state` exports (src/products.rs:43-66): [nr][nq][5] as
  * (rho, u_r, u_theta, p, scalar concentration). */
 int knc_get_primitives(knc_ctx* ctx, int32_t index, double* prim);
+/* BlockProducts::try_from_block_state (src/products.rs:43-66) of one block,
+ * in the reference's layout: radial_vertices [nr+1], polar_vertices [nq+1],
+ * primitive [nr][nq][4] in AnyPrimitive order (velocity_r, velocity_q,
+ * mass_density, gas_pressure; four-velocity components for relativistic
+ * hydro, physics/mod.rs:36-63), scalar [nr][nq] = scalar_mass /
+ * lab_frame_mass of the volume-integrated state. The primitives are recovered
+ * in FP64 from the live state; any output may be NULL. */
+int knc_get_products(knc_ctx* ctx, int32_t index, double* radial_vertices, double* polar_vertices,
+                     double* primitive, double* scalar);
 
 /* State.time and State.iteration (Rational64 as num/den), src/state.rs:39-43 */
 int knc_set_time(knc_ctx* ctx, double time, int64_t iter_num, int64_t iter_den);

@@ -1221,6 +1221,38 @@ int oracle_get_primitives(oracle_ctx* c, int32_t index, double* prim) {
     return KNC_OK;
 }
 
+// BlockProducts::try_from_block_state (src/products.rs:43-66) of one block:
+// the block's vertices, its primitives in AnyPrimitive order (velocity_r,
+// velocity_q, mass_density, gas_pressure) and scalar_mass / lab_frame_mass of
+// the volume-integrated state.
+int oracle_get_products(oracle_ctx* c, int32_t index, double* rv, double* qv, double* prim, double* scalar) {
+    if (!c) return KNC_ERR_INVALID_ARGUMENT;
+    auto it = c->blocks.find(index);
+    if (it == c->blocks.end()) return KNC_ERR_NO_BLOCK;
+    const Geometry& G = geometry_of(c, index);
+    if (rv) std::memcpy(rv, G.rv.data(), G.rv.size() * sizeof(double));
+    if (qv) std::memcpy(qv, G.qv.data(), G.qv.size() * sizeof(double));
+    if (!prim && !scalar) return KNC_OK;
+    PrimBlock pb;
+    ErrorRec e;
+    if (!block_to_primitive(c, index, it->second, G, pb, e)) {
+        c->err = e;
+        return KNC_ERR_HYDRO;
+    }
+    const Block& B = it->second;
+    const int64_t n = G.nr * G.nq;
+    for (int64_t z = 0; z < n; ++z) {
+        if (prim) {
+            prim[z * 4 + 0] = pb.P[z].v[1];
+            prim[z * 4 + 1] = pb.P[z].v[2];
+            prim[z * 4 + 2] = pb.P[z].v[0];
+            prim[z * 4 + 3] = pb.P[z].v[3];
+        }
+        if (scalar) scalar[z] = B.S[z] / B.U[z * 4 + 0];
+    }
+    return KNC_OK;
+}
+
 int oracle_num_blocks(const oracle_ctx* c, int32_t* n) {
     if (!c || !n) return KNC_ERR_INVALID_ARGUMENT;
     *n = (int32_t)c->blocks.size();

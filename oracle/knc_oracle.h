@@ -46,6 +46,9 @@ int oracle_get_block(oracle_ctx* ctx, int32_t index, double* cons_aos,
                      double* scalar_mass);
 /* [nr][nq][5] = (rho, u_r, u_theta, p, scalar concentration) of a block. */
 int oracle_get_primitives(oracle_ctx* ctx, int32_t index, double* prim);
+/* BlockProducts of a block: vertices [nr+1], [nq+1]; primitive [nr][nq][4] in
+ * AnyPrimitive order; scalar [nr][nq] = scalar_mass / lab_frame_mass. */
+int oracle_get_products(oracle_ctx* ctx, int32_t index, double* rv, double* qv, double* prim, double* scalar);
 int oracle_num_blocks(const oracle_ctx* ctx, int32_t* n);
 int oracle_block_indexes(const oracle_ctx* ctx, int32_t* out, int32_t capacity);
 int oracle_set_time(oracle_ctx* ctx, double time, int64_t num, int64_t den);

@@ -50,6 +50,7 @@ def load():
         "oracle_block_shape_of": (C.c_int, [P, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
         "oracle_get_block": (C.c_int, [P, C.c_int32, DP, DP]),
         "oracle_get_primitives": (C.c_int, [P, C.c_int32, DP]),
+        "oracle_get_products": (C.c_int, [P, C.c_int32, DP, DP, DP, DP]),
         "oracle_num_blocks": (C.c_int, [P, C.POINTER(C.c_int32)]),
         "oracle_block_indexes": (C.c_int, [P, C.POINTER(C.c_int32), C.c_int32]),
         "oracle_set_time": (C.c_int, [P, C.c_double, C.c_int64, C.c_int64]),
@@ -160,6 +161,15 @@ class Oracle:
 
     def state(self):
         return {i: self.get_block(i) for i in self.block_indexes()}
+
+    def get_products(self, index):
+        """BlockProducts of a block: radial and polar vertices, primitive
+        [nr, nq, 4] in AnyPrimitive order, scalar [nr, nq]."""
+        nr, nq = self.shape_of(index)
+        rv, qv = np.empty(nr + 1), np.empty(nq + 1)
+        prim, scal = np.empty((nr, nq, 4)), np.empty((nr, nq))
+        self._check(self.lib.oracle_get_products(self.h, index, _d(rv), _d(qv), _d(prim), _d(scal)), "get_products")
+        return {"radial_vertices": rv, "polar_vertices": qv, "primitive": prim, "scalar": scal}
 
     def get_primitives(self, index):
         """(rho, u_r, u_theta, p, scalar concentration) of a block, [nr, nq, 5]."""

@@ -82,3 +82,32 @@ def test_restart_continues_exactly(tmp_path):
     sa, sb = a.state(), b.state()
     for i in sa:
         assert np.array_equal(sa[i][0], sb[i][0]) and np.array_equal(sa[i][1], sb[i][1])
+
+
+def test_products_file_round_trip(tmp_path, oracle_lib):
+    """Products { time, blocks, config, version } with BlockProducts arrays
+    (src/products.rs:17-36) written from the oracle's export and read back."""
+    import knc_oracle
+    w = workloads.wind_small()
+    o = knc_oracle.Oracle(w.hydro, w.mesh, threads=4)
+    o.set_model(w.model)
+    o.init_from_model(0.0)
+    o.advance(2)
+    ctl = config.Control(start_time=0.0, final_time=1e-9, checkpoint_interval=1e-10, fold=2)
+    blocks = {i: o.get_products(i) for i in o.block_indexes()}
+    t, _ = o.time()
+    doc = ck.products_document(blocks, t, w.hydro, "wind", {}, w.mesh, ctl)
+    assert list(doc) == ["time", "blocks", "config", "version"]
+    b0 = doc["blocks"][(0, 0)]
+    assert list(b0) == ["radial_vertices", "polar_vertices", "primitive", "scalar"]
+    assert b0["primitive"]["dim"] == [64, 128] and b0["radial_vertices"]["dim"] == [65]
+    path = tmp_path / "prods.0000.cbor"
+    path.write_bytes(ck.dumps(doc))
+    back = ck.read_products(path)
+    assert back["time"] == t
+    for i, b in blocks.items():
+        for k in ("radial_vertices", "polar_vertices", "primitive", "scalar"):
+            assert np.array_equal(back["blocks"][i][k], b[k])
+    # AnyPrimitive order: the wind's radial four-velocity is ~1, its density ~r^-2
+    p = back["blocks"][0]["primitive"]
+    assert abs(p[10, 10, 0] - 1.0) < 1e-3 and p[10, 10, 2] > p[10, 10, 3]

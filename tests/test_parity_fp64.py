@@ -202,3 +202,28 @@ def test_primitive_export_matches_oracle(name):
     for i in o.block_indexes():
         assert np.array_equal(g.get_primitives(i), o.get_primitives(i)), i
     assert g.launch_count() - n0 == 2 * len(o.block_indexes())   # recovery + layout change per block
+
+
+@pytest.mark.parametrize("name", ["wind_small", "sphere_small", "uneven_small"])
+def test_products_match_oracle(name, tmp_path):
+    """knc_get_products (BlockProducts::try_from_block_state,
+    src/products.rs:43-66) equals the oracle's bit for bit: vertices,
+    AnyPrimitive-ordered primitives and scalar_mass / lab_frame_mass; a
+    products file written from the device reads back the same arrays."""
+    import knc
+    from knc import checkpoint, config, workloads
+    w = getattr(workloads, name)()
+    g, o = make_pair(w)
+    g.advance(3)
+    o.advance(3)
+    for i in o.block_indexes():
+        pg, po = g.get_products(i), o.get_products(i)
+        for k in ("radial_vertices", "polar_vertices", "primitive", "scalar"):
+            assert np.array_equal(pg[k], po[k]), (i, k)
+    ctl = config.Control(start_time=0.0, final_time=1.0, checkpoint_interval=0.1, fold=3)
+    path = tmp_path / "prods.0000.cbor"
+    checkpoint.write_products(path, g, w.hydro, "wind", {}, w.mesh, ctl)
+    back = checkpoint.read_products(path)
+    assert back["time"] == g.time()[0]
+    for i in o.block_indexes():
+        assert np.array_equal(back["blocks"][i]["primitive"], o.get_products(i)["primitive"])
