@@ -278,6 +278,40 @@ def next_rows(args, make, timed, head, w):
         "value": ws.zones * steps / (ms_in * 1e-3), "unit": UNIT, "ms_per_step": ms_in / steps,
         "fold": fold, "steps": steps, "adaptive_dt_fold_of_one": f4}
     sph.close()
+    # the reference's own Newtonian flux on the same grid
+    wh = workloads.sphere_large(riemann="HLLE")
+    sph = make(False, False, True, workload=wh, tune=True)
+    ms_h, _ = timed(sph, steps, fold)
+    out["newtonian_sphere"]["hlle"] = {"value": wh.zones * steps / (ms_h * 1e-3), "ms_per_step": ms_h / steps,
+                                       "tuning": sph.tuning()}
+    sph.close()
+    # f2: a shipped setup through its device model (setups/jet_in_cloud.yaml:
+    # HLLC, 512 polar zones, blocks of 4 radial zones, both excision surfaces
+    # moving), mixed + graph against FP64, started at t = 1 as the setup is
+    import knc
+    from knc import abi
+    hydro = config.RelativisticHydro(1.333, 1.5, 0.4, "RK2", "HLLC")
+    mesh = config.Mesh(reference_radius=3e8, inner_radius=0.0, outer_radius=0.0, inner_excision_speed=3e8,
+                       outer_excision_speed=3e10, num_polar_zones=512, block_size=4)
+    model = config.JetInCloud(cloud_mass=1e32, engine_delay=1.0, engine_duration=1.0, engine_strength=1.0,
+                              engine_theta=0.1, engine_u=30.0, envelop_m1=2e27, envelop_slowest_beta=0.1,
+                              envelop_fastest_beta=0.995, envelop_psi=0.25)
+    setup = {"setup": "jet_in_cloud (setups/jet_in_cloud.yaml), device model, start time 1.0"}
+    for name, mixed in (("fp64", False), ("mixed_graph", True)):
+        sj = knc.Solver(hydro, mesh)
+        sj.set_model(model)
+        sj.init_from_model(1.0)
+        if mixed:
+            sj.set_precision(abi.KNC_PRECISION_MIXED)
+        sj.set_batched(True)
+        sj.autotune(reps=3)
+        b0 = len(sj.block_indexes())
+        ms_j, _ = timed(sj, steps, fold)
+        setup[name] = {"value": timed.zone_updates / (ms_j * 1e-3), "ms_per_step": ms_j / steps,
+                       "blocks_start": b0, "blocks_end": len(sj.block_indexes()), "tuning": sj.tuning()}
+        sj.close()
+    setup["speedup"] = setup["mixed_graph"]["value"] / setup["fp64"]["value"]
+    out["setup_jet_in_cloud"] = setup
     # f3: primitive export of every block of the wind state (device -> host)
     idx = head.block_indexes()
     head.synchronize()
