@@ -194,7 +194,10 @@ struct MixedC2p {
     }
 
     // The same with the zone's state U (D, S_r, S_theta, tau, scalar mass)
-    // already loaded.
+    // already loaded. DT: -1 reduce the time step when the stage asks for it
+    // (a.compute_dt), 0 never, 1 always (a kernel specialised either way
+    // carries no register for the other case).
+    template <int DT = -1>
     __device__ static void zone_state(const StageArgs& a, int slot, const DevBlock& B, int i, int j, bool active,
                                       const double (&U)[5], MlpWeights& W, __nv_bfloat16* act, C2pStats& st) {
         const float gmf = a.gm_f;
@@ -293,7 +296,7 @@ struct MixedC2p {
             const float wz = sqrtf(1.0f + P[1] * P[1] + P[2] * P[2]);
             const float v[NFIELD] = {P[0], P[1], P[2], P[3], scalf / dV / wz};
             store_prim<float>(B, i, j, v);
-            if (a.compute_dt && kind == HYDRO_NONE) {
+            if ((DT < 0 ? a.compute_dt != 0 : DT > 0) && kind == HYDRO_NONE) {
                 // State::time_step (src/state.rs:151-160) on this stage's
                 // primitives: signal speed in FP32, dl and dl / a in FP64
                 PhysT<float> ph;
@@ -360,6 +363,7 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+template <int DT>
 __global__ void __launch_bounds__(TILE_THREADS, 3) c2p_rows_kernel(StageArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int WPC = TILE_THREADS / 32;
@@ -396,7 +400,7 @@ __global__ void __launch_bounds__(TILE_THREADS, 3) c2p_rows_kernel(StageArgs a) 
 #pragma unroll
                 for (int q = 0; q < NFIELD; ++q) U[q] = sU[w][r % C2P_DEPTH][q][lane];
             }
-            MixedC2p<false, true>::zone_state(a, t.x, B, t.y + r, j, jin, U, W, nullptr, st);
+            MixedC2p<false, true>::zone_state<DT>(a, t.x, B, t.y + r, j, jin, U, W, nullptr, st);
         }
     }
     cp_async_wait<0>();
@@ -481,8 +485,9 @@ cudaError_t launch_c2p_mixed(const StageArgs& a, cudaStream_t s) {
         // every zone in FP32; the ones that need the FP64 recovery, densely after
         // one warp per recovery tile
         const int wt = (a.ntiles + TILE_THREADS / 32 - 1) / (TILE_THREADS / 32);
-        const int grid = std::min(wt, resident_grid(c2p_rows_kernel, TILE_THREADS, 0));
-        cudaError_t e = launch_chained(c2p_rows_kernel, grid, TILE_THREADS, 0, s, a);
+        auto k = a.compute_dt ? c2p_rows_kernel<1> : c2p_rows_kernel<0>;
+        const int grid = std::min(wt, resident_grid(k, TILE_THREADS, 0));
+        cudaError_t e = launch_chained(k, grid, TILE_THREADS, 0, s, a);
         if (e != cudaSuccess) return e;
         if (a.mlp) {
             const size_t bytes = sizeof(MlpWeights) + 8 * MLP_ACT_ELEMS * sizeof(__nv_bfloat16);
