@@ -293,7 +293,10 @@ struct MixedC2p {
                 atomicMin(&a.status->err_key, error_key(a.stage, slot, i, j, kind));
                 a.status->err_sel = a.sel_in;
             }
-            const float wz = sqrtf(1.0f + P[1] * P[1] + P[2] * P[2]);
+            // W = sqrt(1 + u^2) with explicit fused operations: the same
+            // products appear in the time-step reduction below, and a kernel
+            // with or without that reduction must round W alike
+            const float wz = sqrtf(__fmaf_rn(P[2], P[2], __fmaf_rn(P[1], P[1], 1.0f)));
             const float v[NFIELD] = {P[0], P[1], P[2], P[3], scalf / dV / wz};
             store_prim<float>(B, i, j, v);
             if ((DT < 0 ? a.compute_dt != 0 : DT > 0) && kind == HYDRO_NONE) {
