@@ -261,6 +261,7 @@ def next_rows(args, make, timed, head, w):
     # recovery (knc_advance) against the reference's order, a full recovery
     # pass for State::time_step and then the step (knc_time_step + knc_advance_dt)
     f4 = {}
+    sph.set_batched(False)   # launches issued directly: a one-step graph per call would be re-captured
     for name, sep in (("dt_in_fold", False), ("separate_pass", True)):
         sph.synchronize()
         sph.mark(0)
