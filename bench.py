@@ -247,7 +247,8 @@ def l1_density(a, b) -> float:
 
 
 def next_rows(args, make, timed, head, w):
-    """Measurements of the rows either side of the path (one GPU, rank 0)."""
+    """Measurements of the rows either side of the path (each rank on its own
+    GPU; rank 0 reports)."""
     import tempfile
     import numpy as np
     from knc import checkpoint, config, workloads
@@ -573,7 +574,8 @@ def run_knc(args):
     # (FP64, HLLC, adaptive dt found inside the fold) against the separate
     # time-step pass, primitive export and CBOR checkpoints of the wind state
     nxt = None
-    if not args.no_next and rank == 0:
+    if not args.no_next:
+        # every rank (its own replica): the timed loops hold a barrier
         nxt = next_rows(args, make, timed, head, w)
 
     cpu = None
