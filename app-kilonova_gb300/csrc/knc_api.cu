@@ -2309,6 +2309,21 @@ int knc_kernel_times(knc_ctx* c, double* ms, int64_t* launches) {
     return KNC_OK;
 }
 
+int knc_set_device(int32_t device) {
+    return cudaSetDevice(device) == cudaSuccess ? KNC_OK : KNC_ERR_CUDA;
+}
+
+int knc_device_count(int32_t* count) {
+    if (!count) return KNC_ERR_INVALID_ARGUMENT;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        n = 0;
+    }
+    *count = n;
+    return KNC_OK;
+}
+
 int knc_host_alloc(size_t bytes, void** ptr) {
     if (!ptr || bytes == 0) return KNC_ERR_INVALID_ARGUMENT;
     if (cudaHostAlloc(ptr, bytes, cudaHostAllocDefault) != cudaSuccess) return KNC_ERR_OUT_OF_MEMORY;

@@ -200,6 +200,8 @@ SIGNATURES = {
     "knc_elapsed_ms": (C.c_int, [_P, C.c_int32, C.c_int32, _DP]),
     "knc_get_primitives": (C.c_int, [_P, C.c_int32, _DP]),
     "knc_get_products": (C.c_int, [_P, C.c_int32, _DP, _DP, _DP, _DP]),
+    "knc_set_device": (C.c_int, [C.c_int32]),
+    "knc_device_count": (C.c_int, [C.POINTER(C.c_int32)]),
     "knc_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
     "knc_host_free": (C.c_int, [C.c_void_p]),
     "knc_mlp_num_params": (C.c_size_t, []),

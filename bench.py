@@ -141,6 +141,13 @@ def dist_setup(n_gpus):
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         dist.init_process_group("gloo")
         pg = dist
+        # one GPU per rank: the library's contexts use the calling thread's device
+        import ctypes as C
+        from knc import abi
+        lib = abi.load()
+        n = C.c_int32()
+        if lib.knc_device_count(C.byref(n)) == abi.KNC_OK and n.value > 0:
+            lib.knc_set_device(local % n.value)
     return rank, world, local, pg
 
 

@@ -338,6 +338,12 @@ int knc_elapsed_ms(knc_ctx* ctx, int32_t a, int32_t b, double* ms);
 
 /* Page-locked host buffers for host-resident drivers (cudaHostAlloc). */
 int knc_host_alloc(size_t bytes, void** ptr);
+/* The GPU that contexts created afterwards on the calling thread use
+ * (cudaSetDevice), and the number of GPUs: one process per GPU under a
+ * launcher that starts one rank per device. No counterpart in the
+ * reference, which runs on the host. */
+int knc_set_device(int32_t device);
+int knc_device_count(int32_t* count);
 int knc_host_free(void* ptr);
 
 /* ---- learned c2p guess: MLP 3 -> 64 -> 64 -> 1 (SiLU) ------------------ */
