@@ -139,3 +139,28 @@ def test_uneven_shape_errors():
     assert g.shape_of(2) == (nr, nq)
     cons, scalar = g.get_block(2)
     assert cons.shape == (nr, nq, 4) and scalar.shape == (nr, nq)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("learned", [False, True])
+def test_uneven_mixed_chained_graph_matches_stream(learned):
+    """The mixed stage's chained launches (row-walking recovery, dense FP64
+    pass, warp strips) captured per fold with blocks retiring and
+    activating: the graph and the direct launches give the same bits."""
+    import knc
+    from knc import learned as L, workloads
+    w = workloads.uneven_small()
+    runs = []
+    for graph in (False, True):
+        g, _ = make_pair(w)
+        g.set_precision(knc.abi.KNC_PRECISION_MIXED)
+        if learned:
+            g.set_c2p_guess(knc.abi.KNC_GUESS_MLP, L.init_weights(seed=5))
+        g.set_tuning(tile_rows=16, strip=True, ctas_per_sm=5, deferred=True)
+        g.set_batched(graph)
+        for _ in range(3):
+            g.advance(10)
+        runs.append(g)
+    assert runs[0].block_indexes() == runs[1].block_indexes()
+    assert max(zone_relative_errors(runs[0].state(), runs[1].state())) == 0.0
+    assert runs[0].time() == runs[1].time()
