@@ -142,3 +142,35 @@ def test_mixed_in_cgs_units():
     assert all(np.isfinite(c).all() and np.isfinite(s).all() for c, s in st.values())
     errs = field_errors(st, g64.state(), momentum_scale=True)
     assert max(errs) <= 1e-5, errs
+
+
+def test_wind_hllc_against_the_oracle():
+    """The mixed stage with the relativistic HLLC solver (Mignone & Bodo):
+    the same accuracy bar as HLLE against the FP64 oracle."""
+    from knc import workloads
+    w = workloads.wind_small()
+    w.hydro.riemann_solver = "HLLC"
+    g, o, l1, linf = _mixed_vs_oracle(w, w.steps)
+    for q in (0, 1, 3):
+        assert l1[q] <= 1e-6, (q, l1)
+        assert linf[q] <= 1e-5, (q, linf)
+
+
+def test_hllc_update_forms_agree():
+    """Tiles, tensor-copy tiles, warp strips (with the deferred recovery) and
+    the fused stage give the same bits with HLLC too."""
+    import knc
+    from helpers import zone_relative_errors
+    from knc import workloads
+    w = workloads.jet_small()
+    w.hydro.riemann_solver = "HLLC"
+    states = []
+    for t in (dict(tile_rows=8), dict(tile_rows=8, tma=True), dict(tile_rows=16, strip=True, deferred=True),
+              dict(tile_rows=8, fused=True)):
+        g = knc.build_solver(w)
+        g.set_precision(knc.abi.KNC_PRECISION_MIXED)
+        g.set_tuning(**t)
+        g.advance(6)
+        states.append(g.state())
+    for st in states[1:]:
+        assert max(zone_relative_errors(st, states[0])) == 0.0
