@@ -174,3 +174,21 @@ def test_hllc_update_forms_agree():
         states.append(g.state())
     for st in states[1:]:
         assert max(zone_relative_errors(st, states[0])) == 0.0
+
+
+def test_mixed_refuses_what_it_does_not_cover():
+    """The mixed stage is built for relativistic hydro on a polar grid: a
+    Newtonian context or a one-zone polar grid refuses to advance in it
+    (and the FP64 path still runs them)."""
+    import knc
+    from knc import workloads
+    one_zone = workloads.wind_small()
+    one_zone.mesh.num_polar_zones = 1
+    for w in (workloads.sphere_small(), one_zone):
+        g = knc.build_solver(w)
+        g.set_precision(knc.abi.KNC_PRECISION_MIXED)
+        with pytest.raises(knc.abi.KncError) as exc:
+            g.advance(1)
+        assert exc.value.status == knc.abi.KNC_ERR_UNSUPPORTED
+        g.set_precision(knc.abi.KNC_PRECISION_FP64)
+        g.advance(1)
