@@ -28,6 +28,7 @@ namespace knc {
 template <bool MLP>
 struct F64C2p {
     static constexpr bool mlp = MLP;
+    using RemapRec = RemapRecoveryF64;
     __device__ static void zone(const StageArgs& a, int slot, const DevBlock& B, int i, int j, bool active,
                                 MlpWeights& W, __nv_bfloat16* act, C2pStats& st) {
         const int nr = B.nr, nq = B.nq;

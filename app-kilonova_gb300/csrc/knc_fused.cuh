@@ -138,7 +138,7 @@ __device__ __forceinline__ void stage_fused_body(const StageArgs& a, const Ghost
             const int total = f.nremap * per;
             for (int k = blockIdx.x * NT + threadIdx.x; k < total; k += gridDim.x * NT) {
                 const int item = k / per;
-                remap_zone<R>(a, f.remap[item], k - item * per);
+                remap_zone<R, typename C2P::RemapRec>(a, f.remap[item], k - item * per);
             }
         }
         grid_barrier(a.status, f.bar_base + 2ull * gridDim.x);

@@ -110,10 +110,35 @@ static __device__ __noinline__ void ghost_zone(const GhostArgs& a, int end, int 
 // Halo zone k of remap item it = {target slot, source slot, side}: target
 // column j of halo row `row` from row `row` of the source's edge rows:
 //  - a finer source (R = nq_s / nq_t): conserved volume integrals and volumes
-//    of its R zones summed in column order, then the FP64 recovery (the
-//    reference's Newton from the plain guess) — a conservative merge;
+//    of its R zones summed in column order, then the stage's recovery REC
+//    — a conservative merge;
 //  - a coarser source: its primitive at column j / R, copied.
-template <class R>
+// The recovery of a merged zone (volume integrals U, volume dv) into the
+// primitive row v: the reference's Newton from the plain guess (the FP64
+// stage, equal to the oracle). The mixed stage passes its own policy.
+struct RemapRecoveryF64 {
+    template <class R>
+    __device__ static int recover(const StageArgs& a, const double (&U)[5], double dv, R (&v)[NFIELD]) {
+        double u[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) u[q] = U[q] / dv;
+        double P[4] = {0.0, 0.0, 0.0, 0.0};
+        double bad = 0.0;
+        int iters = 0, kind;
+        if (a.srhd) kind = srhd_c2p_newton(a.gm, u, 0.0, P, iters, bad);
+        else kind = newt_c2p(a.gm - 1.0, u, P, bad);
+        const double w = a.srhd ? sqrt(1.0 + P[1] * P[1] + P[2] * P[2]) : 1.0;
+        const double sv = U[4] / dv / w;
+        v[0] = (R)P[0];
+        v[1] = (R)P[1];
+        v[2] = (R)P[2];
+        v[3] = (R)P[3];
+        v[4] = (R)sv;
+        return kind;
+    }
+};
+
+template <class R, class REC = RemapRecoveryF64>
 static __device__ __noinline__ void remap_zone(const StageArgs& a, const int4 it, int k) {
     const DevBlock& T = a.blocks[it.x];
     const DevBlock& S = a.blocks[it.y];
@@ -141,23 +166,9 @@ static __device__ __noinline__ void remap_zone(const StageArgs& a, const int4 it
             for (int q = 0; q < 5; ++q) U[q] += Us[q * n + z];
             dv += S.dv[z];
         }
-        double u[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) u[q] = U[q] / dv;
-        double P[4] = {0.0, 0.0, 0.0, 0.0};
-        double bad = 0.0;
-        int iters = 0, kind;
-        if (a.srhd) kind = srhd_c2p_newton(a.gm, u, 0.0, P, iters, bad);
-        else kind = newt_c2p(a.gm - 1.0, u, P, bad);
+        const int kind = REC::recover(a, U, dv, v);
         if (kind != HYDRO_NONE && kind != HYDRO_NEGATIVE_PRESSURE)
             atomicMin(&a.status->err_key, error_key(a.stage, it.y, srow, j * Rr, kind));
-        const double w = a.srhd ? sqrt(1.0 + P[1] * P[1] + P[2] * P[2]) : 1.0;
-        const double sv = U[4] / dv / w;
-        v[0] = (R)P[0];
-        v[1] = (R)P[1];
-        v[2] = (R)P[2];
-        v[3] = (R)P[3];
-        v[4] = (R)sv;
     }
     R* Pt = reinterpret_cast<R*>(T.P);
     const int64_t pt = (int64_t)(T.nr + 4) * nq_t;
@@ -172,11 +183,11 @@ namespace {
 
 __global__ void ghost_kernel(GhostArgs a) { ghost_zone(a, blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x); }
 
-template <class R>
+template <class R, class REC = RemapRecoveryF64>
 __global__ void remap_kernel(StageArgs a, const int4* __restrict__ items) {
     const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
     if (ek != NO_ERROR && (uint32_t)(ek >> 48) < (uint32_t)a.stage) return;
-    remap_zone<R>(a, items[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x);
+    remap_zone<R, REC>(a, items[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 }  // namespace

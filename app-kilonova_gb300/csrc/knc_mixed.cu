@@ -170,6 +170,53 @@ static __device__ __noinline__ Fp64Recovery recover_fp64_call(const StageArgs& a
     return r;
 }
 
+// A merged zone of a halo remap (volume integrals U over the finer
+// neighbour's zones, their summed volume dv) recovered as the mixed stage
+// recovers any zone: the FP32 iteration per unit mass, the FP64 recovery from
+// its root above the Lorentz-factor split or where it did not converge.
+struct MixedRemapRecovery {
+    template <class R>
+    __device__ static int recover(const StageArgs& a, const double (&U)[5], double dv, R (&v)[NFIELD]) {
+        const double m = U[0], tau = U[3];
+        if (is_negative(m)) return HYDRO_NEGATIVE_DENSITY;
+        if (is_negative(tau)) return HYDRO_NEGATIVE_ENERGY_DENSITY;
+        const int de = -a.lscale3;
+        const float mf = d2f_rn_exp(m, de), tauf = d2f_rn_exp(tau, de);
+        const float s1f = d2f_rn_exp(U[1], de), s2f = d2f_rn_exp(U[2], de);
+        const float scalf = d2f_rn_exp(U[4], de);
+        const float dV = d2f_rn_exp(dv, de);
+        const float im = 1.0f / mf;
+        const float s1n = s1f * im, s2n = s2f * im, taun = tauf * im;
+        const float ssn = s1n * s1n + s2n * s2n;
+        const float x1 = __fdividef(sqrtf(ssn), 1.0f + taun);
+        const bool high = x1 * x1 > a.high_thr_f;
+        float p32 = 0.f, w32 = 1.f;
+        int it32 = 0;
+        const bool ok32 = newton_fast<float>(1.0f, ssn, taun, a.gm_f, 0.0f, 2e-7f * taun, 1e-6f, 16, p32, w32, it32);
+        float P[4];
+        int kind = HYDRO_NONE;
+        if (!high && ok32) {
+            const float inv_dv = 1.0f / dV;
+            const float inv_et = 1.0f / (taun + 1.0f + p32);
+            P[0] = mf / w32 * inv_dv;
+            P[1] = w32 * s1n * inv_et;
+            P[2] = w32 * s2n * inv_et;
+            P[3] = p32 * mf * inv_dv;
+            if (p32 < 0.f) P[3] = (float)PRESSURE_FLOOR * P[0];
+        } else {
+            const Fp64Recovery r = recover_fp64(a, m, U[1], U[2], tau, dV, ok32, p32);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) P[q] = r.P[q];
+            kind = r.kind;
+        }
+        const float wz = sqrtf(__fmaf_rn(P[2], P[2], __fmaf_rn(P[1], P[1], 1.0f)));
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = (R)P[q];
+        v[4] = (R)(scalf / dV / wz);
+        return kind;
+    }
+};
+
 // Recovery of one zone; every thread of a warp calls zone() together (the
 // learned guess is a warp-wide inference).
 //
@@ -181,6 +228,7 @@ static __device__ __noinline__ Fp64Recovery recover_fp64_call(const StageArgs& a
 template <bool MLP, bool DEFER = false>
 struct MixedC2p {
     static constexpr bool mlp = MLP;
+    using RemapRec = MixedRemapRecovery;
     __device__ static void zone(const StageArgs& a, int slot, const DevBlock& B, int i, int j, bool active,
                                 MlpWeights& W, __nv_bfloat16* act, C2pStats& st) {
         double U[5] = {1.0, 0.0, 0.0, 1.0, 0.0};
@@ -643,7 +691,7 @@ cudaError_t launch_ghost_mixed(const GhostArgs& a, cudaStream_t s) {
 cudaError_t launch_remap_mixed(const StageArgs& a, const int4* remap, int nremap, int max_nq, cudaStream_t s) {
     if (nremap <= 0) return cudaSuccess;
     dim3 grid((2 * max_nq + 127) / 128, nremap);
-    remap_kernel<float><<<grid, 128, 0, s>>>(a, remap);
+    remap_kernel<float, MixedRemapRecovery><<<grid, 128, 0, s>>>(a, remap);
     return cudaGetLastError();
 }
 
