@@ -268,6 +268,25 @@ struct Layout {
     // warps per SM on a chunk
     int4* d_sstrips = nullptr;
     int sstrips_cap = 0;
+    std::vector<DevBlock> tab_h;   // host copies of d_table, d_tiles and d_sstrips
+    std::vector<int4> tiles_h, sstrips_h;
+    // the host-state advance's independent chunks, built for sc_S stages on
+    // first use (build_chunks): a table with shadow blocks appended, per chunk
+    // its recovery tiles (own blocks' first) and per chunk and stage its strips
+    int sc_S = 0;
+    std::vector<int> sc_cb;              // [G + 1] chunk bounds (slots)
+    std::vector<int> sc_tile_off;        // [G + 1]
+    std::vector<int> sc_own_tiles;       // [G]
+    std::vector<int> sc_strip_off;       // [G S + 1]: chunk k, stage s at k S + s
+    std::vector<int64_t> sc_up;          // [G + 1]: zones each chunk's upload covers
+    DevBlock* d_sc_table = nullptr;
+    int sc_table_cap = 0;
+    int4* d_sc_tiles = nullptr;
+    int sc_tiles_cap = 0;
+    int4* d_sc_strips = nullptr;
+    int sc_strips_cap = 0;
+    double* d_sc_store = nullptr;
+    size_t sc_store_cap = 0;
     // edge blocks, whose outer halo rows the ghost launch writes
     void* P_edge[2] = {nullptr, nullptr};
     int32_t nr_edge[2] = {0, 0}, nq_edge[2] = {0, 0};
@@ -297,6 +316,10 @@ void free_layout(Layout& l) {
     cudaFree(l.d_ghost_dv[0]);
     cudaFree(l.d_ghost_dv[1]);
     cudaFree(l.d_init_tiles);
+    cudaFree(l.d_sc_table);
+    cudaFree(l.d_sc_tiles);
+    cudaFree(l.d_sc_strips);
+    cudaFree(l.d_sc_store);
     l = Layout();
 }
 
@@ -723,6 +746,10 @@ int rebuild_table(knc_ctx* c) {
         L(c).tiles_cap = (int)tiles.size();
     }
     if (nb) CK(cudaMemcpyAsync(L(c).d_table, tab.data(), nb * sizeof(DevBlock), cudaMemcpyHostToDevice, c->stream));
+    L(c).tab_h = tab;
+    L(c).tiles_h = tiles;
+    L(c).sstrips_h = sstrips;
+    L(c).sc_S = 0;
     if (!tiles.empty())
         CK(cudaMemcpyAsync(L(c).d_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
     if ((int)utiles.size() > L(c).utiles_cap) {
@@ -2052,13 +2079,12 @@ namespace {
 
 // Chunks of consecutive slots for the host-state advance, about equal in
 // zones, at most HOST_CHUNKS and at least one slot each: bounds[k] ..
-// bounds[k + 1] - 1 are chunk k's slots. A chunk's download waits for the
-// upload of the 2S - 1 chunks after it (S stages, halo rows one chunk deep
-// per recovery and update). Measured on the 4096 x 1024 wind (64 blocks):
-// 16 chunks 1.55 ms per step, 8 chunks 1.60, 32 chunks 1.69; single blocks
-// at both ends with 8 larger chunks between 1.62 (the downloads then wait on
-// the larger chunks' uploads).
+// bounds[k + 1] - 1 are chunk k's slots.
 constexpr int HOST_CHUNKS = 16;
+// streams the chunks' launches are spread over (chunk k on k % HOST_STREAMS)
+constexpr int HOST_STREAMS = 4;
+// chunks whose uploads are issued before the next chunk's launches
+constexpr int HOST_UPLOADS_AHEAD = 2;
 
 std::vector<int> chunk_bounds(const Layout& l) {
     const int nb = (int)l.slot_index.size();
@@ -2075,6 +2101,180 @@ std::vector<int> chunk_bounds(const Layout& l) {
     return b;
 }
 
+// Whether every chunk boundary whose blocks exchange halo rows has the 2S
+// rows on both sides that its shadow blocks copy (S stages per step).
+bool chunks_fit(const Layout& l, int S) {
+    const std::vector<int> cb = chunk_bounds(l);
+    for (size_t k = 1; k + 1 < cb.size(); ++k) {
+        const DevBlock& lo = l.tab_h[cb[k] - 1];
+        const DevBlock& hi = l.tab_h[cb[k]];
+        if (lo.P_out_nbr && (lo.nr < 2 * S || hi.nr < 2 * S)) return false;
+    }
+    return true;
+}
+
+// Independent chunks for the host-state advance (S stages per step). Each
+// chunk boundary whose blocks exchange halo rows gets two shadow blocks of 2S
+// rows: the first 2S rows of the block above it, for the chunk below, and
+// the last 2S rows of the block below it, for the chunk above. In the chunk's
+// own table the boundary block's halo rows come from its shadow and the
+// shadow's from the boundary block. Each stage recovers all of a shadow's
+// rows and updates those whose stencil lies inside the chunk and its shadow:
+// rows [0, 2S - 2s - 2) of an upper shadow at stage s, rows [2s + 2, 2S) of a
+// lower one. So the halo rows a chunk's blocks read are computed inside the
+// chunk, from the same states with the same arithmetic as in the block they
+// copy, and no chunk waits for another's launches. A shadow's rows that its
+// stages do not update keep the step's initial state in both buffers
+// (state_in_kernel), which recovers as at the first stage; they feed no
+// update. A shadow's halo rows away from its chunk are never read.
+int build_chunks(knc_ctx* c, int S) {
+    Layout& l = L(c);
+    if (l.sc_S == S) return KNC_OK;
+    l.sc_S = 0;
+    const int nb = (int)l.slot_index.size();
+    l.sc_cb = chunk_bounds(l);
+    const std::vector<int>& cb = l.sc_cb;
+    const int G = (int)cb.size() - 1;
+    std::vector<DevBlock> tab = l.tab_h;
+    struct Shadow { int chunk, src, row0; bool upper; };
+    std::vector<Shadow> sh;
+    l.sc_up.assign(1, 0);
+    for (int k = 1; k < G; ++k) {
+        const int lo = cb[k] - 1, hi = cb[k];
+        int64_t up = l.zone_off[hi];
+        if (tab[lo].P_out_nbr) {
+            sh.push_back({k - 1, hi, 0, true});
+            sh.push_back({k, lo, tab[lo].nr - 2 * S, false});
+            up += (int64_t)2 * S * tab[hi].nq;
+        }
+        l.sc_up.push_back(up);
+    }
+    l.sc_up.push_back(l.zone_off[nb]);
+    size_t store = 0;
+    for (const Shadow& x : sh) store += (size_t)(30 * S + 20) * tab[x.src].nq;
+    if (store > l.sc_store_cap) {
+        cudaFree(l.d_sc_store);
+        l.d_sc_store = nullptr;
+        CK(dalloc(&l.d_sc_store, store));
+        l.sc_store_cap = store;
+    }
+    double* mem = l.d_sc_store;
+    std::vector<std::vector<int>> of_chunk(G);
+    for (size_t n = 0; n < sh.size(); ++n) {
+        const Shadow& x = sh[n];
+        const DevBlock src = l.tab_h[x.src];
+        DevBlock d = src;
+        const int64_t nq = src.nq, rows = 2 * S, o = x.row0;
+        d.nr = (int32_t)rows;
+        d.buf[0] = mem;
+        d.buf[1] = mem + 5 * rows * nq;
+        d.P = mem + 10 * rows * nq;
+        mem += (5 * rows + 5 * (rows + 4) + 5 * rows) * nq;
+        d.ar = src.ar + o * nq;
+        d.aq = src.aq + o * (nq + 1);
+        d.dv = src.dv + o * nq;
+        d.rc = src.rc + o;
+        d.rv = src.rv + o;
+        d.ar_r = src.ar_r + o;
+        d.aq_r = src.aq_r + o;
+        d.dv_r = src.dv_r + o;
+        d.dv_r32 = src.dv_r32 + o;
+        d.rc32 = src.rc32 + o;
+        d.shadow = 1;
+        const int slot = nb + (int)n;
+        if (x.upper) {   // above chunk x.chunk, whose last block is x.src - 1
+            const int lo = x.src - 1;
+            d.P_in_nbr = tab[lo].P;
+            d.nr_in_nbr = tab[lo].nr;
+            d.slot_in = lo;
+            d.P_out_nbr = nullptr;
+            d.nr_out_nbr = 0;
+            d.slot_out = -1;
+            tab[lo].P_out_nbr = d.P;
+            tab[lo].nr_out_nbr = (int32_t)rows;
+            tab[lo].slot_out = slot;
+        } else {         // below chunk x.chunk, whose first block is x.src + 1
+            const int hi = x.src + 1;
+            d.P_out_nbr = tab[hi].P;
+            d.nr_out_nbr = tab[hi].nr;
+            d.slot_out = hi;
+            d.P_in_nbr = nullptr;
+            d.nr_in_nbr = 0;
+            d.slot_in = -1;
+            tab[hi].P_in_nbr = d.P;
+            tab[hi].nr_in_nbr = (int32_t)rows;
+            tab[hi].slot_in = slot;
+        }
+        tab.push_back(d);
+        of_chunk[x.chunk].push_back((int)n);
+    }
+    // recovery tiles: per chunk its own blocks' (t.w = first zone of the
+    // block in the whole-state arrays), then its shadows' (t.w = the zone of
+    // the shadow's row 0 there)
+    std::vector<int4> tiles;
+    l.sc_tile_off.clear();
+    l.sc_own_tiles.clear();
+    const std::vector<int4>& own_tiles = l.tiles_h;
+    for (int k = 0; k < G; ++k) {
+        l.sc_tile_off.push_back((int)tiles.size());
+        tiles.insert(tiles.end(), own_tiles.begin() + l.tile_off[cb[k]], own_tiles.begin() + l.tile_off[cb[k + 1]]);
+        l.sc_own_tiles.push_back(l.tile_off[cb[k + 1]] - l.tile_off[cb[k]]);
+        for (int n : of_chunk[k]) {
+            const Shadow& x = sh[n];
+            const int64_t w = l.zone_off[x.src] + (int64_t)x.row0 * tab[x.src].nq;
+            for (int j0 = 0; j0 < tab[x.src].nq; j0 += TILE_Q) tiles.push_back(make_int4(nb + n, 0, j0, (int)w));
+        }
+    }
+    l.sc_tile_off.push_back((int)tiles.size());
+    // update strips: per chunk and stage its own blocks' short strips, then
+    // its shadows' rows that stage updates
+    std::vector<int4> strips;
+    l.sc_strip_off.clear();
+    for (int k = 0; k < G; ++k)
+        for (int s = 0; s < S; ++s) {
+            l.sc_strip_off.push_back((int)strips.size());
+            strips.insert(strips.end(), l.sstrips_h.begin() + l.sstrip_off[cb[k]],
+                          l.sstrips_h.begin() + l.sstrip_off[cb[k + 1]]);
+            const int rows = 2 * S - 2 * s - 2;
+            if (rows <= 0) continue;
+            for (int n : of_chunk[k]) {
+                const Shadow& x = sh[n];
+                const int i0 = x.upper ? 0 : 2 * s + 2;
+                for (int j0 = 0; j0 < tab[x.src].nq; j0 += STRIP_OUT)
+                    strips.push_back(make_int4(nb + n, i0, j0, rows));
+            }
+        }
+    l.sc_strip_off.push_back((int)strips.size());
+    if ((int)tab.size() > l.sc_table_cap) {
+        cudaFree(l.d_sc_table);
+        l.d_sc_table = nullptr;
+        CK(dalloc(&l.d_sc_table, tab.size()));
+        l.sc_table_cap = (int)tab.size();
+    }
+    if ((int)tiles.size() > l.sc_tiles_cap) {
+        cudaFree(l.d_sc_tiles);
+        l.d_sc_tiles = nullptr;
+        CK(dalloc(&l.d_sc_tiles, tiles.size()));
+        l.sc_tiles_cap = (int)tiles.size();
+    }
+    if ((int)strips.size() > l.sc_strips_cap) {
+        cudaFree(l.d_sc_strips);
+        l.d_sc_strips = nullptr;
+        CK(dalloc(&l.d_sc_strips, strips.size()));
+        l.sc_strips_cap = (int)strips.size();
+    }
+    // (the chunk streams start after the library's stream)
+    CK(cudaMemcpyAsync(l.d_sc_table, tab.data(), tab.size() * sizeof(DevBlock), cudaMemcpyHostToDevice, c->stream));
+    if (!tiles.empty())
+        CK(cudaMemcpyAsync(l.d_sc_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                           c->stream));
+    if (!strips.empty())
+        CK(cudaMemcpyAsync(l.d_sc_strips, strips.data(), strips.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                           c->stream));
+    l.sc_S = S;
+    return KNC_OK;
+}
+
 int ensure_chunk_events(knc_ctx* c, size_t n) {
     while (c->ev_chunk.size() < n) {
         cudaEvent_t e;
@@ -2087,139 +2287,153 @@ int ensure_chunk_events(knc_ctx* c, size_t n) {
 // One RK step with the state streamed between page-locked host memory and
 // the device by chunks of blocks: hc_in / hs_in are uploaded before the
 // step's first stage reads them, hc_out / hs_out downloaded after its last
-// stage (either pair may be null). Uploads (one copy direction), downloads
-// (the other) and the stages of the chunks in between run at the same time.
+// stage (either pair may be null; without an upload the step starts from the
+// device state). Uploads (one copy direction), downloads (the other) and the
+// chunks' launches run at the same time.
 //
-// Stage s recovers chunk g (R_s(g)) and updates it (X_s(g)). X_s(g) reads the
-// halo rows that R_s(g - 1) and R_s(g + 1) push into g's primitives, and
-// R_{s+1}(g) overwrites the halo rows that X_s(g - 1) and X_s(g + 1) read and
-// the state X_s(g) wrote. Each of the 2S kinds R_0, X_0, R_1, X_1, ... runs in
-// chunk order on a stream of its own, so these orders reduce to
-//   X_s(g)     after R_s(min(g + 1, G - 1)),
-//   R_{s+1}(g) after X_s(min(g + 1, G - 1)),
-// one event wait each; chunks of different kinds then overlap on the GPU
-// (a chunk's launch alone does not fill it). Launches are issued in waves
-// (R_s(g) in wave g + 2s, X_s(g) in wave g + 2s + 1, kinds in that order
-// within a wave), so every event is recorded before it is waited on. The
-// ghost rows of stage s at the inner (outer) mesh end go on X_s's stream just
-// before X_s of the first (last) chunk, which runs after X_{s-1} of that
-// chunk read the previous stage's. Recoveries run in the inline form (the
-// deferred list is per stage, not per chunk) and updates as short warp
-// strips. Every zone meets the arithmetic of rk_step, so states are bitwise
-// those of knc_set_state + knc_advance + knc_get_state.
+// Chunk k's launches go in order on a stream of their own: after the upload
+// of its zones (and of the first 2S rows of the next chunk, which its upper
+// shadow copies), state_in, then per stage the recovery of its blocks and
+// shadows, the ghost rows at a mesh end, the update; then state_out into a
+// separate staging area, which its download reads. No launch waits for
+// another chunk (build_chunks), so chunk k's download starts once its own
+// upload and six launches are done, and the last download follows the last
+// upload by the same. Recoveries run in the inline form (the deferred list
+// is per stage) and updates as short warp strips. Every zone of a block
+// meets the arithmetic of rk_step, so states are bitwise those of
+// knc_set_state + knc_advance + knc_get_state.
 int stream_step(knc_ctx* c, double dt, const double* hc_in, const double* hs_in, double* hc_out,
                 double* hs_out) {
     int r;
-    const Layout& lay = L(c);
     StagePlan p[3];
     const int S = step_plan(c, dt, p);
-    const std::vector<int> cb = chunk_bounds(lay);
+    if ((r = build_chunks(c, S))) return r;
+    const Layout& lay = L(c);
+    const std::vector<int>& cb = lay.sc_cb;
     const int G = (int)cb.size() - 1;
     const int64_t total = lay.zone_off.back();
-    const int K = 2 * S;
     GhostArgs g[3];
     StageArgs a[3];
     for (int s = 0; s < S; ++s)
         if ((r = prepare_stage(c, p[s].sel_in, p[s].sel_out, p[s].sel_base, p[s].w1, p[s].bf, p[s].t, dt, p[s].sub,
                                g[s], a[s])))
             return r;
-    if ((r = ensure_stage(c, 5 * (size_t)total))) return r;
-    // events: uploads [0, G), kinds [G, G + K G), downloads ready [G + K G, 2 G + K G), start
-    const size_t ev_start = (size_t)(2 + K) * G;
-    if ((r = ensure_chunk_events(c, ev_start + 1))) return r;
-    while ((int)c->kstreams.size() < K) {
+    // staging: the step's input state (cons [total][4], then scalar [total]),
+    // then its output state in the same layout, then per stage and mesh end
+    // the ghost rows [5][2][nq]
+    const int64_t gq = std::max(lay.nq_edge[0], lay.nq_edge[1]);
+    if ((r = ensure_stage(c, 10 * (size_t)total + (size_t)S * 2 * 10 * gq))) return r;
+    const int NS = std::min(G, HOST_STREAMS);
+    // events: uploads [0, G), downloads ready [G, 2 G), start, stream ends
+    // [2 G + 1, 2 G + 2 + NS) (the last: ghost rows), ghost rows of stage s
+    const size_t ev_start = (size_t)2 * G;
+    const size_t ev_ghost = ev_start + 2 + NS;
+    if ((r = ensure_chunk_events(c, ev_ghost + S))) return r;
+    while ((int)c->kstreams.size() < NS + 1) {
         cudaStream_t st;
         CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         c->kstreams.push_back(st);
     }
-    auto evH = [&](int k) { return c->ev_chunk[k]; };
-    auto evK = [&](int kind, int k) { return c->ev_chunk[G + (size_t)kind * G + k]; };
-    auto evO = [&](int k) { return c->ev_chunk[(size_t)(1 + K) * G + k]; };
-    double* sc = c->d_stage;               // whole-state layout: cons [total][4], then scalar [total]
+    double* sc = c->d_stage;
     double* ss = c->d_stage + 4 * total;
-    auto zlo = [&](int k) { return lay.zone_off[cb[k]]; };
-    auto nz = [&](int k) { return lay.zone_off[cb[k + 1]] - lay.zone_off[cb[k]]; };
-    auto tiles_of = [&](int k) { return lay.d_tiles + lay.tile_off[cb[k]]; };
-    auto ntiles_of = [&](int k) { return lay.tile_off[cb[k + 1]] - lay.tile_off[cb[k]]; };
-    auto chunk_args = [&](const StageArgs& x, int k) {
-        StageArgs y = x;
-        const int s0 = cb[k], s1 = cb[k + 1];
-        y.tiles = lay.d_tiles + lay.tile_off[s0];
-        y.ntiles = lay.tile_off[s1] - lay.tile_off[s0];
-        // the update as warp strips of STREAM_STRIP_ROWS rows, whatever the
-        // tuned form (every form gives the same state)
-        y.strips = lay.d_sstrips + lay.sstrip_off[s0];
-        y.nstrips = lay.sstrip_off[s1] - lay.sstrip_off[s0];
-        y.tma = 0;
-        y.high = nullptr;
-        y.high_count = nullptr;
-        y.high_count_next = nullptr;
-        y.high_cap = 0;
-        return y;
-    };
+    double* oc = c->d_stage + 5 * total;
+    double* os = c->d_stage + 9 * total;
+    if (!hc_in) {   // the device state into the input staging
+        CK(launch_state_out(lay.d_table, lay.d_tiles, lay.ntiles, p[0].sel_in, sc, ss, c->stream));
+        ++c->launches;
+    }
     // every stream starts after the work already on the library's stream
     CK(cudaEventRecord(c->ev_chunk[ev_start], c->stream));
-    for (int k = 0; k < K; ++k) CK(cudaStreamWaitEvent(c->kstreams[k], c->ev_chunk[ev_start], 0));
-    if (hc_in) {
-        CK(cudaStreamWaitEvent(c->h2d, c->ev_chunk[ev_start], 0));
-        for (int k = 0; k < G; ++k) {
-            CK(cudaMemcpyAsync(sc + 4 * zlo(k), hc_in + 4 * zlo(k), 4 * nz(k) * sizeof(double),
-                               cudaMemcpyHostToDevice, c->h2d));
-            CK(cudaMemcpyAsync(ss + zlo(k), hs_in + zlo(k), nz(k) * sizeof(double), cudaMemcpyHostToDevice, c->h2d));
-            CK(cudaEventRecord(evH(k), c->h2d));
-        }
-    }
-    auto recover = [&](int s, int k) -> int {
-        cudaStream_t st = c->kstreams[2 * s];
-        if (s == 0 && hc_in) {
-            CK(cudaStreamWaitEvent(st, evH(k), 0));
-            CK(launch_state_in(lay.d_table, tiles_of(k), ntiles_of(k), p[0].sel_in, sc, ss, st));
-            ++c->launches;
-        }
-        if (s > 0) CK(cudaStreamWaitEvent(st, evK(2 * s - 1, std::min(k + 1, G - 1)), 0));
-        const StageArgs y = chunk_args(a[s], k);
-        CK(mixed(c) ? launch_c2p_mixed(y, st) : launch_c2p_f64(y, st));
-        ++c->launches;
-        CK(cudaEventRecord(evK(2 * s, k), st));
-        return KNC_OK;
-    };
-    auto update = [&](int s, int k) -> int {
-        cudaStream_t st = c->kstreams[2 * s + 1];
-        CK(cudaStreamWaitEvent(st, evK(2 * s, std::min(k + 1, G - 1)), 0));
+    for (int k = 0; k < NS; ++k) CK(cudaStreamWaitEvent(c->kstreams[k], c->ev_chunk[ev_start], 0));
+    if (hc_in) CK(cudaStreamWaitEvent(c->h2d, c->ev_chunk[ev_start], 0));
+    if (hc_out) CK(cudaStreamWaitEvent(c->d2h, c->ev_chunk[ev_start], 0));
+    // The ghost rows of every stage depend only on the model and the stage
+    // time: computed at once on a stream of their own into the staging area,
+    // then copied into the edge block's halo rows just before the update of
+    // the chunk at that mesh end, after its previous stage's update read them.
+    cudaStream_t gst = c->kstreams[NS];
+    CK(cudaStreamWaitEvent(gst, c->ev_chunk[ev_start], 0));
+    double* gscr = c->d_stage + 10 * total;
+    auto gscratch = [&](int s, int end) { return gscr + (size_t)(2 * s + end) * 10 * gq; };
+    for (int s = 0; s < S; ++s) {
+        GhostArgs ge = g[s];
         for (int end = 0; end < 2; ++end) {
-            if (k != (end ? G - 1 : 0)) continue;
-            GhostArgs ge = g[s];
-            ge.P[1 - end] = nullptr;   // this end only
-            CK(mixed(c) ? launch_ghost_mixed(ge, st) : launch_ghost_f64(ge, st));
-            ++c->launches;
+            if (ge.P[end]) ge.P[end] = gscratch(s, end);
+            ge.row0[end] = 0;
+            ge.nr_t[end] = -2;   // row stride nr_t + 4 = 2: the compact [5][2][nq]
         }
-        const StageArgs y = chunk_args(a[s], k);
-        CK(mixed(c) ? launch_update_mixed(y, st) : launch_update_f64(y, st));
+        CK(mixed(c) ? launch_ghost_mixed(ge, gst) : launch_ghost_f64(ge, gst));
         ++c->launches;
-        CK(cudaEventRecord(evK(2 * s + 1, k), st));
-        if (s == S - 1 && hc_out) {
-            CK(launch_state_out(lay.d_table, tiles_of(k), ntiles_of(k), p[S - 1].sel_out, sc, ss, st));
-            ++c->launches;
-            CK(cudaEventRecord(evO(k), st));
-            CK(cudaStreamWaitEvent(c->d2h, evO(k), 0));
-            CK(cudaMemcpyAsync(hc_out + 4 * zlo(k), sc + 4 * zlo(k), 4 * nz(k) * sizeof(double),
-                               cudaMemcpyDeviceToHost, c->d2h));
-            CK(cudaMemcpyAsync(hs_out + zlo(k), ss + zlo(k), nz(k) * sizeof(double), cudaMemcpyDeviceToHost,
-                               c->d2h));
+        CK(cudaEventRecord(c->ev_chunk[ev_ghost + s], gst));
+    }
+    CK(cudaEventRecord(c->ev_chunk[ev_start + 1 + NS], gst));
+    auto upload = [&](int k) -> int {
+        const int64_t z0 = lay.sc_up[k], nz = lay.sc_up[k + 1] - z0;
+        if (nz > 0) {
+            CK(cudaMemcpyAsync(sc + 4 * z0, hc_in + 4 * z0, 4 * nz * sizeof(double), cudaMemcpyHostToDevice,
+                               c->h2d));
+            CK(cudaMemcpyAsync(ss + z0, hs_in + z0, nz * sizeof(double), cudaMemcpyHostToDevice, c->h2d));
         }
+        CK(cudaEventRecord(c->ev_chunk[k], c->h2d));
         return KNC_OK;
     };
-    for (int w = 0; w < G + 2 * S - 1; ++w) {
-        if (w < G && (r = recover(0, w))) return r;
+    // Issue order: uploads HOST_UPLOADS_AHEAD chunks ahead of the chunk whose
+    // launches are issued next, so that chunk 0's launches are queued while
+    // its upload runs and the copy engine still always has the next upload.
+    for (int k = 0; hc_in && k < std::min(G, HOST_UPLOADS_AHEAD); ++k)
+        if ((r = upload(k))) return r;
+    for (int k = 0; k < G; ++k) {
+        if (hc_in && k + HOST_UPLOADS_AHEAD < G && (r = upload(k + HOST_UPLOADS_AHEAD))) return r;
+        cudaStream_t st = c->kstreams[k % NS];
+        if (hc_in) CK(cudaStreamWaitEvent(st, c->ev_chunk[k], 0));
+        const int4* tiles = lay.d_sc_tiles + lay.sc_tile_off[k];
+        const int ntiles = lay.sc_tile_off[k + 1] - lay.sc_tile_off[k];
+        CK(launch_state_in(lay.d_sc_table, tiles, ntiles, p[0].sel_in, sc, ss, st));
+        ++c->launches;
         for (int s = 0; s < S; ++s) {
-            const int gx = w - 2 * s - 1;
-            if (gx >= 0 && gx < G && (r = update(s, gx))) return r;
-            const int gr = w - 2 * s - 2;
-            if (s + 1 < S && gr >= 0 && gr < G && (r = recover(s + 1, gr))) return r;
+            StageArgs y = a[s];
+            y.blocks = lay.d_sc_table;
+            y.tiles = tiles;
+            y.ntiles = ntiles;
+            // the update as warp strips of STREAM_STRIP_ROWS rows, whatever
+            // the tuned form (every form gives the same state)
+            y.strips = lay.d_sc_strips + lay.sc_strip_off[k * S + s];
+            y.nstrips = lay.sc_strip_off[k * S + s + 1] - lay.sc_strip_off[k * S + s];
+            y.tma = 0;
+            y.high = nullptr;
+            y.high_count = nullptr;
+            y.high_count_next = nullptr;
+            y.high_cap = 0;
+            CK(mixed(c) ? launch_c2p_mixed(y, st) : launch_c2p_f64(y, st));
+            ++c->launches;
+            for (int end = 0; end < 2; ++end) {
+                if (k != (end ? G - 1 : 0) || !g[s].P[end]) continue;
+                CK(cudaStreamWaitEvent(st, c->ev_chunk[ev_ghost + s], 0));
+                CK(launch_halo_rows(gscratch(s, end), g[s].P[end], g[s].nq[end], g[s].nr_t[end], g[s].row0[end],
+                                    mixed(c) ? 4 : 8, st));
+                ++c->launches;
+            }
+            CK(mixed(c) ? launch_update_mixed(y, st) : launch_update_f64(y, st));
+            ++c->launches;
+        }
+        if (hc_out) {
+            const int64_t z0 = lay.zone_off[cb[k]], nz = lay.zone_off[cb[k + 1]] - z0;
+            CK(launch_state_out(lay.d_sc_table, tiles, lay.sc_own_tiles[k], p[S - 1].sel_out, oc, os, st));
+            ++c->launches;
+            CK(cudaEventRecord(c->ev_chunk[G + k], st));
+            CK(cudaStreamWaitEvent(c->d2h, c->ev_chunk[G + k], 0));
+            CK(cudaMemcpyAsync(hc_out + 4 * z0, oc + 4 * z0, 4 * nz * sizeof(double), cudaMemcpyDeviceToHost,
+                               c->d2h));
+            CK(cudaMemcpyAsync(hs_out + z0, os + z0, nz * sizeof(double), cudaMemcpyDeviceToHost, c->d2h));
         }
     }
-    // the library's stream continues after every kind's last chunk and the downloads
-    for (int k = 0; k < K; ++k) CK(cudaStreamWaitEvent(c->stream, evK(k, G - 1), 0));
+    // the library's stream continues after every chunk stream, the ghost rows
+    // and the downloads
+    for (int k = 0; k < NS; ++k) {
+        CK(cudaEventRecord(c->ev_chunk[ev_start + 1 + k], c->kstreams[k]));
+        CK(cudaStreamWaitEvent(c->stream, c->ev_chunk[ev_start + 1 + k], 0));
+    }
+    CK(cudaStreamWaitEvent(c->stream, c->ev_chunk[ev_start + 1 + NS], 0));
     if (hc_out) {
         CK(cudaEventRecord(c->ev_chunk[ev_start], c->d2h));
         CK(cudaStreamWaitEvent(c->stream, c->ev_chunk[ev_start], 0));
@@ -2271,7 +2485,8 @@ int knc_advance_host(knc_ctx* c, const double* cons_in, const double* scalar_in,
                         device_view(scalar_out);
     // (the chunks update as warp strips, which need a polar grid)
     const bool streamed = pinned && fold > 0 && !adaptive && !c->fused && L(c).nremap == 0 &&
-                          c->model.kind != KNC_MODEL_HOST && c->mesh.p.num_polar_zones > 1;
+                          c->model.kind != KNC_MODEL_HOST && c->mesh.p.num_polar_zones > 1 &&
+                          chunks_fit(L(c), c->hp.runge_kutta_order);
     if (!streamed) {
         // whole-state copies around the fold
         if ((r = knc_set_state(c, cons_in, scalar_in))) return r;

@@ -204,7 +204,9 @@ __global__ void soa_to_aos_kernel(const double* __restrict__ soa, double* __rest
 // [nr][nq][4] then [nr][nq] scalar mass), one launch over the recovery tiles
 // (t.w = the block's first zone in the whole-state arrays). The host arrays
 // may be page-locked host memory read or written directly over the
-// CPU-GPU link, or a device staging copy.
+// CPU-GPU link, or a device staging copy. A shadow block's rows go into both
+// of its state buffers: rows its later stages do not update then still hold
+// a state that recovers as the first stage's did.
 __global__ void __launch_bounds__(TILE_THREADS) state_in_kernel(const DevBlock* __restrict__ blocks,
                                                                const int4* __restrict__ tiles, int sel,
                                                                const double* __restrict__ cons,
@@ -216,12 +218,15 @@ __global__ void __launch_bounds__(TILE_THREADS) state_in_kernel(const DevBlock* 
     const int64_t n = (int64_t)B.nr * B.nq, z = (int64_t)i * B.nq + j, g = (int64_t)t.w + z;
     const double2 a = reinterpret_cast<const double2*>(cons)[2 * g];
     const double2 b = reinterpret_cast<const double2*>(cons)[2 * g + 1];
-    double* U = B.buf[sel];
-    U[z] = a.x;
-    U[n + z] = a.y;
-    U[2 * n + z] = b.x;
-    U[3 * n + z] = b.y;
-    U[4 * n + z] = scalar[g];
+    const double sm = scalar[g];
+    for (int k = 0; k <= B.shadow; ++k) {
+        double* U = B.buf[sel ^ k];
+        U[z] = a.x;
+        U[n + z] = a.y;
+        U[2 * n + z] = b.x;
+        U[3 * n + z] = b.y;
+        U[4 * n + z] = sm;
+    }
 }
 
 __global__ void __launch_bounds__(TILE_THREADS) state_out_kernel(const DevBlock* __restrict__ blocks,
@@ -422,6 +427,26 @@ cudaError_t launch_state_out(const DevBlock* blocks, const int4* tiles, int ntil
                              double* scalar, cudaStream_t s) {
     if (ntiles <= 0) return cudaSuccess;
     state_out_kernel<<<ntiles, TILE_THREADS, 0, s>>>(blocks, tiles, sel, cons, scalar);
+    return cudaGetLastError();
+}
+
+// Two ghost rows of the five primitive fields, computed ahead into a compact
+// [5][2][nq] array, into rows row0, row0 + 1 of a block's padded
+// [5][nr + 4][nq] primitives; copied as 32-bit words (fields of 4 or 8 bytes).
+__global__ void halo_rows_kernel(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int64_t words,
+                                 int64_t dst_field_words, int64_t dst_off_words) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int f = blockIdx.y;
+    if (k >= words) return;
+    dst[f * dst_field_words + dst_off_words + k] = src[f * words + k];
+}
+
+cudaError_t launch_halo_rows(const void* src, void* dst, int nq, int nr, int row0, int elem_bytes, cudaStream_t s) {
+    const int64_t wq = (int64_t)nq * elem_bytes / 4;   // words per row
+    const int64_t words = 2 * wq;
+    dim3 grid((unsigned)((words + 255) / 256), NFIELD);
+    halo_rows_kernel<<<grid, 256, 0, s>>>(reinterpret_cast<const uint32_t*>(src), reinterpret_cast<uint32_t*>(dst),
+                                          words, (int64_t)(nr + 4) * wq, (int64_t)row0 * wq);
     return cudaGetLastError();
 }
 

@@ -64,7 +64,7 @@ struct DevBlock {
     int32_t nr_out_nbr;    // rows of the outer neighbour
     int32_t slot_in;       // slot of the inner neighbour, -1 at the inner edge
     int32_t slot_out;      // slot of the outer neighbour, -1 at the outer edge
-    int32_t pad_;
+    int32_t shadow;        // 1: a copy of a neighbour's edge rows (host-state chunks)
 };
 
 // Error key: lexicographic (stage, slot, i, j) with the hydro kind in the low
@@ -234,6 +234,7 @@ cudaError_t launch_state_in(const DevBlock* blocks, const int4* tiles, int ntile
                             const double* scalar, cudaStream_t s);
 cudaError_t launch_state_out(const DevBlock* blocks, const int4* tiles, int ntiles, int sel, double* cons,
                              double* scalar, cudaStream_t s);
+cudaError_t launch_halo_rows(const void* src, void* dst, int nq, int nr, int row0, int elem_bytes, cudaStream_t s);
 cudaError_t launch_prims_to_aos(const void* P, double* out, int64_t nr, int64_t nq, cudaStream_t s);
 cudaError_t launch_products(const void* P, const double* U, double* prim, double* scalar, int64_t nr, int64_t nq,
                             cudaStream_t s);

@@ -111,6 +111,20 @@ def test_streamed_many_blocks_per_chunk(tuning):
     _check(w, knc.abi.KNC_PRECISION_MIXED, 2, tuning)
 
 
+@pytest.mark.parametrize("order,block_size", [("RK3", 6), ("RK3", 4), ("RK2", 4), ("RK1", 2)])
+def test_streamed_short_blocks(order, block_size):
+    """Blocks of exactly the 2S rows a chunk boundary's shadow copies (S
+    stages), and RK3 on blocks of 4 rows, too short for shadows, which the
+    call advances through whole-state copies instead."""
+    import knc
+    from knc import workloads
+    w = workloads.wind_small()
+    w.mesh.block_size = block_size
+    w.mesh.num_polar_zones = 32
+    w.hydro.runge_kutta_order = order
+    _check(w, knc.abi.KNC_PRECISION_MIXED, 2)
+
+
 def test_streamed_separate_output():
     import knc
     from knc import workloads
@@ -140,10 +154,13 @@ def test_moving_mesh_rejected():
 
 @pytest.mark.parametrize("pinned", [True, False])
 @pytest.mark.parametrize("field,value,kind", [(0, -1.0, "NegativeDensity"), (3, -1e-3, "NegativeEnergyDensity")])
-def test_failure_reported_like_the_copies(pinned, field, value, kind):
+@pytest.mark.parametrize("row", [5, 0, -1])
+def test_failure_reported_like_the_copies(pinned, field, value, kind, row):
     """A poisoned zone in the host state fails the host-state advance at the
     zone the oracle reports (stage 0), in the streamed and the whole-copy
-    form; the context then refuses to go on until a state is set again."""
+    form; the context then refuses to go on until a state is set again. Rows
+    0 and nr - 1 of a block at a chunk boundary are also recovered in the
+    neighbouring chunk's shadow block: the block's own zone is reported."""
     import knc
     from helpers import make_pair
     from knc import workloads
@@ -151,11 +168,12 @@ def test_failure_reported_like_the_copies(pinned, field, value, kind):
     g, o = make_pair(w)
     keep, cons, scal = _host_state(g, pinned)
     nr, nq = g.shape_of(2)
-    z = 2 * nr * nq + 5 * nq + 7          # block 2, zone (5, 7)
+    i = row % nr
+    z = 2 * nr * nq + i * nq + 7          # block 2, zone (i, 7)
     cons[z, field] = value
     c2, s2 = o.get_block(2)
     c2 = c2.copy()
-    c2[5, 7, field] = value
+    c2[i, 7, field] = value
     o.add_block(2, c2, s2)
     assert o.try_advance(1) == 5
     eo = o.last_error()
@@ -163,7 +181,7 @@ def test_failure_reported_like_the_copies(pinned, field, value, kind):
         g.advance_host(cons, scal, 1)
     e = exc.value.error
     assert e["kind"] == kind
-    assert (e["block"], e["i"], e["j"]) == (eo.block, eo.i, eo.j) == (2, 5, 7)
+    assert (e["block"], e["i"], e["j"]) == (eo.block, eo.i, eo.j) == (2, i, 7)
     assert e["r"] == eo.r and e["theta"] == eo.theta
     with pytest.raises(knc.HydroError):
         g.advance(1)
