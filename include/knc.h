@@ -245,10 +245,10 @@ int knc_advance_dt(knc_ctx* ctx, int32_t fold, double dt);
  * excision surfaces change the block set, and so the arrays' size, inside
  * the fold: KNC_ERR_INVALID_ARGUMENT). With page-locked buffers
  * (knc_host_alloc or registered), a device model, no remaps, more than one
- * polar zone, the fixed SRHD time step and the separate stage form, the
- * first step's upload and the
- * last step's download run by chunks of blocks beside the stages; otherwise
- * the three calls run in turn. On failure the output buffers are unspecified
+ * polar zone, the fixed SRHD time step, the separate stage form and blocks
+ * of at least 2 x runge_kutta_order rows at chunk boundaries, the first
+ * step's upload and the last step's download run by chunks of blocks beside
+ * the stages; otherwise the three calls run in turn. On failure the output buffers are unspecified
  * and the state must be set again. */
 int knc_advance_host(knc_ctx* ctx, const double* cons_in, const double* scalar_in, double* cons_out,
                      double* scalar_out, int32_t fold);
