@@ -78,9 +78,11 @@ R0 = 1e6            # cm: the tube's inner end
 BLOCK = 0.5 / R0    # block width in log r: 4 blocks make a 2 cm tube
 
 
-def _tube(system, riemann, zones_per_block, left, right, gamma, t_end):
-    """Run a shock tube in the oracle; density L1 error against the exact
-    solution over the middle half of the tube, at the time reached."""
+def _tube(system, riemann, zones_per_block, left, right, gamma, t_end, make=None, out=None):
+    """Run a shock tube in the oracle (or in the solver `make(hydro, mesh)`
+    returns); density L1 error against the exact solution over the middle
+    half of the tube, at the time reached. `out` receives the final
+    primitives per block."""
     nb = 4
     mesh = config.Mesh(reference_radius=R0, inner_radius=R0, outer_radius=R0 * (1 + BLOCK) ** nb * (1 - 1e-12),
                        inner_excision_speed=0.0, outer_excision_speed=0.0, num_polar_zones=1,
@@ -91,7 +93,7 @@ def _tube(system, riemann, zones_per_block, left, right, gamma, t_end):
         hydro = config.RelativisticHydro(gamma, 1.5, 0.4, "RK2", riemann)
     hp, mp = hydro.to_c(), mesh.to_c()
     x0 = R0 * ((1 + BLOCK) ** nb - 1) / 2     # the diaphragm, mid-tube
-    o = ko.Oracle(hydro, mesh, threads=1)
+    o = make(hydro, mesh) if make else ko.Oracle(hydro, mesh, threads=1)
     o.set_model(config.SphereModel(rho_in=left[0], rho_out=right[0], radius=R0 + x0, pressure=right[2],
                                    noise=0.0))
     o.init_from_model(0.0)
@@ -110,7 +112,10 @@ def _tube(system, riemann, zones_per_block, left, right, gamma, t_end):
         o.advance(1)
     t = o.time()[0]
     x = np.concatenate([geo[i]["rc"][:, 0] - R0 - x0 for i in idx])
-    rho = np.concatenate([o.get_primitives(i)[:, 0, 0] for i in idx])
+    prims = {i: o.get_primitives(i) for i in idx}
+    if out is not None:
+        out.update(prims)
+    rho = np.concatenate([prims[i][:, 0, 0] for i in idx])
     ex = Newtonian(left, right, gamma) if system == "newtonian" else Relativistic(left, right, gamma)
     xi = x / (t if system == "newtonian" else t * LIGHT_SPEED)
     exact = np.array([ex.sample(z)[0] for z in xi])
@@ -135,6 +140,21 @@ def test_shock_tube_against_exact_solution(oracle_lib, name, riemann):
     fine = _tube(system, riemann, 200, left, right, gamma, t_end)
     assert fine < bound, (coarse, fine)
     assert fine < 0.65 * coarse, (coarse, fine)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["newtonian", "srhd_blast"])
+def test_gpu_shock_tube_bitwise(oracle_lib, name):
+    """The FP64 GPU stage through the C ABI on the same tubes: primitives
+    bit for bit the oracle's, so the same L1 against the exact solution."""
+    import knc
+    system, left, right, gamma, t_end, bound = TUBES[name]
+    po, pg = {}, {}
+    l1o = _tube(system, "HLLC", 200, left, right, gamma, t_end, out=po)
+    l1g = _tube(system, "HLLC", 200, left, right, gamma, t_end, make=knc.Solver, out=pg)
+    assert l1g == l1o and l1g < bound
+    for i in po:
+        assert np.array_equal(pg[i], po[i]), i
 
 
 # ---- uniform static state ------------------------------------------------------
