@@ -139,6 +139,35 @@ def test_whole_copy_forms():
     _check(workloads.uneven_small(moving=False), knc.abi.KNC_PRECISION_FP64, 2)
 
 
+@pytest.mark.parametrize("case", ["newtonian", "srhd_adaptive", "host_model"])
+def test_whole_copy_forms_of_other_systems(case):
+    """Adaptive time steps (Newtonian, SRHD with adaptive_time_step) and a
+    host callback model take the whole-copy form; still bitwise the copies."""
+    import knc
+    from knc import workloads
+    if case == "newtonian":
+        w = workloads.sphere_small(riemann="HLLC")
+    else:
+        w = workloads.wind_small()
+        if case == "srhd_adaptive":
+            w.hydro.adaptive_time_step = True
+    prec = knc.abi.KNC_PRECISION_FP64
+    if case == "host_model":
+        a, b = _solvers(w, prec)
+        def wind(r, q, t):   # AnyPrimitive [u_r, u_theta, rho, p], scalar
+            return [1.0, 0.0, 1.0 / (r * r), 1e-4 / (r * r)], 0.0
+        for s in (a, b):
+            s.set_host_model(wind)
+            s.advance(2)
+        keep, cons, scal = _host_state(a, True)
+        ref_c, ref_s = _by_copies(b, cons.copy(), scal.copy(), 2)
+        a.advance_host(cons, scal, 2)
+        assert np.array_equal(cons, ref_c) and np.array_equal(scal, ref_s)
+        del keep
+        return
+    _check(w, prec, 2)
+
+
 def test_moving_mesh_rejected():
     """The block set of a moving mesh changes inside the fold, so flat
     whole-state arrays cannot hold the result: the call refuses."""
