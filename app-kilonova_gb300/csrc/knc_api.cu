@@ -224,7 +224,9 @@ void free_block(BlockH& b) {
     b = BlockH();
 }
 
-// Rows of the warp strips the host-state advance updates chunks with.
+// Rows of the warp strips the host-state advance updates chunks with
+// (host-state step on the 4096 x 1024 wind: 2, 4, 8 rows measured 1.372,
+// 1.358, 1.379 ms).
 constexpr int STREAM_STRIP_ROWS = 4;
 
 // One block set's device view.
