@@ -297,6 +297,9 @@ struct Layout {
     double* d_ghost_rc = nullptr;                  // [2 ends][2 rows]
     double* d_ghost_dv[2] = {nullptr, nullptr};    // per end [2][nq]
     int64_t ghost_nq[2] = {0, 0};
+    // mixed stage: the ghost rows in FP64 as well, per end [5][2][nq_edge]
+    double* d_ghost64[2] = {nullptr, nullptr};
+    int32_t ghost64_nq[2] = {0, 0};
     std::vector<double> ghost_rc_h, ghost_dv_h[2];
     // a block activated at the start of the step this layout begins
     int4* d_init_tiles = nullptr;
@@ -317,6 +320,8 @@ void free_layout(Layout& l) {
     cudaFree(l.d_ghost_rc);
     cudaFree(l.d_ghost_dv[0]);
     cudaFree(l.d_ghost_dv[1]);
+    cudaFree(l.d_ghost64[0]);
+    cudaFree(l.d_ghost64[1]);
     cudaFree(l.d_init_tiles);
     cudaFree(l.d_sc_table);
     cudaFree(l.d_sc_tiles);
@@ -820,6 +825,12 @@ int rebuild_table(knc_ctx* c) {
         L(c).P_edge[end] = e.P;
         L(c).nr_edge[end] = (int32_t)e.nr;
         L(c).nq_edge[end] = (int32_t)e.nq;
+        if (L(c).ghost64_nq[end] != (int32_t)e.nq) {
+            cudaFree(L(c).d_ghost64[end]);
+            L(c).d_ghost64[end] = nullptr;
+            CK(dalloc(&L(c).d_ghost64[end], (size_t)(NFIELD * 2 * e.nq)));
+            L(c).ghost64_nq[end] = (int32_t)e.nq;
+        }
     }
     CK(cudaStreamSynchronize(c->stream));
     L(c).ntiles = (int)tiles.size();
@@ -975,6 +986,7 @@ StageArgs base_args(knc_ctx* c) {
     a.theta_f = (float)a.plm_theta;
     a.cflux_f = (float)a.cflux;
     a.high_thr_f = (float)(1.0 - 1.0 / (c->w_split * c->w_split));
+    a.uu_high_f = (float)(c->w_split * c->w_split - 1.0);
     const int le = length_exponent(c->mesh.p);
     a.lscale2 = 2 * le;
     a.lscale3 = 3 * le;
@@ -1053,6 +1065,8 @@ int prepare_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, 
     g.stage = stage;
     g.gm = c->hp.gamma_law_index;
     g.single_precision = mixed(c) ? 1 : 0;
+    if (mixed(c))
+        for (int end = 0; end < 2; ++end) g.P64[end] = lay.P_edge[end] ? lay.d_ghost64[end] : nullptr;
     g.status = c->d_status;
     if (c->ddt) {
         g.dt_bits = &c->d_status->dt_bits;
@@ -1077,6 +1091,8 @@ int prepare_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, 
     a.dt = dt;
     a.dt_f = (float)dt;
     a.avg_half = w1 == 0.5 && bf == 0.5 ? 1 : 0;
+    a.g64[0] = g.P64[0];
+    a.g64[1] = g.P64[1];
     if (mixed(c) && !c->fused && c->rform == KNC_RECOVERY_DEFERRED && L(c).d_high) {
         a.high = L(c).d_high;
         a.high_count = &c->d_status->high_count[stage & 1];
@@ -2328,9 +2344,9 @@ int stream_step(knc_ctx* c, double dt, const double* hc_in, const double* hs_in,
             return r;
     // staging: the step's input state (cons [total][4], then scalar [total]),
     // then its output state in the same layout, then per stage and mesh end
-    // the ghost rows [5][2][nq]
+    // the ghost rows [5][2][nq], then (mixed) the same rows in FP64
     const int64_t gq = std::max(lay.nq_edge[0], lay.nq_edge[1]);
-    if ((r = ensure_stage(c, 10 * (size_t)total + (size_t)S * 2 * 10 * gq))) return r;
+    if ((r = ensure_stage(c, 10 * (size_t)total + (size_t)S * 2 * 10 * gq * 2))) return r;
     const int NS = std::min(G, HOST_STREAMS);
     // events: uploads [0, G), downloads ready [G, 2 G), start, stream ends
     // [2 G + 1, 2 G + 2 + NS) (the last: ghost rows), ghost rows of stage s
@@ -2363,10 +2379,12 @@ int stream_step(knc_ctx* c, double dt, const double* hc_in, const double* hs_in,
     CK(cudaStreamWaitEvent(gst, c->ev_chunk[ev_start], 0));
     double* gscr = c->d_stage + 10 * total;
     auto gscratch = [&](int s, int end) { return gscr + (size_t)(2 * s + end) * 10 * gq; };
+    auto gscratch64 = [&](int s, int end) { return gscr + (size_t)(2 * S + 2 * s + end) * 10 * gq; };
     for (int s = 0; s < S; ++s) {
         GhostArgs ge = g[s];
         for (int end = 0; end < 2; ++end) {
             if (ge.P[end]) ge.P[end] = gscratch(s, end);
+            if (ge.P64[end]) ge.P64[end] = gscratch64(s, end);
             ge.row0[end] = 0;
             ge.nr_t[end] = -2;   // row stride nr_t + 4 = 2: the compact [5][2][nq]
         }
@@ -2408,6 +2426,9 @@ int stream_step(knc_ctx* c, double dt, const double* hc_in, const double* hs_in,
             y.strips = lay.d_sc_strips + lay.sc_strip_off[k * S + s];
             y.nstrips = lay.sc_strip_off[k * S + s + 1] - lay.sc_strip_off[k * S + s];
             y.tma = 0;
+            // the FP64 ghost rows of this stage, computed ahead like the FP32 ones
+            for (int end = 0; end < 2; ++end)
+                if (y.g64[end]) y.g64[end] = gscratch64(s, end);
             y.high = nullptr;
             y.high_count = nullptr;
             y.high_count_next = nullptr;

@@ -155,7 +155,7 @@ __device__ __forceinline__ void stage_fused_body(const StageArgs& a, const Ghost
             constexpr int WPC = NT / 32;
             const PhysT<R> ph = make_phys<R>(a);
             for (int k = blockIdx.x * WPC + (int)(threadIdx.x >> 5); k < a.nstrips; k += gridDim.x * WPC)
-                update_strip<R, MIXED>(a, a.strips[k], ph);
+                strip_dispatch<R, MIXED>(a, a.strips[k], ph);
         } else if constexpr (!STRIPS_ONLY) {
             for (int tile = blockIdx.x; tile < a.nutiles; tile += gridDim.x) {
                 update_tile<R, MIXED, TR>(a, a.utiles[tile], smem_raw);

@@ -100,6 +100,11 @@ static __device__ __noinline__ void ghost_zone(const GhostArgs& a, int end, int 
         float* Pd = reinterpret_cast<float*>(a.P[end]);
 #pragma unroll
         for (int c = 0; c < NFIELD; ++c) Pd[c * pn + off] = (float)v[c];
+        if (a.P64[end]) {
+            double* Q = a.P64[end] + (int64_t)row * nq + j;
+#pragma unroll
+            for (int c = 0; c < NFIELD; ++c) Q[(int64_t)c * 2 * nq] = v[c];
+        }
     } else {
         double* Pd = reinterpret_cast<double*>(a.P[end]);
 #pragma unroll

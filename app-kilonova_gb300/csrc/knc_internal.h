@@ -124,6 +124,13 @@ struct StageArgs {
     // in FP64 for them (on GB300 the FP64 pipe is the narrow one)
     float gm_f, gm1_f, gh_f, theta_f, dt_f, cflux_f;
     float high_thr_f;       // 1 - 1 / w_split^2: |S| / (D + tau) squared above it means W > w_split
+    // mixed update: a zone whose stored FP32 four-velocity has
+    // u_r^2 + u_theta^2 = W^2 - 1 above uu_high_f (W above the split) makes
+    // every face whose 4-zone stencil reaches it an FP64 face (zone_hp)
+    float uu_high_f;
+    // FP64 ghost rows of the inner / outer mesh end ([5][2][nq], written by the
+    // ghost launch of this stage), or null (the FP32 rows are used instead)
+    const double* g64[2];
     // mixed stage length unit L = 2^e: its FP32 geometry is in units of L
     // (areas 2^(-2e), volumes 2^(-3e)), so increments scale back by 2^(2e)
     // and recovered densities use volumes in L^3
@@ -155,6 +162,8 @@ struct GhostArgs {
     int32_t stage;
     double gm;
     int32_t single_precision;   // write float P
+    // mixed stage: the same rows in FP64 as well, [5][2][nq] per end, or null
+    double* P64[2];
     DevStatus* status;
     // adaptive dt found on the device in the fold's first recovery: the stage
     // time is then fold_stage_time(t0, dt, order, step, sub), dt = *dt_bits x cfl

@@ -53,41 +53,6 @@ static cudaError_t launch_chained(void (*k)(Params...), int grid, int block, siz
     return cudaLaunchKernelEx(&cfg, k, args...);
 }
 
-
-// Newton-Raphson on the pressure, the reference's iteration rewritten with two
-// divisions: with X = tau + m (1 - W) + p (1 - W^2) and 1 - v^2 = 1/W^2,
-// rho e = X / W^2, f = (gamma - 1) rho e - p, rho h = m / W + rho e + p and
-// f / f' = f rho h / (v^2 gamma p - rho h). Converged when |f| < tol_abs or the
-// step is below tol_rel |p| (FP32 only; tol_rel = 0 reproduces the reference's
-// criterion). Returns the root and W at the last evaluated pressure.
-template <class R>
-__device__ __forceinline__ bool newton_fast(R m, R ss, R tau, R gm, R p, R tol_abs, R tol_rel, int maxit, R& p_out,
-                                            R& w_out, int& iters) {
-    const R bmax = sizeof(R) == 8 ? R(1.0 - 1e-10) : R(1.0f - 1e-6f);
-    for (int n = 0; n < maxit; ++n) {
-        const R et = tau + p + m;
-        const R inv = R(1) / et;
-        const R b2 = rmin(ss * inv * inv, bmax);
-        const R omb = R(1) - b2;
-        const R w = sizeof(R) == 8 ? (R)rsqrt((double)omb) : (R)rsqrtf((float)omb);
-        const R w2 = w * w;
-        const R X = tau + m * (R(1) - w) + p * (R(1) - w2);
-        const R de = X * omb;
-        const R f = (gm - R(1)) * de - p;
-        const R dh = m * omb * w + de + p;
-        const R den = b2 * gm * p - dh;
-        const R step = f * dh / den;
-        p = p - step;
-        iters = n + 1;
-        if (rabs(f) < tol_abs || rabs(step) <= tol_rel * rabs(p)) {
-            p_out = p;
-            w_out = w;
-            return p == p;   // false for NaN
-        }
-    }
-    return false;
-}
-
 // The learned-guess inference out of line: warps run it only when one of
 // their zones needs the FP64 recovery, so its register demand stays out of
 // the common path.

@@ -99,6 +99,32 @@ __device__ __forceinline__ R stage_dt(const StageArgs& a) {
     return sizeof(R) == 4 ? (R)a.dt_f : (R)a.dt;
 }
 
+// ---- FP64 faces of the mixed stage at high Lorentz factor -----------------------
+// FP32 face states of a flow with W well above 1 lose its thermal energy: the
+// kinetic part of tau and of the energy flux is O(rho W^2) and rounds at
+// 6e-8 of that, which for p / rho ~ 1e-3 is a 1e-4 error in the pressure and
+// moves shocks by a fraction of a zone (the W = 100 jet). So the mixed stage
+// keeps FP64 where the Lorentz factor is above the split, as it already does
+// for the recovery: every face whose 4-zone stencil holds a zone with
+// W > w_split (judged from the stored FP32 four-velocity, the same test in
+// every update form) is solved in FP64 from FP64 primitives, and the zones
+// such faces bound are updated in FP64 (zone_hp, after the strip helpers).
+
+__device__ __forceinline__ bool high_zone(float ur, float uq, float thr) {
+    return __fmaf_rn(ur, ur, __fmul_rn(uq, uq)) > thr;
+}
+
+// The FP64 faces of zone (i, j) from the relativistic zones of its plus-shaped
+// stencil: col bit k = zone (i - 2 + k, j), row bit k = zone (i, j - 2 + k),
+// k = 0..4. Result: bit 0 radial face i, bit 1 radial face i + 1, bit 2 polar
+// face j, bit 3 polar face j + 1 (zero: the zone takes the FP32 update).
+__device__ __forceinline__ unsigned hp_faces(unsigned col, unsigned row) {
+    return ((col & 0xfu) ? 1u : 0u) | ((col & 0x1eu) ? 2u : 0u) | ((row & 0xfu) ? 4u : 0u) |
+           ((row & 0x1eu) ? 8u : 0u);
+}
+
+static __device__ __noinline__ void zone_hp(const StageArgs& a, const DevBlock& B, int i, int j);
+
 template <class R, bool MIXED, int TR_, bool BOX = false>
 __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, unsigned char* smem_raw,
                                             const R* boxP = nullptr, const double* boxU = nullptr,
@@ -250,7 +276,23 @@ __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, un
     if (tid < TR * TQ) {
         const int r = tid / TQ, c = tid - r * TQ;
         const int i = i0 + r, j = j0 + c;
-        if (i < nr && j < nq) {
+        unsigned hpf = 0u;
+        if constexpr (MIXED) {
+            // FP64 faces (a relativistic zone in the plus stencil): zone_hp
+            if (i < nr && j < nq) {
+                unsigned cm = 0u, rm = 0u;
+#pragma unroll
+                for (int k = 0; k < 5; ++k) {
+                    const R* zc = sPc + (PR + r + k) * PQS + c + 2;   // u_r of zone (i - 2 + k, j)
+                    const R* zr = sPc + (PR + r + 2) * PQS + c + k;   // u_r of zone (i, j - 2 + k)
+                    cm |= high_zone(zc[0], zc[PR * PQS], a.uu_high_f) ? 1u << k : 0u;
+                    rm |= high_zone(zr[0], zr[PR * PQS], a.uu_high_f) ? 1u << k : 0u;
+                }
+                hpf = hp_faces(cm, rm);
+                if (hpf) zone_hp(a, B, i, j);
+            }
+        }
+        if (i < nr && j < nq && !(MIXED && hpf)) {
             const int64_t n = (int64_t)nr * nq;
             const int64_t z = (int64_t)i * nq + j;
             R Pc[4];
@@ -373,7 +415,200 @@ __device__ __forceinline__ void strip_face(const PhysT<R>& ph, const StageArgs& 
     }
 }
 
-template <class R, bool MIXED>
+// ---- FP64 faces of the mixed stage at high Lorentz factor (zone_hp) -----------
+// FP64 primitive (rho, u_r, u_theta, p, s) of zone (r, c) of block B,
+// r in [-2, nr + 1] (rows outside the block from the neighbour or the ghost
+// rows), recovered from the FP64 state of this stage with the reference's
+// residual |f| < 1e-12 (D + tau), the stored FP32 pressure as the Newton
+// start. Where no FP64 state is at hand (a neighbour of another polar
+// resolution, ghost rows without an FP64 copy) the stored FP32 primitive is
+// taken as it is.
+static __device__ __noinline__ void prim_hp(const StageArgs& a, const DevBlock& B, int r, int c, double v[NFIELD]) {
+    const int nq = B.nq;
+    const float* P = reinterpret_cast<const float*>(B.P);
+    const int64_t pn = (int64_t)(B.nr + 4) * nq;
+    const int64_t off = (int64_t)(r + 2) * nq + c;
+    float pf[NFIELD];
+#pragma unroll
+    for (int q = 0; q < NFIELD; ++q) pf[q] = P[q * pn + off];
+    const DevBlock* S = &B;
+    int rr = r;
+    int ghost = -1;
+    if (r < 0) {
+        if (B.slot_in >= 0) {
+            S = &a.blocks[B.slot_in];
+            rr = S->nr + r;
+        } else {
+            ghost = 0;
+        }
+    } else if (r >= B.nr) {
+        if (B.slot_out >= 0) {
+            S = &a.blocks[B.slot_out];
+            rr = r - B.nr;
+        } else {
+            ghost = 1;
+        }
+    }
+    if (ghost >= 0 && !B.shadow && a.g64[ghost]) {
+        const int row = ghost == 0 ? r + 2 : r - B.nr;
+#pragma unroll
+        for (int q = 0; q < NFIELD; ++q) v[q] = a.g64[ghost][(int64_t)q * 2 * nq + (int64_t)row * nq + c];
+        return;
+    }
+#pragma unroll
+    for (int q = 0; q < NFIELD; ++q) v[q] = (double)pf[q];
+    if (ghost >= 0 || S->nq != nq) return;
+    const int64_t n = (int64_t)S->nr * nq, z = (int64_t)rr * nq + c;
+    const double* U = S->buf[a.sel_in] + z;
+    const double m = U[0], s1 = U[n], s2 = U[2 * n], tau = U[3 * n], smass = U[4 * n];
+    const double dv = S->dv[z];
+    if (!(m > 0.0) || !(tau >= 0.0)) return;
+    const double ss = s1 * s1 + s2 * s2;
+    const double tol = NEWTON_TOLERANCE * (m + tau);
+    double p = 0.0, w = 1.0;
+    int it = 0;
+    // the FP32 pressure as the start, volume-integrated like the state
+    if (!newton_fast<double>(m, ss, tau, a.gm, (double)pf[3] * dv, tol, 0.0, NEWTON_ITER_MAX, p, w, it)) {
+        const double u[4] = {m, s1, s2, tau};
+        double Pd[4];
+        double bad;
+        if (srhd_c2p_newton(a.gm, u, 0.0, Pd, it, bad) == HYDRO_ROOT_FINDER_FAILED) return;
+        v[0] = Pd[0] / dv;
+        v[1] = Pd[1];
+        v[2] = Pd[2];
+        v[3] = Pd[3] / dv;
+        v[4] = smass / dv / sqrt(1.0 + Pd[1] * Pd[1] + Pd[2] * Pd[2]);
+        return;
+    }
+    const double inv_et = 1.0 / (tau + m + p);
+    v[0] = m / w / dv;
+    v[1] = w * s1 * inv_et;
+    v[2] = w * s2 * inv_et;
+    v[3] = p < 0.0 ? PRESSURE_FLOOR * v[0] : p / dv;
+    v[4] = smass / dv / sqrt(1.0 + v[1] * v[1] + v[2] * v[2]);
+}
+
+// One face from its stencil s[0..3] (the face between s[1] and s[2]) with the
+// stage's limiter; zl / zr: zero slope for s[1] / s[2] (the block's first and
+// last column). FP64: the reference's face solve. FP32: the instructions the
+// update forms run for the same face, so the value equals theirs.
+template <class R>
+__device__ __forceinline__ void face_states(R th, const R (*s)[NFIELD], bool zl, bool zr, R pl[NFIELD],
+                                            R pr[NFIELD]) {
+#pragma unroll
+    for (int q = 0; q < NFIELD; ++q) {
+        const R gl = zl ? R(0) : stage_plm<R, sizeof(R) == 4>(th, s[0][q], s[1][q], s[2][q]);
+        const R gr = zr ? R(0) : stage_plm<R, sizeof(R) == 4>(th, s[1][q], s[2][q], s[3][q]);
+        pl[q] = s[1][q] + gl * R(0.5);
+        pr[q] = s[2][q] - gr * R(0.5);
+    }
+}
+
+// Zone (i, j) of the mixed stage when its plus-shaped stencil holds a zone
+// above the Lorentz-factor split (update forms: high_zone / hp_faces). Its
+// faces whose 4-zone stencil holds such a zone are solved in FP64 from FP64
+// primitives (prim_hp); its other faces are solved again in FP32 from the
+// stored primitives with the update forms' own instructions, so a face
+// shared with a zone of the FP32 update carries the same flux on both sides.
+// Sources, update and RK average in FP64, written to U_out. Every zone
+// bordering an FP64 face solves that face from the same inputs with the same
+// instructions, so both of its zones see one flux.
+static __device__ __noinline__ void zone_hp(const StageArgs& a, const DevBlock& B, int i, int j) {
+    const int nq = B.nq, nr = B.nr;
+    const float* P = reinterpret_cast<const float*>(B.P);
+    const int64_t pn = (int64_t)(nr + 4) * nq;
+    // FP32 primitives as the update forms see them: col32[k] zone (i - 2 + k, j),
+    // row32[k] zone (i, j - 2 + k), zero outside the padded rows and the block's columns
+    float col32[5][NFIELD], row32[5][NFIELD];
+    unsigned cm = 0u, rm = 0u;
+    for (int k = 0; k < 5; ++k) {
+        const int c = j - 2 + k;
+        load_prim_row(P, pn, nq, nr, j, true, i - 2 + k, col32[k]);
+        load_prim_row(P, pn, nq, nr, c, c >= 0 && c < nq, i, row32[k]);
+        cm |= high_zone(col32[k][1], col32[k][2], a.uu_high_f) ? 1u << k : 0u;
+        rm |= high_zone(row32[k][1], row32[k][2], a.uu_high_f) ? 1u << k : 0u;
+    }
+    const unsigned faces = hp_faces(cm, rm);
+    const PhysT<float> ph32 = make_phys<float>(a);
+    const PhysT<double> ph = make_phys<double>(a);
+    // col[k]: zone (i - 2 + k, j); row[k]: zone (i, j - 2 + k), FP64
+    double col[5][NFIELD], row[5][NFIELD];
+    prim_hp(a, B, i, j, col[2]);
+#pragma unroll
+    for (int q = 0; q < NFIELD; ++q) row[2][q] = col[2][q];
+    if (faces & 3u)
+        for (int k = 0; k < 5; ++k)
+            if (k != 2) prim_hp(a, B, i - 2 + k, j, col[k]);
+    if (faces & 12u)
+        for (int k = 0; k < 5; ++k) {
+            const int c = j - 2 + k;
+            if (k == 2) continue;
+            if (c >= 0 && c < nq) {
+                prim_hp(a, B, i, c, row[k]);
+            } else {
+#pragma unroll
+                for (int q = 0; q < NFIELD; ++q) row[k][q] = 0.0;
+            }
+        }
+    const double l2 = ldexp(1.0, a.lscale2);   // FP32 fluxes carry areas in the stage's length units
+    double F[4][NFIELD];
+    for (int f = 0; f < 4; ++f) {
+        // face f: radial i, radial i + 1, polar j, polar j + 1
+        const bool radial = f < 2;
+        const int k = radial ? i + f : j + (f - 2);   // between rows / columns k - 1 and k
+        const bool exists = radial ? k <= nr : (k > 0 && k < nq && i < nr);
+        const bool zl = !radial && (k - 1 == 0 || k - 1 == nq - 1);
+        const bool zr = !radial && (k == 0 || k == nq - 1);
+#pragma unroll
+        for (int q = 0; q < NFIELD; ++q) F[f][q] = 0.0;
+        if (!exists) continue;
+        if ((faces >> f) & 1u) {
+            double pl[NFIELD], pr[NFIELD], out[NFIELD];
+            face_states<double>(ph.theta, radial ? &col[f] : &row[f - 2], zl, zr, pl, pr);
+            riemann(ph, pl, pr, pl[4], pr[4], radial ? 0 : 1, out);
+            const double A = radial ? B.ar[(int64_t)k * nq + j] : B.aq[(int64_t)i * (nq + 1) + k];
+#pragma unroll
+            for (int q = 0; q < NFIELD; ++q) F[f][q] = out[q] * a.cflux * A;
+        } else {
+            float pl[NFIELD], pr[NFIELD], out[NFIELD] = {0.f, 0.f, 0.f, 0.f, 0.f};
+            face_states<float>(ph32.theta, radial ? &col32[f] : &row32[f - 2], zl, zr, pl, pr);
+            strip_face<float, true>(ph32, a, B, radial ? 0 : 1, pl, pr, radial ? k : i, radial ? j : k, nq,
+                                    a.cflux_f, out);
+#pragma unroll
+            for (int q = 0; q < NFIELD; ++q) F[f][q] = (double)out[q] * l2;
+        }
+    }
+    const int64_t n = (int64_t)nr * nq, z = (int64_t)i * nq + j;
+    double src[4];
+    sources(ph, col[2], B.rc[i], B.cot[j], src);
+    const double dv = B.dv[z];
+    const double dt = stage_dt<double>(a);
+    const double* Uin = B.buf[a.sel_in];
+    double* Uout = B.buf[a.sel_out];
+    double res[NFIELD];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const double du = (src[q] * a.cflux * dv - (F[1][q] - F[0][q]) - (F[3][q] - F[2][q])) * dt;
+        res[q] = Uin[q * n + z] + du;
+    }
+    res[4] = Uin[4 * n + z] + ((F[1][4] - F[0][4]) + (F[3][4] - F[2][4])) * -dt;
+    if (a.sel_base >= 0) {
+        const double* U0 = B.buf[a.sel_base];
+        if (a.avg_half) {
+#pragma unroll
+            for (int q = 0; q < NFIELD; ++q) res[q] = half_exact(res[q] + U0[q * n + z]);
+        } else {
+#pragma unroll
+            for (int q = 0; q < NFIELD; ++q) res[q] = res[q] * a.w1 + U0[q * n + z] * a.bf;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NFIELD; ++q) Uout[q * n + z] = res[q];
+}
+
+// HP (mixed stage only): the strip reaches a zone above the Lorentz-factor
+// split; zones with FP64 faces are left to zone_hp after the row loop.
+template <class R, bool MIXED, bool HP = false>
 __device__ __forceinline__ void update_strip(const StageArgs& a, const int4 it, const PhysT<R>& ph) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -412,7 +647,18 @@ __device__ __forceinline__ void update_strip(const StageArgs& a, const int4 it, 
         for (int q = 0; q < NFIELD; ++q) Flo[q] = R(0);
         if (i0 <= nr && j < nq && jin) strip_face<R, MIXED>(ph, a, B, 0, pl, pr, i0, j, nq, cflux, Flo);
     }
+    // mixed: hk = the warp's relativistic zones of window row i - 2 + k (bit =
+    // lane), warp-uniform; hp: some lane left zones to zone_hp
+    unsigned h0 = 0u, h1 = 0u, h2 = 0u, h3 = 0u, h4 = 0u;
+    bool hp = false;
+    if constexpr (HP) {
+        h0 = __ballot_sync(full, high_zone(Pa[1], Pa[2], a.uu_high_f));
+        h1 = __ballot_sync(full, high_zone(P2[1], P2[2], a.uu_high_f));
+        h2 = __ballot_sync(full, high_zone(P0[1], P0[2], a.uu_high_f));
+        h3 = __ballot_sync(full, high_zone(P1[1], P1[2], a.uu_high_f));
+    }
     load_prim_row(P, pn, nq, nr, j, jin, i0 + 2, P2);
+    if constexpr (HP) h4 = __ballot_sync(full, high_zone(P2[1], P2[2], a.uu_high_f));
 
     // per-column factors
     const int jc = jin ? j : 0;
@@ -421,6 +667,8 @@ __device__ __forceinline__ void update_strip(const StageArgs& a, const int4 it, 
         // the next row, one step ahead
         R Pn[NFIELD];
         load_prim_row(P, pn, nq, nr, j, jin, i + 3, Pn);
+        unsigned h5 = 0u;
+        if constexpr (HP) h5 = __ballot_sync(full, high_zone(Pn[1], Pn[2], a.uu_high_f));
         // this row's state and RK base towards L1 (read at the end of the step)
         if (MIXED && writes) {
             const int64_t z = (int64_t)i * nq + j;
@@ -454,8 +702,19 @@ __device__ __forceinline__ void update_strip(const StageArgs& a, const int4 it, 
             Fhi[q] = R(0);
         }
         if (i + 1 <= nr && jin) strip_face<R, MIXED>(ph, a, B, 0, plr, prr, i + 1, j, nq, cflux, Fhi);
-        // ---- sources, conserved update, RK average of zone (i, j)
-        if (writes) {
+        // ---- mixed: a relativistic zone in the plus stencil (FP64 faces) leaves
+        // the zone to zone_hp after the row loop, its state untouched until then
+        unsigned hpf = 0u;
+        if constexpr (HP) {
+            if ((h0 | h1 | h2 | h3 | h4) != 0u) {
+                const unsigned col = ((h0 >> lane) & 1u) | ((h1 >> lane) & 1u) << 1 | ((h2 >> lane) & 1u) << 2 |
+                                     ((h3 >> lane) & 1u) << 3 | ((h4 >> lane) & 1u) << 4;
+                hpf = hp_faces(col, lane >= 2 ? (h2 >> (lane - 2)) & 0x1fu : 0u);   // lane = column + 2 - j0
+                hp = hp || __any_sync(full, writes && hpf);
+            }
+        }
+        if (writes && !(HP && hpf)) {
+            // ---- sources, conserved update, RK average of zone (i, j)
             const int64_t z = (int64_t)i * nq + jc;
             R src[4];
             R dV = R(0);
@@ -493,6 +752,13 @@ __device__ __forceinline__ void update_strip(const StageArgs& a, const int4 it, 
             for (int q = 0; q < NFIELD; ++q) Uout[q * n + z] = res[q];
         }
         // ---- advance the window
+        if constexpr (HP) {
+            h0 = h1;
+            h1 = h2;
+            h2 = h3;
+            h3 = h4;
+            h4 = h5;
+        }
 #pragma unroll
         for (int q = 0; q < NFIELD; ++q) {
             Flo[q] = Fhi[q];
@@ -502,6 +768,66 @@ __device__ __forceinline__ void update_strip(const StageArgs& a, const int4 it, 
             P2[q] = Pn[q];
         }
     }
+    // the zones with FP64 faces, once the row window is dead: the strip's rows
+    // again, with the same relativistic-zone test (four-velocity rows only)
+    if constexpr (HP) {
+        if (hp) {
+            const float* Pu = reinterpret_cast<const float*>(B.P) + pn;   // u_r; u_theta one field further
+            auto high_row = [&](int zrow) -> unsigned {
+                const int prow = zrow + 2;
+                if (!jin || prow >= nr + 4) return 0u;
+                const int64_t off = (int64_t)prow * nq + j;
+                return high_zone(Pu[off], Pu[pn + off], a.uu_high_f) ? 1u : 0u;
+            };
+            unsigned h = high_row(i0 - 2) | high_row(i0 - 1) << 1 | high_row(i0) << 2 | high_row(i0 + 1) << 3;
+            for (int s = 0; s < rows; ++s) {
+                h |= high_row(i0 + s + 2) << 4;
+                const unsigned m = __ballot_sync(full, (h & 4u) != 0u);
+                if (writes && hp_faces(h & 0x1fu, lane >= 2 ? (m >> (lane - 2)) & 0x1fu : 0u))
+                    zone_hp(a, B, i0 + s, jc);
+                h >>= 1;
+            }
+        }
+    }
+}
+
+// Whether strip it = {slot, i0, j0, rows} reaches a zone above the Lorentz
+// factor split: the stored four-velocity of every zone its output zones'
+// stencils read (rows i0 - 2 .. i0 + rows + 1 of its 32 columns), warp-wide.
+__device__ __forceinline__ bool strip_reaches_high(const StageArgs& a, const int4 it) {
+    const DevBlock& B = a.blocks[it.x];
+    const int nr = B.nr, nq = B.nq;
+    const int j = it.z - 2 + (int)(threadIdx.x & 31);
+    const float* Pu = reinterpret_cast<const float*>(B.P) + (int64_t)(nr + 4) * nq;   // u_r; u_theta one field on
+    const int64_t pn = (int64_t)(nr + 4) * nq;
+    bool any = false;
+    if (j >= 0 && j < nq) {
+        const int r1 = min(it.y + it.w + 4, nr + 4);   // padded rows i0 .. i0 + rows + 3
+        for (int r = it.y; r < r1; ++r) {
+            const int64_t off = (int64_t)r * nq + j;
+            any |= high_zone(Pu[off], Pu[pn + off], a.uu_high_f);
+        }
+    }
+    return __any_sync(0xffffffffu, any);
+}
+
+// A strip with FP64 faces, out of line: its detection and zone_hp calls stay
+// out of the register allocation of the common strip.
+static __device__ __noinline__ void update_strip_hp(const StageArgs& a, const int4 it) {
+    update_strip<float, true, true>(a, it, make_phys<float>(a));
+}
+
+// One warp strip of a stage: the mixed stage checks first whether the strip
+// reaches a zone above the Lorentz-factor split.
+template <class R, bool MIXED>
+__device__ __forceinline__ void strip_dispatch(const StageArgs& a, const int4 it, const PhysT<R>& ph) {
+    if constexpr (MIXED) {
+        if (strip_reaches_high(a, it)) {
+            update_strip_hp(a, it);
+            return;
+        }
+    }
+    update_strip<R, MIXED>(a, it, ph);
 }
 
 // Strips (a.strips) in a grid-stride loop over warps; MB = resident CTAs per
@@ -516,7 +842,7 @@ __global__ void __launch_bounds__(STRIP_WARPS * 32, MB) update_strip_kernel(Stag
     if (*(volatile unsigned long long*)&a.status->err_key != NO_ERROR) return;
     const PhysT<R> ph = make_phys<R>(a);
     const int warp = blockIdx.x * STRIP_WARPS + (threadIdx.x >> 5);
-    for (int k = warp; k < a.nstrips; k += gridDim.x * STRIP_WARPS) update_strip<R, MIXED>(a, a.strips[k], ph);
+    for (int k = warp; k < a.nstrips; k += gridDim.x * STRIP_WARPS) strip_dispatch<R, MIXED>(a, a.strips[k], ph);
 }
 
 // Block-wide reduction helpers (warp shuffles, then one atomic per warp).
