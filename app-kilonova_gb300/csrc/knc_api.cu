@@ -396,6 +396,10 @@ struct knc_ctx {
     int ddt_step = 0;      // step of the fold being issued
     double w_split = 2.0;
     float* d_mlp = nullptr;
+    // the bounded-wait test (knc_set_wait_test): poll limit of the fused
+    // stage's grid barriers (0: the default) and a barrier that cannot complete
+    int32_t wait_polls = 0;
+    int32_t wait_unreachable = 0;
     // bookkeeping
     int64_t launches = 0;
     int64_t zone_updates = 0;   // zones x RK steps advanced since creation
@@ -1123,7 +1127,10 @@ int run_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, doub
         f.nremap = lay.nremap;
         f.remap = lay.d_remap;
         f.max_nq = lay.max_nq;
-        f.bar_base = c->bar_epoch;
+        // the wait test: a poll limit of its own, and a first barrier that
+        // counts one arrival more than the grid makes (it cannot complete)
+        f.spin_limit = c->wait_polls > 0 ? c->wait_polls : BARRIER_SPIN_LIMIT;
+        f.bar_base = c->bar_epoch + (c->wait_unreachable ? 1u : 0u);
         const int grid = fused_grid(c);
         c->bar_epoch += (unsigned long long)grid * (lay.nremap ? 2u : 1u);
         ProfScope ps(c, KNC_KERNEL_FUSED);
@@ -2753,6 +2760,13 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
 int knc_set_batched(knc_ctx* c, int32_t graph) {
     if (!c) return KNC_ERR_INVALID_ARGUMENT;
     c->batched = graph ? 1 : 0;
+    return KNC_OK;
+}
+
+int knc_set_wait_test(knc_ctx* c, int32_t polls, int32_t unreachable) {
+    if (!c || polls < 0) return KNC_ERR_INVALID_ARGUMENT;
+    c->wait_polls = polls;
+    c->wait_unreachable = unreachable ? 1 : 0;
     return KNC_OK;
 }
 

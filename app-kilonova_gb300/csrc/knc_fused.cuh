@@ -33,9 +33,7 @@
 
 namespace knc {
 
-constexpr int BARRIER_SPIN_LIMIT = 1 << 22;   // polls of >= 64 ns: a bound of about 0.3 s or more
-
-__device__ __forceinline__ void grid_barrier(DevStatus* st, unsigned long long target) {
+__device__ __forceinline__ void grid_barrier(DevStatus* st, unsigned long long target, int limit) {
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -43,7 +41,7 @@ __device__ __forceinline__ void grid_barrier(DevStatus* st, unsigned long long t
         if (*(volatile int32_t*)&st->bar_abort == 0) {
             int n = 0;
             while (*(volatile unsigned long long*)&st->bar_count < target) {
-                if (++n > BARRIER_SPIN_LIMIT) {
+                if (++n > limit) {
                     atomicExch(&st->bar_abort, 1);
                     break;
                 }
@@ -129,7 +127,7 @@ __device__ __forceinline__ void stage_fused_body(const StageArgs& a, const Ghost
         for (int o = 16; o > 0; o >>= 1) dtz = fmin(dtz, __shfl_down_sync(0xffffffffu, dtz, o));
         if ((threadIdx.x & 31) == 0) atomicMin(&a.status->dt_bits, (unsigned long long)__double_as_longlong(dtz));
     }
-    grid_barrier(a.status, f.bar_base + gridDim.x);
+    grid_barrier(a.status, f.bar_base + gridDim.x, f.spin_limit);
 
     // ---- B: remaps
     if (f.nremap > 0) {
@@ -141,7 +139,7 @@ __device__ __forceinline__ void stage_fused_body(const StageArgs& a, const Ghost
                 remap_zone<R, typename C2P::RemapRec>(a, f.remap[item], k - item * per);
             }
         }
-        grid_barrier(a.status, f.bar_base + 2ull * gridDim.x);
+        grid_barrier(a.status, f.bar_base + 2ull * gridDim.x, f.spin_limit);
     }
 
     // ---- C: update tiles (skipped after any failure, like the separate kernel)

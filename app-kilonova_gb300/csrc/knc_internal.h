@@ -176,13 +176,15 @@ struct GhostArgs {
 // Fused-stage extras: recovery chunks {slot, z0, nz, 0} of at most
 // update_threads(utr) consecutive zones of one block, the remap items, and the
 // barrier base of this launch.
+constexpr int BARRIER_SPIN_LIMIT = 1 << 22;   // grid-barrier polls of >= 64 ns: about 0.3 s or more
+
 struct FusedArgs {
     const int4* chunks;
     int32_t nchunks;
     int32_t nremap;
     const int4* remap;
     int32_t max_nq;
-    int32_t pad_;
+    int32_t spin_limit;     // polls a grid barrier waits before it gives up
     unsigned long long bar_base;
 };
 

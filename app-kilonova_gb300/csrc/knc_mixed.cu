@@ -594,6 +594,18 @@ __global__ void __launch_bounds__(update_threads<TR>(), 1) update_tma_kernel(Sta
     }
 }
 
+// The bounded mbarrier wait of update_tma_kernel on a barrier that nothing
+// arrives on and no copy targets: it must give up after `polls` polls.
+__global__ void copy_wait_selftest_kernel(int32_t polls, int32_t* timed_out) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *timed_out = mbar_wait_bounded(&bar, 0u, polls) ? 0 : 1;
+}
+
 template <int TR>
 static void update_tma(const StageArgs& a, cudaStream_t s) {
     const int grid = std::min(a.nutiles, resident_grid(update_tma_kernel<TR>, update_threads<TR>(), TmaSmem<TR>::bytes));
@@ -766,3 +778,17 @@ cudaError_t configure_kernels() {
 }
 
 }  // namespace knc
+
+extern "C" int knc_selftest_copy_wait(int32_t polls, int32_t* timed_out) {
+    if (polls < 1 || !timed_out) return KNC_ERR_INVALID_ARGUMENT;
+    int32_t* d = nullptr;
+    if (cudaMalloc(&d, sizeof(int32_t)) != cudaSuccess) return KNC_ERR_OUT_OF_MEMORY;
+    cudaError_t e = cudaMemset(d, 0xff, sizeof(int32_t));
+    if (e == cudaSuccess) {
+        knc::copy_wait_selftest_kernel<<<1, 32>>>(polls, d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(timed_out, d, sizeof(int32_t), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? KNC_OK : KNC_ERR_CUDA;
+}

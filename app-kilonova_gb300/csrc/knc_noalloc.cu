@@ -20,7 +20,6 @@
 // time) race on it: serialise them.
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 #include <vector>
 
 #include "knc_internal.h"
@@ -65,10 +64,6 @@ __global__ void recover_noalloc_kernel(const double* __restrict__ cons, const do
 
 namespace {
 
-constexpr int MAX_DEVICES = 64;
-std::mutex g_setup_mutex;
-double* g_scratch_ptr[MAX_DEVICES] = {nullptr};
-
 void fill_error(knc_error* err, int kind, const char* msg) {
     if (!err) return;
     std::memset(err, 0, sizeof(*err));
@@ -108,29 +103,26 @@ extern "C" int knc_recover_primitives_noalloc(const knc_hydro_params* hydro, con
     }
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
 
-    // Set-up, once per device, with that device current: the scratch array's
-    // name is only a host-side stand-in, so resolve its device address.
+    // The scratch array's name is only a host-side stand-in: resolve its
+    // device address on the current device at every call (cheap once the
+    // module is loaded), so that no address outlives a device reset.
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) {
+    if (cudaGetDevice(&dev) != cudaSuccess) {
         fill_error(err, KNC_HYDRO_NONE, "knc_recover_primitives_noalloc: no current CUDA device");
         return KNC_ERR_CUDA;
     }
     double* scratch = nullptr;
     {
-        std::lock_guard<std::mutex> lock(g_setup_mutex);
-        if (!g_scratch_ptr[dev]) {
-            void* p = nullptr;
-            const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-            if (e != cudaSuccess || !p) {
-                char msg[256];
-                std::snprintf(msg, sizeof(msg), "knc_recover_primitives_noalloc: cudaGetSymbolAddress: %s",
-                              cudaGetErrorString(e));
-                fill_error(err, KNC_HYDRO_NONE, msg);
-                return KNC_ERR_CUDA;
-            }
-            g_scratch_ptr[dev] = static_cast<double*>(p);
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            char msg[256];
+            std::snprintf(msg, sizeof(msg), "knc_recover_primitives_noalloc: cudaGetSymbolAddress: %s",
+                          cudaGetErrorString(e));
+            fill_error(err, KNC_HYDRO_NONE, msg);
+            return KNC_ERR_CUDA;
         }
-        scratch = g_scratch_ptr[dev];
+        scratch = static_cast<double*>(p);
     }
 
     // Cell volumes of the block (src/mesh.rs:119-123, 246-264) into the scratch.

@@ -190,6 +190,8 @@ SIGNATURES = {
     "knc_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
     "knc_autotune": (C.c_int, [_P, C.c_int32, C.POINTER(Tuning), _DP]),
     "knc_set_mixed_w_split": (C.c_int, [_P, C.c_double]),
+    "knc_set_wait_test": (C.c_int, [_P, C.c_int32, C.c_int32]),
+    "knc_selftest_copy_wait": (C.c_int, [C.c_int32, C.POINTER(C.c_int32)]),
     "knc_synchronize": (C.c_int, [_P]),
     "knc_c2p_stats": (C.c_int, [_P, _I64P, _I64P, _I64P, _I64P]),
     "knc_reset_c2p_stats": (C.c_int, [_P]),

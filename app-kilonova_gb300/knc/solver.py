@@ -139,6 +139,12 @@ class Solver:
     def set_mixed_w_split(self, w: float):
         self._check(self.lib.knc_set_mixed_w_split(self.h, float(w)), "set_mixed_w_split")
 
+    def set_wait_test(self, polls: int = 0, unreachable: bool = False):
+        """Bounded-wait test: the fused stage's grid barriers give up after
+        `polls` polls (0: the default); `unreachable` makes the first barrier
+        of each fused stage wait for one arrival more than the grid makes."""
+        self._check(self.lib.knc_set_wait_test(self.h, int(polls), int(bool(unreachable))), "set_wait_test")
+
     # ---- state
     def init_from_model(self, time: float = 0.0):
         self._check(self.lib.knc_init_from_model(self.h, float(time)), "init_from_model")

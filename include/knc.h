@@ -302,9 +302,25 @@ int knc_get_tuning(const knc_ctx* ctx, knc_tuning* tuning);
  * NULL). */
 int knc_autotune(knc_ctx* ctx, int32_t reps, knc_tuning* best, double* ms_per_stage);
 
-/* Mixed precision: zones whose Lorentz factor estimate exceeds this recover
- * primitives in FP64 (default 2.0); below it recovery runs in FP32. */
+/* Mixed precision: the Lorentz-factor split (default 2.0). Zones whose
+ * Lorentz factor estimate exceeds it recover primitives in FP64 (below it
+ * recovery runs in FP32), and every face whose 4-zone stencil holds a zone
+ * above it is solved in FP64, with the zones it bounds updated in FP64. */
 int knc_set_mixed_w_split(knc_ctx* ctx, double w_split);
+
+/* Bounded waits, tested without a GPU fault. No counterpart in the
+ * reference (its errors are values, src/traits.rs:78-82; this keeps the
+ * library's device waits in that contract). knc_set_wait_test: the fused
+ * stage's grid barriers give up after `polls` polls (0: the default, about
+ * 0.3 s); with `unreachable` the first barrier of each fused stage counts one
+ * arrival more than the grid makes, so it cannot complete and the stage fails
+ * with KNC_ERR_TIMEOUT before any state is written. The context stays usable:
+ * reload the state (knc_set_state) and advance. knc_selftest_copy_wait: one
+ * CTA waits on an mbarrier that nothing arrives on, with the poll loop of the
+ * tensor-copy update (no copy is issued); *timed_out = 1 when the wait gave
+ * up after `polls` polls. */
+int knc_set_wait_test(knc_ctx* ctx, int32_t polls, int32_t unreachable);
+int knc_selftest_copy_wait(int32_t polls, int32_t* timed_out);
 
 /* Wait for all work of the context; returns the first deferred error. */
 int knc_synchronize(knc_ctx* ctx);
@@ -426,11 +442,11 @@ void knc_mlp_features(const double u[4], float out[3]);
  * array inside the library (KNC_NOALLOC_MAX_ZONES cell volumes plus a status
  * word, 1 MiB; every GPU that loads the library holds it until the process
  * exits). Blocks larger than KNC_NOALLOC_MAX_ZONES zones are rejected with
- * KNC_ERR_INVALID_ARGUMENT. The first call on a device resolves that array's
- * address; make it before any stream capture. Calls share the array, so
- * calls whose GPU work overlaps race on it: serialise them. Returns after
- * synchronising `stream`; a failing zone gives KNC_ERR_HYDRO with `err`
- * (optional) filled like knc_last_error. */
+ * KNC_ERR_INVALID_ARGUMENT. Each call resolves that array's address on the
+ * current device. Calls share the array, so calls whose GPU work overlaps
+ * race on it: serialise them. Returns after synchronising `stream` and
+ * reading the array's status word back to the host; a failing zone gives
+ * KNC_ERR_HYDRO with `err` (optional) filled like knc_last_error. */
 #define KNC_NOALLOC_MAX_ZONES 131072
 int knc_recover_primitives_noalloc(const knc_hydro_params* hydro, const knc_mesh_params* mesh,
                                    int32_t block_index, const double* d_cons,

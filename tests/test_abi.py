@@ -24,11 +24,6 @@ def test_header_declares_entry_points():
 def test_library_exports_every_declared_symbol():
     import ctypes
     from knc import abi
-    try:
-        import __graft_entry__ as g  # noqa: F401
-        sys_build = True
-    except Exception:
-        sys_build = False
     if not abi.LIB_PATH.exists():
         import build as b
         b.build()
@@ -37,7 +32,6 @@ def test_library_exports_every_declared_symbol():
     assert not missing, missing
     # the Python binding declares a signature for each of them
     assert set(header_functions()) <= set(abi.SIGNATURES), set(header_functions()) - set(abi.SIGNATURES)
-    assert sys_build or True
 
 
 def test_no_cpu_fallback_without_library(tmp_path):
