@@ -14,7 +14,8 @@ Reported (one JSON line from rank 0):
   l1_density   L1 error of the comoving density of the mixed path against the
                FP64 path after the workload's 200 steps (the FP64 path equals
                the CPU oracle to 1e-12, so this is the error against the FP64
-               oracle); l1_density_after_run: after this run's steps
+               oracle); l1_density_twice_the_steps: after 400;
+               l1_density_after_run: after this run's steps
   errors_vs_fp64  relative L1 and Linf per conserved field, same comparison
   roofline     the dominant kernel of the headline path: algorithmic bytes per
                launch / its average CUDA-event duration, against measured HBM
@@ -24,10 +25,10 @@ Reported (one JSON line from rank 0):
                downloads by chunks of blocks, beside the stages)
   batched_uneven  96 uneven blocks (nr 32..512, nq 64..256), RK3, both
                excision surfaces at 0.5c: mixed + learned + graph vs FP64
-  learned_jet  the W = 100 jet on 2048 x 512: plain Newton from the
-               reference's guess vs the learned guess, in the mixed path and
-               in the FP64 path (iterations per zone, throughput, density L1
-               against the FP64 path)
+  learned_jet  the W = 100 jet on 2048 x 512 for its configured 200 steps:
+               plain Newton from the reference's guess vs the learned guess,
+               in the mixed path and in the FP64 path (iterations per zone,
+               throughput, density L1 against the FP64 path)
   next_rows    the Newtonian sphere on the same grid (FP64, HLLC, adaptive
                dt found inside the fold vs a separate time-step pass),
                primitive export and CBOR checkpoint rates of the wind state
@@ -463,22 +464,25 @@ def run_knc(args):
     l1_run = l1_density(head, fp64)   # after this run's warm-up + timed steps
     # the accuracy gate at the workload's own step count (200 RK2 steps),
     # whatever --steps this run timed: a fresh pair of solvers
-    if args.steps + args.warmup == ACCURACY_STEPS:
-        acc_m, acc_64 = head, fp64
-    else:
-        acc_m, acc_64 = make(True, True, True), make(False, False, True)
-        acc_m.set_tuning(**tuning)
+    # (and again after twice as many steps, how the error grows)
+    acc_m, acc_64 = make(True, True, True), make(False, False, True)
+    acc_m.set_tuning(**tuning)
+
+    def advance_both(n):
         for s_ in (acc_m, acc_64):
-            for _ in range(ACCURACY_STEPS // args.fold):
+            for _ in range(n // args.fold):
                 s_.advance(args.fold)
-            if ACCURACY_STEPS % args.fold:
-                s_.advance(ACCURACY_STEPS % args.fold)
+            if n % args.fold:
+                s_.advance(n % args.fold)
+
+    advance_both(ACCURACY_STEPS)
     l1 = l1_density(acc_m, acc_64)
     errs = field_errors(acc_m, acc_64)
     acc_steps = ACCURACY_STEPS
-    if acc_m is not head:
-        acc_m.close()
-        acc_64.close()
+    advance_both(ACCURACY_STEPS)
+    l1_twice = l1_density(acc_m, acc_64)
+    acc_m.close()
+    acc_64.close()
 
     # ---- same path without the graph, kernels timed with events (roofline)
     prof = make(True, True, False)
@@ -549,20 +553,24 @@ def run_knc(args):
     jet = None
     if not args.no_jet:
         wj = workloads.jet(seed=1 + rank)
+        # the jet's configured step count in all (warm-up steps included), so
+        # the density L1 is the accuracy gate at that count
+        jet_steps = args.jet_steps if args.jet_steps else wj.steps - args.warmup
         j64 = make(False, False, False, workload=wj)
-        timed(j64, args.jet_steps, args.fold)
+        timed(j64, jet_steps, args.fold)
         jet = {"workload": f"{wj.name}: relativistic jet, W = 100, theta_j = 0.1, p/rho = 1e-3, through r = 1 "
                            "into a seeded r^-2 ambient, 2048x512 zones in 32 blocks of 64x512, RK2",
-               "zones": wj.zones, "steps": args.jet_steps}
+               "zones": wj.zones, "steps": jet_steps, "accuracy_steps": jet_steps + args.warmup,
+               "mixed_faces": f"FP64 where the stencil reaches a zone above W = {args.w_split}, else FP32"}
         for name, guess, mixed in (("plain_newton", False, True), ("learned_guess", True, True),
                                    ("fp64_plain_newton", False, False), ("fp64_learned_guess", True, False)):
             sj = make(mixed, guess, True, workload=wj, tune=True)
             sj.reset_c2p_stats()
-            ms_j, _ = timed(sj, args.jet_steps, args.fold)
+            ms_j, _ = timed(sj, jet_steps, args.fold)
             ms_j = max_over_ranks(pg, ms_j)
             st = sj.c2p_stats()
-            jet[name] = {"value": wj.zones * args.jet_steps * world / (ms_j * 1e-3),
-                         "ms_per_step": ms_j / args.jet_steps,
+            jet[name] = {"value": wj.zones * jet_steps * world / (ms_j * 1e-3),
+                         "ms_per_step": ms_j / jet_steps,
                          "fp64_iters_per_zone": st["iters_fp64"] / max(st["zones"], 1),
                          "fp32_iters_per_zone": st["iters_fp32"] / max(st["zones"], 1),
                          "fallbacks": st["fallbacks"], "l1_density": l1_density(sj, j64),
@@ -608,6 +616,7 @@ def run_knc(args):
             "l1_density": l1,
             "errors_vs_fp64": errs,
             "accuracy_steps": acc_steps,
+            "l1_density_twice_the_steps": l1_twice,
             "l1_density_after_run": l1_run,
             "c2p": {"fp64_iters_per_zone": sth["iters_fp64"] / max(sth["zones"], 1),
                     "fp32_iters_per_zone": sth["iters_fp32"] / max(sth["zones"], 1),
@@ -686,7 +695,7 @@ def main():
     ap.add_argument("--no-jet", action="store_true")
     ap.add_argument("--no-next", action="store_true")
     ap.add_argument("--next-steps", type=int, default=50)
-    ap.add_argument("--jet-steps", type=int, default=100)
+    ap.add_argument("--jet-steps", type=int, default=0, help="0: the jet's configured steps less the warm-up")
     ap.add_argument("--workload", default="wind_large", help="workload of --only runs")
     ap.add_argument("--tile-rows", type=int, default=0, help="launch shape of --only runs (0: default)")
     ap.add_argument("--fused", action="store_true")
