@@ -201,6 +201,7 @@ struct BlockH {
     int64_t nr = 0, nq = 0;
     double* buf[2] = {nullptr, nullptr};
     void* P = nullptr;
+    double* P64 = nullptr;   // mixed stage: FP64 primitives of the zones above the split
     double *ar = nullptr, *aq = nullptr, *dv = nullptr, *rc = nullptr, *rv = nullptr;
     float2 *ar_r = nullptr, *aq_r = nullptr, *dv_r = nullptr;
     float *dv_r32 = nullptr, *rc32 = nullptr;
@@ -211,6 +212,7 @@ void free_block(BlockH& b) {
     cudaFree(b.buf[0]);
     cudaFree(b.buf[1]);
     cudaFree(b.P);
+    cudaFree(b.P64);
     cudaFree(b.ar);
     cudaFree(b.aq);
     cudaFree(b.dv);
@@ -244,6 +246,8 @@ struct Layout {
     int64_t nzones = 0;         // zones of the block set
     int2* d_high = nullptr;     // mixed recovery: zones deferred to the dense FP64 pass
     int64_t high_cap = 0;
+    int2* d_hp = nullptr;       // mixed stage: stored zones above the Lorentz-factor split (drain_hp)
+    int64_t hp_cap = 0;
     TmaMaps* d_tmaps = nullptr; // tensor maps per slot (tiles of `utr` rows), when every block allows them
     int tmaps_cap = 0;
     bool tma_ok = false;
@@ -291,15 +295,13 @@ struct Layout {
     size_t sc_store_cap = 0;
     // edge blocks, whose outer halo rows the ghost launch writes
     void* P_edge[2] = {nullptr, nullptr};
+    double* P64_edge[2] = {nullptr, nullptr};
     int32_t nr_edge[2] = {0, 0}, nq_edge[2] = {0, 0};
     // ghost rows
     int32_t ghost_lo = INT32_MIN, ghost_hi = INT32_MIN;
     double* d_ghost_rc = nullptr;                  // [2 ends][2 rows]
     double* d_ghost_dv[2] = {nullptr, nullptr};    // per end [2][nq]
     int64_t ghost_nq[2] = {0, 0};
-    // mixed stage: the ghost rows in FP64 as well, per end [5][2][nq_edge]
-    double* d_ghost64[2] = {nullptr, nullptr};
-    int32_t ghost64_nq[2] = {0, 0};
     std::vector<double> ghost_rc_h, ghost_dv_h[2];
     // a block activated at the start of the step this layout begins
     int4* d_init_tiles = nullptr;
@@ -313,6 +315,7 @@ void free_layout(Layout& l) {
     cudaFree(l.d_utiles);
     cudaFree(l.d_chunks);
     cudaFree(l.d_high);
+    cudaFree(l.d_hp);
     cudaFree(l.d_strips);
     cudaFree(l.d_sstrips);
     cudaFree(l.d_tmaps);
@@ -320,8 +323,6 @@ void free_layout(Layout& l) {
     cudaFree(l.d_ghost_rc);
     cudaFree(l.d_ghost_dv[0]);
     cudaFree(l.d_ghost_dv[1]);
-    cudaFree(l.d_ghost64[0]);
-    cudaFree(l.d_ghost64[1]);
     cudaFree(l.d_init_tiles);
     cudaFree(l.d_sc_table);
     cudaFree(l.d_sc_tiles);
@@ -520,6 +521,7 @@ int alloc_block(knc_ctx* c, int32_t index, BlockH& b) {
         b.buf[0] = r.buf[0];
         b.buf[1] = r.buf[1];
         b.P = r.P;
+        b.P64 = r.P64;
         b.ar = r.ar;
         b.aq = r.aq;
         b.dv = r.dv;
@@ -535,6 +537,7 @@ int alloc_block(knc_ctx* c, int32_t index, BlockH& b) {
         CK(dalloc(&b.buf[0], 5 * n));
         CK(dalloc(&b.buf[1], 5 * n));
         CK(cudaMalloc(&b.P, 5 * (size_t)((nr + 4) * nq) * sizeof(double)));
+        CK(dalloc(&b.P64, 5 * (size_t)((nr + 4) * nq)));
         CK(dalloc(&b.ar, (size_t)((nr + 1) * nq)));
         CK(dalloc(&b.aq, (size_t)(nr * (nq + 1))));
         CK(dalloc(&b.dv, n));
@@ -660,6 +663,7 @@ int rebuild_table(knc_ctx* c) {
         d.buf[0] = b.buf[0];
         d.buf[1] = b.buf[1];
         d.P = b.P;
+        d.P64 = b.P64;
         d.ar = b.ar;
         d.aq = b.aq;
         d.dv = b.dv;
@@ -803,6 +807,15 @@ int rebuild_table(knc_ctx* c) {
         CK(dalloc(&L(c).d_high, (size_t)zoff));
         L(c).high_cap = zoff;
     }
+    // every zone a P array holds, halo rows included: the most a stage can list
+    int64_t padded = 0;
+    for (const BlockH* b : order) padded += (b->nr + 4) * b->nq;
+    if (padded > L(c).hp_cap) {
+        cudaFree(L(c).d_hp);
+        L(c).d_hp = nullptr;
+        CK(dalloc(&L(c).d_hp, (size_t)padded));
+        L(c).hp_cap = padded;
+    }
     L(c).tma_ok = false;
     if (tma_ok) {
         if (nb > L(c).tmaps_cap) {
@@ -829,12 +842,7 @@ int rebuild_table(knc_ctx* c) {
         L(c).P_edge[end] = e.P;
         L(c).nr_edge[end] = (int32_t)e.nr;
         L(c).nq_edge[end] = (int32_t)e.nq;
-        if (L(c).ghost64_nq[end] != (int32_t)e.nq) {
-            cudaFree(L(c).d_ghost64[end]);
-            L(c).d_ghost64[end] = nullptr;
-            CK(dalloc(&L(c).d_ghost64[end], (size_t)(NFIELD * 2 * e.nq)));
-            L(c).ghost64_nq[end] = (int32_t)e.nq;
-        }
+        L(c).P64_edge[end] = e.P64;
     }
     CK(cudaStreamSynchronize(c->stream));
     L(c).ntiles = (int)tiles.size();
@@ -1070,7 +1078,7 @@ int prepare_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, 
     g.gm = c->hp.gamma_law_index;
     g.single_precision = mixed(c) ? 1 : 0;
     if (mixed(c))
-        for (int end = 0; end < 2; ++end) g.P64[end] = lay.P_edge[end] ? lay.d_ghost64[end] : nullptr;
+        for (int end = 0; end < 2; ++end) g.P64[end] = lay.P_edge[end] ? lay.P64_edge[end] : nullptr;
     g.status = c->d_status;
     if (c->ddt) {
         g.dt_bits = &c->d_status->dt_bits;
@@ -1095,8 +1103,22 @@ int prepare_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, 
     a.dt = dt;
     a.dt_f = (float)dt;
     a.avg_half = w1 == 0.5 && bf == 0.5 ? 1 : 0;
-    a.g64[0] = g.P64[0];
-    a.g64[1] = g.P64[1];
+    if (mixed(c) && L(c).d_hp) {
+        // the list of stored zones above the Lorentz-factor split (written by
+        // this stage's recovery, ghost and remap launches, read by its update)
+        a.hp_list = L(c).d_hp;
+        a.hp_count = &c->d_status->hp_count[stage & 1];
+        a.hp_claim = &c->d_status->hp_claim[stage & 1];
+        a.hp_count_next = &c->d_status->hp_count[(stage + 1) & 1];
+        a.hp_claim_next = &c->d_status->hp_claim[(stage + 1) & 1];
+        a.hp_cap = (unsigned)L(c).hp_cap;
+        g.hp_list = a.hp_list;
+        g.hp_count = a.hp_count;
+        g.hp_cap = a.hp_cap;
+        g.edge_slot[0] = 0;
+        g.edge_slot[1] = (int32_t)L(c).slot_index.size() - 1;
+        g.uu_high_f = a.uu_high_f;
+    }
     if (mixed(c) && !c->fused && c->rform == KNC_RECOVERY_DEFERRED && L(c).d_high) {
         a.high = L(c).d_high;
         a.high_count = &c->d_status->high_count[stage & 1];
@@ -1335,6 +1357,7 @@ int reset_status(knc_ctx* c, bool keep_stats) {
         CK(cudaMemsetAsync(&d->dt_bits, 0xff, sizeof(d->dt_bits), c->stream));
         CK(cudaMemsetAsync(&d->bar_count, 0, sizeof(d->bar_count) + sizeof(d->bar_abort), c->stream));
         CK(cudaMemsetAsync(d->high_count, 0, sizeof(d->high_count), c->stream));
+        CK(cudaMemsetAsync(d->hp_count, 0, sizeof(d->hp_count) + sizeof(d->hp_claim), c->stream));
     } else {
         DevStatus s;
         std::memset(&s, 0, sizeof(s));
@@ -2182,7 +2205,7 @@ int build_chunks(knc_ctx* c, int S) {
     }
     l.sc_up.push_back(l.zone_off[nb]);
     size_t store = 0;
-    for (const Shadow& x : sh) store += (size_t)(30 * S + 20) * tab[x.src].nq;
+    for (const Shadow& x : sh) store += (size_t)(40 * S + 40) * tab[x.src].nq;
     if (store > l.sc_store_cap) {
         cudaFree(l.d_sc_store);
         l.d_sc_store = nullptr;
@@ -2200,7 +2223,8 @@ int build_chunks(knc_ctx* c, int S) {
         d.buf[0] = mem;
         d.buf[1] = mem + 5 * rows * nq;
         d.P = mem + 10 * rows * nq;
-        mem += (5 * rows + 5 * (rows + 4) + 5 * rows) * nq;
+        d.P64 = mem + (15 * rows + 20) * nq;   // the mixed stage's FP64 primitives, like P
+        mem += (5 * rows + 5 * (rows + 4) + 5 * rows + 5 * (rows + 4)) * nq;
         d.ar = src.ar + o * nq;
         d.aq = src.aq + o * (nq + 1);
         d.dv = src.dv + o * nq;
@@ -2392,6 +2416,7 @@ int stream_step(knc_ctx* c, double dt, const double* hc_in, const double* hs_in,
         for (int end = 0; end < 2; ++end) {
             if (ge.P[end]) ge.P[end] = gscratch(s, end);
             if (ge.P64[end]) ge.P64[end] = gscratch64(s, end);
+            ge.hp_list = nullptr;
             ge.row0[end] = 0;
             ge.nr_t[end] = -2;   // row stride nr_t + 4 = 2: the compact [5][2][nq]
         }
@@ -2433,9 +2458,14 @@ int stream_step(knc_ctx* c, double dt, const double* hc_in, const double* hs_in,
             y.strips = lay.d_sc_strips + lay.sc_strip_off[k * S + s];
             y.nstrips = lay.sc_strip_off[k * S + s + 1] - lay.sc_strip_off[k * S + s];
             y.tma = 0;
-            // the FP64 ghost rows of this stage, computed ahead like the FP32 ones
-            for (int end = 0; end < 2; ++end)
-                if (y.g64[end]) y.g64[end] = gscratch64(s, end);
+            // chunks run side by side: no shared list (each strip checks its
+            // own stencil and updates its zones with FP64 faces itself)
+            y.hp_list = nullptr;
+            y.hp_count = nullptr;
+            y.hp_claim = nullptr;
+            y.hp_count_next = nullptr;
+            y.hp_claim_next = nullptr;
+            y.hp_cap = 0;
             y.high = nullptr;
             y.high_count = nullptr;
             y.high_count_next = nullptr;
@@ -2448,6 +2478,12 @@ int stream_step(knc_ctx* c, double dt, const double* hc_in, const double* hs_in,
                 CK(launch_halo_rows(gscratch(s, end), g[s].P[end], g[s].nq[end], g[s].nr_t[end], g[s].row0[end],
                                     mixed(c) ? 4 : 8, st));
                 ++c->launches;
+                if (g[s].P64[end]) {
+                    // mixed: the rows in FP64 too (zone_hp reads those above the split)
+                    CK(launch_halo_rows(gscratch64(s, end), g[s].P64[end], g[s].nq[end], g[s].nr_t[end],
+                                        g[s].row0[end], 8, st));
+                    ++c->launches;
+                }
             }
             CK(mixed(c) ? launch_update_mixed(y, st) : launch_update_f64(y, st));
             ++c->launches;
@@ -2708,6 +2744,8 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
         c->rform = t.recovery_form;
         // a fresh start for the deferred-recovery counters of every candidate
         CK(cudaMemsetAsync(c->d_status->high_count, 0, sizeof(c->d_status->high_count), c->stream));
+        CK(cudaMemsetAsync(c->d_status->hp_count, 0, sizeof(c->d_status->hp_count) + sizeof(c->d_status->hp_claim),
+                           c->stream));
         if ((r = rebuild_table(c))) break;
         if (t.update_form == KNC_UPDATE_TILE_TMA && !L(c).tma_ok) continue;
         // the first stage reads buf[cur] and writes buf[1 - cur]: the state stays

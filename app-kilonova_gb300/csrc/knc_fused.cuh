@@ -143,6 +143,8 @@ __device__ __forceinline__ void stage_fused_body(const StageArgs& a, const Ghost
     }
 
     // ---- C: update tiles (skipped after any failure, like the separate kernel)
+    // (the next stage's producers run in the next launch: clear its list)
+    if constexpr (MIXED) clear_next_hp(a);
     if (threadIdx.x == 0)
         run_update = *(volatile unsigned long long*)&a.status->err_key == NO_ERROR &&
                      *(volatile int32_t*)&a.status->bar_abort == 0;
@@ -152,14 +154,16 @@ __device__ __forceinline__ void stage_fused_body(const StageArgs& a, const Ghost
             // warp strips: every warp of the grid takes strips on its own
             constexpr int WPC = NT / 32;
             const PhysT<R> ph = make_phys<R>(a);
+            const bool any_high = MIXED && stage_has_high(a);
             for (int k = blockIdx.x * WPC + (int)(threadIdx.x >> 5); k < a.nstrips; k += gridDim.x * WPC)
-                strip_dispatch<R, MIXED>(a, a.strips[k], ph);
+                strip_dispatch<R, MIXED>(a, a.strips[k], ph, any_high);
         } else if constexpr (!STRIPS_ONLY) {
             for (int tile = blockIdx.x; tile < a.nutiles; tile += gridDim.x) {
                 update_tile<R, MIXED, TR>(a, a.utiles[tile], smem_raw);
                 __syncthreads();
             }
         }
+        if constexpr (MIXED) drain_hp(a);
     }
     warp_reduce_stats(a.status, st.zones, st.it64, st.it32, st.fbs, st.dtz, false);
 }

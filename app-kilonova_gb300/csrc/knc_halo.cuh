@@ -100,15 +100,81 @@ static __device__ __noinline__ void ghost_zone(const GhostArgs& a, int end, int 
         float* Pd = reinterpret_cast<float*>(a.P[end]);
 #pragma unroll
         for (int c = 0; c < NFIELD; ++c) Pd[c * pn + off] = (float)v[c];
-        if (a.P64[end]) {
-            double* Q = a.P64[end] + (int64_t)row * nq + j;
+        // above the Lorentz-factor split: the FP64 row for zone_hp, and listed
+        if (a.P64[end] && high_zone((float)v[1], (float)v[2], a.uu_high_f)) {
 #pragma unroll
-            for (int c = 0; c < NFIELD; ++c) Q[(int64_t)c * 2 * nq] = v[c];
+            for (int c = 0; c < NFIELD; ++c) a.P64[end][c * pn + off] = v[c];
+            if (a.hp_list) note_high(a.hp_list, a.hp_count, a.hp_cap, a.edge_slot[end], a.row0[end] + row, nq, j);
         }
     } else {
         double* Pd = reinterpret_cast<double*>(a.P[end]);
 #pragma unroll
         for (int c = 0; c < NFIELD; ++c) Pd[c * pn + off] = v[c];
+    }
+}
+
+// ---- FP64 primitives of the mixed stage's zones above the Lorentz-factor split
+// FP64 primitive (rho, u_r, u_theta, p, s) of the volume integrals U over the
+// FP64 volume dv: Newton on the pressure to the reference's residual
+// |f| < 1e-12 (D + tau) from the stored FP32 pressure pf[3] (a start one or
+// two iterations from the root), the reference's iteration from the plain
+// guess as the fallback, the stored FP32 primitive if both fail.
+__device__ __forceinline__ void recover_hp(const double gm, const double (&U)[5], double dv, const float (&pf)[NFIELD],
+                                           double (&v)[NFIELD]) {
+#pragma unroll
+    for (int q = 0; q < NFIELD; ++q) v[q] = (double)pf[q];
+    const double m = U[0], s1 = U[1], s2 = U[2], tau = U[3];
+    if (!(m > 0.0) || !(tau >= 0.0)) return;
+    const double ss = s1 * s1 + s2 * s2;
+    double p = 0.0, w = 1.0;
+    int it = 0;
+    if (newton_fast<double>(m, ss, tau, gm, (double)pf[3] * dv, NEWTON_TOLERANCE * (m + tau), 0.0, NEWTON_ITER_MAX,
+                            p, w, it)) {
+        const double inv_et = 1.0 / (tau + m + p);
+        v[0] = m / w / dv;
+        v[1] = w * s1 * inv_et;
+        v[2] = w * s2 * inv_et;
+        v[3] = p < 0.0 ? PRESSURE_FLOOR * v[0] : p / dv;
+    } else {
+        const double u[4] = {m, s1, s2, tau};
+        double Pd[4];
+        double bad;
+        if (srhd_c2p_newton(gm, u, 0.0, Pd, it, bad) == HYDRO_ROOT_FINDER_FAILED) return;
+        v[0] = Pd[0] / dv;
+        v[1] = Pd[1];
+        v[2] = Pd[2];
+        v[3] = Pd[3] / dv;
+    }
+    v[4] = U[4] / dv / sqrt(1.0 + v[1] * v[1] + v[2] * v[2]);
+}
+
+template <class T>
+__device__ __forceinline__ void store_row_zone(T* P, int nr, int nq, int prow, int j, const T (&v)[NFIELD]) {
+    const int64_t pn = (int64_t)(nr + 4) * nq, off = (int64_t)prow * nq + j;
+#pragma unroll
+    for (int q = 0; q < NFIELD; ++q) P[q * pn + off] = v[q];
+}
+
+// A zone (i, j) of block `slot` just stored with FP32 primitive pf above the
+// split: its FP64 primitive from this stage's state into P64, in every block
+// view store_prim wrote it to (its own rows and the neighbours' halo rows),
+// each listed for the update's FP64 faces.
+__device__ __forceinline__ void hp_store(const StageArgs& a, int slot, const DevBlock& B, int i, int j,
+                                         const float (&pf)[NFIELD]) {
+    const int64_t n = (int64_t)B.nr * B.nq, z = (int64_t)i * B.nq + j;
+    const double* Ub = B.buf[a.sel_in] + z;
+    const double U[5] = {Ub[0], Ub[n], Ub[2 * n], Ub[3 * n], Ub[4 * n]};
+    double v[NFIELD];
+    recover_hp(a.gm, U, B.dv[z], pf, v);
+    store_row_zone(B.P64, B.nr, B.nq, i + 2, j, v);
+    if (a.hp_list) note_high(a.hp_list, a.hp_count, a.hp_cap, slot, i + 2, B.nq, j);
+    if (i < 2 && B.P_in_nbr) {
+        store_row_zone(a.blocks[B.slot_in].P64, B.nr_in_nbr, B.nq, B.nr_in_nbr + 2 + i, j, v);
+        if (a.hp_list) note_high(a.hp_list, a.hp_count, a.hp_cap, B.slot_in, B.nr_in_nbr + 2 + i, B.nq, j);
+    }
+    if (i >= B.nr - 2 && B.P_out_nbr) {
+        store_row_zone(a.blocks[B.slot_out].P64, B.nr_out_nbr, B.nq, i - (B.nr - 2), j, v);
+        if (a.hp_list) note_high(a.hp_list, a.hp_count, a.hp_cap, B.slot_out, i - (B.nr - 2), B.nq, j);
     }
 }
 
@@ -154,17 +220,17 @@ static __device__ __noinline__ void remap_zone(const StageArgs& a, const int4 it
     const int srow = side == 0 ? S.nr - 2 + row : row;          // source interior row
     const int trow = side == 0 ? row : T.nr + 2 + row;          // target padded row
     R v[NFIELD];
+    double U[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, dv = 0.0;   // a merged zone's volume integrals
+    const int64_t soff = (int64_t)(srow + 2) * nq_s + j / (nq_t > nq_s ? nq_t / nq_s : 1);
     if (nq_s < nq_t) {
         const R* Ps = reinterpret_cast<const R*>(S.P);
         const int64_t pn = (int64_t)(S.nr + 4) * nq_s;
-        const int64_t off = (int64_t)(srow + 2) * nq_s + j / (nq_t / nq_s);
 #pragma unroll
-        for (int q = 0; q < NFIELD; ++q) v[q] = Ps[q * pn + off];
+        for (int q = 0; q < NFIELD; ++q) v[q] = Ps[q * pn + soff];
     } else {
         const int Rr = nq_s / nq_t;
         const double* Us = S.buf[a.sel_in];
         const int64_t n = (int64_t)S.nr * nq_s;
-        double U[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, dv = 0.0;
         for (int m = 0; m < Rr; ++m) {
             const int64_t z = (int64_t)srow * nq_s + j * Rr + m;
 #pragma unroll
@@ -180,6 +246,26 @@ static __device__ __noinline__ void remap_zone(const StageArgs& a, const int4 it
     const int64_t ot = (int64_t)trow * nq_t + j;
 #pragma unroll
     for (int q = 0; q < NFIELD; ++q) Pt[q * pt + ot] = v[q];
+    if constexpr (sizeof(R) == 4) {
+        // the mixed stage: a halo zone above the split takes its FP64 primitive
+        // too (the coarser source's, or the merged zone's recovered in FP64)
+        // and is listed in the target's view
+        if (T.P64 && high_zone((float)v[1], (float)v[2], a.uu_high_f)) {
+            double v64[NFIELD];
+            if (nq_s < nq_t) {
+                const int64_t pn = (int64_t)(S.nr + 4) * nq_s;
+#pragma unroll
+                for (int q = 0; q < NFIELD; ++q) v64[q] = S.P64[q * pn + soff];
+            } else {
+                float pf[NFIELD];
+#pragma unroll
+                for (int q = 0; q < NFIELD; ++q) pf[q] = (float)v[q];
+                recover_hp(a.gm, U, dv, pf, v64);
+            }
+            store_row_zone(T.P64, T.nr, nq_t, trow, j, v64);
+            if (a.hp_list) note_high(a.hp_list, a.hp_count, a.hp_cap, it.x, trow, nq_t, j);
+        }
+    }
 }
 
 // Separate-launch forms: blockIdx.y = end / remap item. Internal linkage, so

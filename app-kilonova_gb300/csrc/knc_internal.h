@@ -8,6 +8,8 @@
 //                                           FP64 path, float in the mixed path);
 //                                           rows 0-1 and nr+2..nr+3 hold the radial
 //                                           halo (neighbour rows or ghost rows)
+//           P64     [5][nr+4][nq] double   mixed path: the same, written only for
+//                                           zones above the Lorentz-factor split
 //   geometry ar [nr+1][nq], aq [nr][nq+1], dv [nr][nq] (FP64, mesh.rs formulas),
 //            rc [nr] centroid radii, rv [nr+1] vertices; per-column tables
 //            qv [nq+1], qc [nq], cot [nq]; FP32 row/column factors for the
@@ -56,6 +58,11 @@ struct DevBlock {
     const float* dv_r32;   // [nr] (r1^3 - r0^3) 2 pi / 3 in FP32, without c
     const float* rc32;     // [nr]
     const float* cot32;    // [nq]
+    // mixed stage: FP64 primitives [5][nr+4][nq] like P, written only for the
+    // zones whose stored FP32 primitive is above the Lorentz-factor split
+    // (own rows by the recovery, halo rows by the neighbours' recovery, the
+    // ghost and the remap launches), read by zone_hp; null in the FP64 stage
+    double* P64;
     void* P_in_nbr;        // inner neighbour's P: my rows 0,1 go to its rows nr'+2, nr'+3
     void* P_out_nbr;       // outer neighbour's P: my rows nr-2, nr-1 go to its rows 0, 1
     int32_t nr, nq;
@@ -90,6 +97,11 @@ struct DevStatus {
     int32_t bar_abort;              // a grid barrier gave up waiting
     int32_t pad2;
     unsigned high_count[2];         // deferred FP64 recoveries, by stage parity
+    // mixed stage, by stage parity: the stored FP32 primitives above the
+    // Lorentz-factor split listed by this stage (FP64 faces around them), and
+    // the work items of that list the update has claimed
+    unsigned hp_count[2];
+    unsigned hp_claim[2];
 };
 
 struct StageArgs {
@@ -128,9 +140,19 @@ struct StageArgs {
     // u_r^2 + u_theta^2 = W^2 - 1 above uu_high_f (W above the split) makes
     // every face whose 4-zone stencil reaches it an FP64 face (zone_hp)
     float uu_high_f;
-    // FP64 ghost rows of the inner / outer mesh end ([5][2][nq], written by the
-    // ghost launch of this stage), or null (the FP32 rows are used instead)
-    const double* g64[2];
+    // mixed stage: every stored FP32 primitive above the Lorentz-factor split,
+    // as {slot, padded row x nq + column} of the block whose P array holds it
+    // (own rows and halo rows alike), appended by the recovery, ghost and
+    // remap launches (hp_count entries); the update claims its zones with
+    // FP64 faces from this list (hp_claim). The update of a stage clears the
+    // next stage's counters. No list (null): every strip checks its own
+    // stencil and updates such zones itself.
+    int2* hp_list;
+    unsigned* hp_count;
+    unsigned* hp_claim;
+    unsigned* hp_count_next;
+    unsigned* hp_claim_next;
+    unsigned hp_cap;
     // mixed stage length unit L = 2^e: its FP32 geometry is in units of L
     // (areas 2^(-2e), volumes 2^(-3e)), so increments scale back by 2^(2e)
     // and recovered densities use volumes in L^3
@@ -162,8 +184,17 @@ struct GhostArgs {
     int32_t stage;
     double gm;
     int32_t single_precision;   // write float P
-    // mixed stage: the same rows in FP64 as well, [5][2][nq] per end, or null
+    // mixed stage: the target's FP64 primitive array (laid out like P[end]),
+    // which takes the rows whose FP32 values are above the split, or null
     double* P64[2];
+    // mixed stage: stored ghost zones above the Lorentz-factor split are
+    // appended to the stage's list (StageArgs::hp_list) as zones of the edge
+    // blocks (slots edge_slot[end], padded rows row0[end] + 0, 1)
+    int2* hp_list;
+    unsigned* hp_count;
+    unsigned hp_cap;
+    int32_t edge_slot[2];
+    float uu_high_f;
     DevStatus* status;
     // adaptive dt found on the device in the fold's first recovery: the stage
     // time is then fold_stage_time(t0, dt, order, step, sub), dt = *dt_bits x cfl

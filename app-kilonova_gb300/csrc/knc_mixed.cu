@@ -7,7 +7,9 @@
 //   FP64  the conserved state and its RK accumulation, time and excision
 //         radius (host), and the cons -> prim recovery of zones whose Lorentz
 //         factor exceeds `w_split` — converged to the reference's residual
-//         |f| < 1e-12 (D + tau).
+//         |f| < 1e-12 (D + tau) — and the faces whose stencil reaches such a
+//         zone, with the update of the zones they bound (zone_hp,
+//         knc_stage.cuh).
 // Zones below `w_split` recover in FP32. Every zone first runs the Newton
 // iteration in FP32; an FP64 recovery then starts from that root and usually
 // needs one or two FP64 iterations instead of the 3-6 the plain guess takes.
@@ -312,6 +314,8 @@ struct MixedC2p {
             const float wz = sqrtf(__fmaf_rn(P[2], P[2], __fmaf_rn(P[1], P[1], 1.0f)));
             const float v[NFIELD] = {P[0], P[1], P[2], P[3], scalf / dV / wz};
             store_prim<float>(B, i, j, v);
+            // above the split: its FP64 primitive for the update's FP64 faces
+            if (high_zone(P[1], P[2], a.uu_high_f)) hp_store(a, slot, B, i, j, v);
             if ((DT < 0 ? a.compute_dt != 0 : DT > 0) && kind == HYDRO_NONE) {
                 // State::time_step (src/state.rs:151-160) on this stage's
                 // primitives: signal speed in FP32, dl and dl / a in FP64
@@ -547,6 +551,7 @@ __global__ void __launch_bounds__(update_threads<TR>(), 1) update_tma_kernel(Sta
     const bool avg = a.sel_base >= 0;
     const uint32_t tx = (uint32_t)(L::P_BYTES + L::U_BYTES * (avg ? 2 : 1));
     const TmaMaps* maps = reinterpret_cast<const TmaMaps*>(a.tmaps);
+    clear_next_hp(a);
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
@@ -592,6 +597,7 @@ __global__ void __launch_bounds__(update_threads<TR>(), 1) update_tma_kernel(Sta
         if (tile + gridDim.x < a.nutiles)
             mbar_wait_bounded(&bar[(k + 1) & 1], (uint32_t)((k + 1) >> 1) & 1u, TMA_WAIT_LIMIT);
     }
+    if (ok) drain_hp(a);
 }
 
 // The bounded mbarrier wait of update_tma_kernel on a barrier that nothing

@@ -581,6 +581,23 @@ __device__ __forceinline__ int newt_c2p(R gm1, const R* U, R* P, R& bad) {
     return HYDRO_NONE;
 }
 
+// The mixed stage's test for a zone above the Lorentz-factor split, on its
+// stored FP32 four-velocity: u_r^2 + u_theta^2 = W^2 - 1 above thr. Every
+// launch that stores primitives and every update form evaluates this one
+// expression, so they agree zone by zone.
+__device__ __forceinline__ bool high_zone(float ur, float uq, float thr) {
+    return __fmaf_rn(ur, ur, __fmul_rn(uq, uq)) > thr;
+}
+
+// Append a stored zone above the split, {slot, padded row x nq + column}, to
+// the stage's list (the capacity is every padded zone of the block set, so it
+// is never exceeded).
+__device__ __forceinline__ void note_high(int2* list, unsigned* count, unsigned cap, int slot, int prow, int nq,
+                                          int j) {
+    const unsigned k = atomicAdd(count, 1u);
+    if (k < cap) list[k] = make_int2(slot, prow * nq + j);
+}
+
 // Max signal speed of a primitive state (time_step, state.rs:151-160).
 template <class R>
 __device__ __forceinline__ R max_signal_speed(const PhysT<R>& ph, const R* P) {

@@ -110,10 +110,6 @@ __device__ __forceinline__ R stage_dt(const StageArgs& a) {
 // every update form) is solved in FP64 from FP64 primitives, and the zones
 // such faces bound are updated in FP64 (zone_hp, after the strip helpers).
 
-__device__ __forceinline__ bool high_zone(float ur, float uq, float thr) {
-    return __fmaf_rn(ur, ur, __fmul_rn(uq, uq)) > thr;
-}
-
 // The FP64 faces of zone (i, j) from the relativistic zones of its plus-shaped
 // stencil: col bit k = zone (i - 2 + k, j), row bit k = zone (i, j - 2 + k),
 // k = 0..4. Result: bit 0 radial face i, bit 1 radial face i + 1, bit 2 polar
@@ -124,6 +120,14 @@ __device__ __forceinline__ unsigned hp_faces(unsigned col, unsigned row) {
 }
 
 static __device__ __noinline__ void zone_hp(const StageArgs& a, const DevBlock& B, int i, int j);
+__device__ __forceinline__ void drain_hp(const StageArgs& a);
+__device__ __forceinline__ void clear_next_hp(const StageArgs& a);
+
+// Whether this stage stored a primitive above the split (a uniform read of
+// the list's length; a stage without a list is taken to have some).
+__device__ __forceinline__ bool stage_has_high(const StageArgs& a) {
+    return a.hp_count == nullptr || *(volatile const unsigned*)a.hp_count != 0u;
+}
 
 template <class R, bool MIXED, int TR_, bool BOX = false>
 __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, unsigned char* smem_raw,
@@ -279,7 +283,7 @@ __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, un
         unsigned hpf = 0u;
         if constexpr (MIXED) {
             // FP64 faces (a relativistic zone in the plus stencil): zone_hp
-            if (i < nr && j < nq) {
+            if (i < nr && j < nq && stage_has_high(a)) {
                 unsigned cm = 0u, rm = 0u;
 #pragma unroll
                 for (int k = 0; k < 5; ++k) {
@@ -289,7 +293,8 @@ __device__ __forceinline__ void update_tile(const StageArgs& a, const int4 t, un
                     rm |= high_zone(zr[0], zr[PR * PQS], a.uu_high_f) ? 1u << k : 0u;
                 }
                 hpf = hp_faces(cm, rm);
-                if (hpf) zone_hp(a, B, i, j);
+                // with a list the zone waits for drain_hp; without, it is updated here
+                if (hpf && !a.hp_list) zone_hp(a, B, i, j);
             }
         }
         if (i < nr && j < nq && !(MIXED && hpf)) {
@@ -372,10 +377,12 @@ __global__ void __launch_bounds__(update_threads<TR>(), MIXED ? (TR == 4 ? 6 : T
     // A failed c2p in this or an earlier stage stops the step: keep the
     // input state untouched so the failure can be reported from it.
     if (*(volatile unsigned long long*)&a.status->err_key != NO_ERROR) return;
+    if constexpr (MIXED) clear_next_hp(a);
     for (int tile = blockIdx.x; tile < a.nutiles; tile += gridDim.x) {
         update_tile<R, MIXED, TR>(a, a.utiles[tile], smem_raw);
         __syncthreads();
     }
+    if constexpr (MIXED) drain_hp(a);
 }
 
 // ---- warp strips ---------------------------------------------------------------
@@ -417,75 +424,23 @@ __device__ __forceinline__ void strip_face(const PhysT<R>& ph, const StageArgs& 
 
 // ---- FP64 faces of the mixed stage at high Lorentz factor (zone_hp) -----------
 // FP64 primitive (rho, u_r, u_theta, p, s) of zone (r, c) of block B,
-// r in [-2, nr + 1] (rows outside the block from the neighbour or the ghost
-// rows), recovered from the FP64 state of this stage with the reference's
-// residual |f| < 1e-12 (D + tau), the stored FP32 pressure as the Newton
-// start. Where no FP64 state is at hand (a neighbour of another polar
-// resolution, ghost rows without an FP64 copy) the stored FP32 primitive is
-// taken as it is.
-static __device__ __noinline__ void prim_hp(const StageArgs& a, const DevBlock& B, int r, int c, double v[NFIELD]) {
-    const int nq = B.nq;
+// r in [-2, nr + 1] (padded rows, halo included): a zone above the split
+// takes the FP64 primitive its producer stored in P64 (the recovery from
+// this stage's state, the ghost rows' model values, a remapped halo zone's);
+// every other zone its stored FP32 primitive. P64 and P are read-only while
+// the update runs, so every update form and every order of the FP64-face
+// zones sees the same values (the middle RK3 stage updates in place).
+__device__ __forceinline__ void prim_hp(const StageArgs& a, const DevBlock& B, int r, int c, double v[NFIELD]) {
     const float* P = reinterpret_cast<const float*>(B.P);
-    const int64_t pn = (int64_t)(B.nr + 4) * nq;
-    const int64_t off = (int64_t)(r + 2) * nq + c;
-    float pf[NFIELD];
+    const int64_t pn = (int64_t)(B.nr + 4) * B.nq;
+    const int64_t off = (int64_t)(r + 2) * B.nq + c;
+    if (high_zone(P[pn + off], P[2 * pn + off], a.uu_high_f)) {
 #pragma unroll
-    for (int q = 0; q < NFIELD; ++q) pf[q] = P[q * pn + off];
-    const DevBlock* S = &B;
-    int rr = r;
-    int ghost = -1;
-    if (r < 0) {
-        if (B.slot_in >= 0) {
-            S = &a.blocks[B.slot_in];
-            rr = S->nr + r;
-        } else {
-            ghost = 0;
-        }
-    } else if (r >= B.nr) {
-        if (B.slot_out >= 0) {
-            S = &a.blocks[B.slot_out];
-            rr = r - B.nr;
-        } else {
-            ghost = 1;
-        }
-    }
-    if (ghost >= 0 && !B.shadow && a.g64[ghost]) {
-        const int row = ghost == 0 ? r + 2 : r - B.nr;
+        for (int q = 0; q < NFIELD; ++q) v[q] = B.P64[q * pn + off];
+    } else {
 #pragma unroll
-        for (int q = 0; q < NFIELD; ++q) v[q] = a.g64[ghost][(int64_t)q * 2 * nq + (int64_t)row * nq + c];
-        return;
+        for (int q = 0; q < NFIELD; ++q) v[q] = (double)P[q * pn + off];
     }
-#pragma unroll
-    for (int q = 0; q < NFIELD; ++q) v[q] = (double)pf[q];
-    if (ghost >= 0 || S->nq != nq) return;
-    const int64_t n = (int64_t)S->nr * nq, z = (int64_t)rr * nq + c;
-    const double* U = S->buf[a.sel_in] + z;
-    const double m = U[0], s1 = U[n], s2 = U[2 * n], tau = U[3 * n], smass = U[4 * n];
-    const double dv = S->dv[z];
-    if (!(m > 0.0) || !(tau >= 0.0)) return;
-    const double ss = s1 * s1 + s2 * s2;
-    const double tol = NEWTON_TOLERANCE * (m + tau);
-    double p = 0.0, w = 1.0;
-    int it = 0;
-    // the FP32 pressure as the start, volume-integrated like the state
-    if (!newton_fast<double>(m, ss, tau, a.gm, (double)pf[3] * dv, tol, 0.0, NEWTON_ITER_MAX, p, w, it)) {
-        const double u[4] = {m, s1, s2, tau};
-        double Pd[4];
-        double bad;
-        if (srhd_c2p_newton(a.gm, u, 0.0, Pd, it, bad) == HYDRO_ROOT_FINDER_FAILED) return;
-        v[0] = Pd[0] / dv;
-        v[1] = Pd[1];
-        v[2] = Pd[2];
-        v[3] = Pd[3] / dv;
-        v[4] = smass / dv / sqrt(1.0 + Pd[1] * Pd[1] + Pd[2] * Pd[2]);
-        return;
-    }
-    const double inv_et = 1.0 / (tau + m + p);
-    v[0] = m / w / dv;
-    v[1] = w * s1 * inv_et;
-    v[2] = w * s2 * inv_et;
-    v[3] = p < 0.0 ? PRESSURE_FLOOR * v[0] : p / dv;
-    v[4] = smass / dv / sqrt(1.0 + v[1] * v[1] + v[2] * v[2]);
 }
 
 // One face from its stencil s[0..3] (the face between s[1] and s[2]) with the
@@ -606,8 +561,76 @@ static __device__ __noinline__ void zone_hp(const StageArgs& a, const DevBlock& 
     for (int q = 0; q < NFIELD; ++q) Uout[q * n + z] = res[q];
 }
 
+// ---- the zones with FP64 faces, from the stage's list of zones above the split
+// Work item c of listed zone h = (slot, padded row, column): the candidate
+// zone at offset c of h's plus-shaped neighbourhood (c < 5: rows -2..2 of
+// h's column; c >= 5: columns -2, -1, 1, 2 of h's row). A candidate inside
+// its block is updated by zone_hp if h is the first zone above the split in
+// the candidate's own plus stencil (column zones top to bottom, then row
+// zones left to right): every zone with FP64 faces has exactly one such
+// first zone, and every stored zone above the split is listed, so each is
+// updated once.
+__device__ __forceinline__ void hp_candidate(const StageArgs& a, unsigned item, unsigned c) {
+    const int2 e = a.hp_list[item];
+    const DevBlock& B = a.blocks[e.x];
+    const int nq = B.nq, nr = B.nr;
+    const int ih = e.y / nq - 2, jh = e.y - (e.y / nq) * nq;
+    const int d = (int)c < 5 ? (int)c - 2 : ((int)c < 7 ? (int)c - 7 : (int)c - 6);
+    const int ic = (int)c < 5 ? ih + d : ih;
+    const int jc = (int)c < 5 ? jh : jh + d;
+    if (ic < 0 || ic >= nr || jc < 0 || jc >= nq) return;
+    const float* Pu = reinterpret_cast<const float*>(B.P) + (int64_t)(nr + 4) * nq;   // u_r; u_theta one field on
+    const int64_t pn = (int64_t)(nr + 4) * nq;
+    auto high = [&](int i, int j) {
+        if (j < 0 || j >= nq) return false;
+        const int64_t off = (int64_t)(i + 2) * nq + j;
+        return high_zone(Pu[off], Pu[pn + off], a.uu_high_f);
+    };
+    int fi = 0, fj = -1;
+    for (int k = 0; k < 5 && fj < 0; ++k)
+        if (high(ic - 2 + k, jc)) {
+            fi = ic - 2 + k;
+            fj = jc;
+        }
+    for (int k = 0; k < 5 && fj < 0; ++k)
+        if (k != 2 && high(ic, jc - 2 + k)) {
+            fi = ic;
+            fj = jc - 2 + k;
+        }
+    if (fi == ih && fj == jh) zone_hp(a, B, ic, jc);
+}
+
+// The update's second part: whole warps claim 32 work items at a time until
+// the list's 9 items per listed zone are done. The list is complete before
+// the update starts (the recovery, ghost and remap launches wrote it), and
+// the zones it updates are the ones every update form left untouched.
+__device__ __forceinline__ void drain_hp(const StageArgs& a) {
+    if (!a.hp_list) return;
+    const unsigned count = min(*(volatile const unsigned*)a.hp_count, a.hp_cap);
+    if (count == 0u) return;
+    const unsigned total = 9u * count;
+    const unsigned lane = threadIdx.x & 31u;
+    for (;;) {
+        unsigned base = 0u;
+        if (lane == 0u) base = atomicAdd(a.hp_claim, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= total) break;
+        const unsigned w = base + lane;
+        if (w < total) hp_candidate(a, w / 9u, w % 9u);
+    }
+}
+
+// The next stage's list starts empty: cleared by the update of this stage
+// (the previous stage's update, its last reader, finished before this one).
+__device__ __forceinline__ void clear_next_hp(const StageArgs& a) {
+    if (a.hp_count_next && blockIdx.x == 0 && threadIdx.x == 0) {
+        *a.hp_count_next = 0u;
+        *a.hp_claim_next = 0u;
+    }
+}
+
 // HP (mixed stage only): the strip reaches a zone above the Lorentz-factor
-// split; zones with FP64 faces are left to zone_hp after the row loop.
+// split; zones with FP64 faces are left untouched by the row loop.
 template <class R, bool MIXED, bool HP = false>
 __device__ __forceinline__ void update_strip(const StageArgs& a, const int4 it, const PhysT<R>& ph) {
     const unsigned full = 0xffffffffu;
@@ -768,10 +791,11 @@ __device__ __forceinline__ void update_strip(const StageArgs& a, const int4 it, 
             P2[q] = Pn[q];
         }
     }
-    // the zones with FP64 faces, once the row window is dead: the strip's rows
-    // again, with the same relativistic-zone test (four-velocity rows only)
+    // a stage without a list: the zones with FP64 faces, once the row window
+    // is dead (the strip's rows again, with the same relativistic-zone test
+    // on the four-velocity rows); with a list, drain_hp updates them
     if constexpr (HP) {
-        if (hp) {
+        if (hp && !a.hp_list) {
             const float* Pu = reinterpret_cast<const float*>(B.P) + pn;   // u_r; u_theta one field further
             auto high_row = [&](int zrow) -> unsigned {
                 const int prow = zrow + 2;
@@ -820,9 +844,9 @@ static __device__ __noinline__ void update_strip_hp(const StageArgs& a, const in
 // One warp strip of a stage: the mixed stage checks first whether the strip
 // reaches a zone above the Lorentz-factor split.
 template <class R, bool MIXED>
-__device__ __forceinline__ void strip_dispatch(const StageArgs& a, const int4 it, const PhysT<R>& ph) {
+__device__ __forceinline__ void strip_dispatch(const StageArgs& a, const int4 it, const PhysT<R>& ph, bool any_high) {
     if constexpr (MIXED) {
-        if (strip_reaches_high(a, it)) {
+        if (any_high && strip_reaches_high(a, it)) {
             update_strip_hp(a, it);
             return;
         }
@@ -842,7 +866,11 @@ __global__ void __launch_bounds__(STRIP_WARPS * 32, MB) update_strip_kernel(Stag
     if (*(volatile unsigned long long*)&a.status->err_key != NO_ERROR) return;
     const PhysT<R> ph = make_phys<R>(a);
     const int warp = blockIdx.x * STRIP_WARPS + (threadIdx.x >> 5);
-    for (int k = warp; k < a.nstrips; k += gridDim.x * STRIP_WARPS) strip_dispatch<R, MIXED>(a, a.strips[k], ph);
+    const bool any_high = MIXED && stage_has_high(a);
+    if constexpr (MIXED) clear_next_hp(a);
+    for (int k = warp; k < a.nstrips; k += gridDim.x * STRIP_WARPS)
+        strip_dispatch<R, MIXED>(a, a.strips[k], ph, any_high);
+    if constexpr (MIXED) drain_hp(a);
 }
 
 // Block-wide reduction helpers (warp shuffles, then one atomic per warp).

@@ -217,3 +217,15 @@ def test_failure_reported_like_the_copies(pinned, field, value, kind, row):
     g.init_from_model(0.0)
     g.advance(1)
     del keep
+
+
+@pytest.mark.parametrize("order", ["RK2", "RK3"])
+def test_streamed_jet_matches_copies(order):
+    """The W = 100 jet in the mixed stage: its FP64 faces (zones above the
+    Lorentz-factor split, the jet's ghost rows among them) give the same bits
+    through the host-state chunks as through the device state."""
+    import knc
+    from knc import workloads
+    w = workloads.jet_small()
+    w.hydro.runge_kutta_order = order
+    _check(w, knc.abi.KNC_PRECISION_MIXED, 2, dict(tile_rows=16, strip=True, deferred=True))

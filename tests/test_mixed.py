@@ -187,16 +187,18 @@ def test_wind_hllc_against_the_oracle():
         assert linf[q] <= 1e-5, (q, linf)
 
 
-@pytest.mark.parametrize("riemann", ["HLLE", "HLLC"])
-def test_jet_update_forms_agree(riemann):
+@pytest.mark.parametrize("riemann,order", [("HLLE", "RK2"), ("HLLC", "RK2"), ("HLLE", "RK3")])
+def test_jet_update_forms_agree(riemann, order):
     """Tiles, tensor-copy tiles, warp strips (with the deferred recovery) and
     the fused stage give the same bits on the jet, whose zones above the
-    Lorentz-factor split bring in the FP64 faces, with HLLE and HLLC."""
+    Lorentz-factor split bring in the FP64 faces, with HLLE and HLLC, and
+    with RK3, whose middle stage updates the state in place."""
     import knc
     from helpers import zone_relative_errors
     from knc import workloads
     w = workloads.jet_small()
     w.hydro.riemann_solver = riemann
+    w.hydro.runge_kutta_order = order
     states = []
     for t in (dict(tile_rows=8), dict(tile_rows=8, tma=True), dict(tile_rows=16, strip=True, deferred=True),
               dict(tile_rows=8, fused=True), dict(tile_rows=16, strip=True, fused=True)):
