@@ -143,8 +143,6 @@ __device__ __forceinline__ void stage_fused_body(const StageArgs& a, const Ghost
     }
 
     // ---- C: update tiles (skipped after any failure, like the separate kernel)
-    // (the next stage's producers run in the next launch: clear its list)
-    if constexpr (MIXED) clear_next_hp(a);
     if (threadIdx.x == 0)
         run_update = *(volatile unsigned long long*)&a.status->err_key == NO_ERROR &&
                      *(volatile int32_t*)&a.status->bar_abort == 0;
@@ -153,17 +151,18 @@ __device__ __forceinline__ void stage_fused_body(const StageArgs& a, const Ghost
         if (STRIPS_ONLY || a.strips) {
             // warp strips: every warp of the grid takes strips on its own
             constexpr int WPC = NT / 32;
-            const PhysT<R> ph = make_phys<R>(a);
-            const bool any_high = MIXED && stage_has_high(a);
-            for (int k = blockIdx.x * WPC + (int)(threadIdx.x >> 5); k < a.nstrips; k += gridDim.x * WPC)
-                strip_dispatch<R, MIXED>(a, a.strips[k], ph, any_high);
+            stage_strips<R, MIXED>(a, blockIdx.x * WPC + (int)(threadIdx.x >> 5), gridDim.x * WPC);
         } else if constexpr (!STRIPS_ONLY) {
+            // (the next stage's producers run in the next launch: clear its list)
+            if constexpr (MIXED) clear_next_hp(a);
             for (int tile = blockIdx.x; tile < a.nutiles; tile += gridDim.x) {
                 update_tile<R, MIXED, TR>(a, a.utiles[tile], smem_raw);
                 __syncthreads();
             }
         }
-        if constexpr (MIXED) drain_hp(a);
+        if constexpr (MIXED) {
+            if (!(STRIPS_ONLY || a.strips)) drain_hp(a);   // (the strips' form drains its own list)
+        }
     }
     warp_reduce_stats(a.status, st.zones, st.it64, st.it32, st.fbs, st.dtz, false);
 }

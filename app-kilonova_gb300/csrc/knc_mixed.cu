@@ -261,6 +261,15 @@ struct MixedC2p {
         if (valid && !(DEFER && high))
             ok32 = newton_fast<float>(1.0f, ssn, taun, gmf, guess, 2e-7f * taun, 1e-6f, 16, p32, w32, it32);
         bool fp64 = valid && (high || !ok32);
+        if (DEFER && valid && !fp64 && w32 * w32 > 0.99f * (a.uu_high_f + 1.0f)) {
+            // a zone whose stored FP32 four-velocity would be above the split
+            // (the estimate from |S| / (D + tau) missed it) goes to the dense
+            // pass too, which keeps its FP64 primitive for the update's FP64
+            // faces: this kernel stores no zone above the split. (Below 0.99 of
+            // the split's W^2 the converged W cannot give such a velocity.)
+            const float inv_et = 1.0f / (taun + 1.0f + p32);
+            fp64 = high_zone(w32 * s1n * inv_et, w32 * s2n * inv_et, a.uu_high_f);
+        }
         if (DEFER) {
             const unsigned full = 0xffffffffu;
             const unsigned mask = __ballot_sync(full, fp64);
@@ -315,7 +324,11 @@ struct MixedC2p {
             const float v[NFIELD] = {P[0], P[1], P[2], P[3], scalf / dV / wz};
             store_prim<float>(B, i, j, v);
             // above the split: its FP64 primitive for the update's FP64 faces
-            if (high_zone(P[1], P[2], a.uu_high_f)) hp_store(a, slot, B, i, j, v);
+            // (the deferring form stores no such zone: it defers every zone
+            // above the split, and its list holds every zone of the layout)
+            if constexpr (!DEFER) {
+                if (high_zone(P[1], P[2], a.uu_high_f)) hp_store(a, slot, B, i, j, v);
+            }
             if ((DT < 0 ? a.compute_dt != 0 : DT > 0) && kind == HYDRO_NONE) {
                 // State::time_step (src/state.rs:151-160) on this stage's
                 // primitives: signal speed in FP32, dl and dl / a in FP64

@@ -841,36 +841,47 @@ static __device__ __noinline__ void update_strip_hp(const StageArgs& a, const in
     update_strip<float, true, true>(a, it, make_phys<float>(a));
 }
 
-// One warp strip of a stage: the mixed stage checks first whether the strip
-// reaches a zone above the Lorentz-factor split.
+// The mixed stage's strips when the stage listed zones above the split:
+// each strip checks whether it reaches one (then the out-of-line form leaves
+// its zones with FP64 faces untouched), then the list's zones are updated.
+// Out of line, so that the common strip loop keeps its own registers.
+// first / step: this thread's warp's first strip and the warps of the grid.
+static __device__ __noinline__ void update_strips_hp(const StageArgs& a, int first, int step) {
+    const PhysT<float> ph = make_phys<float>(a);
+    for (int k = first; k < a.nstrips; k += step) {
+        const int4 it = a.strips[k];
+        if (strip_reaches_high(a, it)) update_strip_hp(a, it);
+        else update_strip<float, true>(a, it, ph);
+    }
+    drain_hp(a);
+}
+
+// The strips of a stage, warps first .. in steps of `step`: the mixed stage
+// takes the form above when its list holds a zone.
 template <class R, bool MIXED>
-__device__ __forceinline__ void strip_dispatch(const StageArgs& a, const int4 it, const PhysT<R>& ph, bool any_high) {
+__device__ __forceinline__ void stage_strips(const StageArgs& a, int first, int step) {
     if constexpr (MIXED) {
-        if (any_high && strip_reaches_high(a, it)) {
-            update_strip_hp(a, it);
+        clear_next_hp(a);
+        if (stage_has_high(a)) {
+            update_strips_hp(a, first, step);
             return;
         }
     }
-    update_strip<R, MIXED>(a, it, ph);
+    const PhysT<R> ph = make_phys<R>(a);
+    for (int k = first; k < a.nstrips; k += step) update_strip<R, MIXED>(a, a.strips[k], ph);
 }
 
 // Strips (a.strips) in a grid-stride loop over warps; MB = resident CTAs per
 // SM the register allocation is sized for (a tuning choice: more warps
 // against fewer registers).
 template <class R, bool MIXED, int MB>
-__global__ void __launch_bounds__(STRIP_WARPS * 32, MB) update_strip_kernel(StageArgs a) {
+__global__ void __launch_bounds__(STRIP_WARPS * 32, MB) update_strip_kernel(const __grid_constant__ StageArgs a) {
     // launched chained to the recovery (programmatic dependent launch): wait
     // for it to complete, let the next stage's recovery be scheduled
     asm volatile("griddepcontrol.wait;" ::: "memory");
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (*(volatile unsigned long long*)&a.status->err_key != NO_ERROR) return;
-    const PhysT<R> ph = make_phys<R>(a);
-    const int warp = blockIdx.x * STRIP_WARPS + (threadIdx.x >> 5);
-    const bool any_high = MIXED && stage_has_high(a);
-    if constexpr (MIXED) clear_next_hp(a);
-    for (int k = warp; k < a.nstrips; k += gridDim.x * STRIP_WARPS)
-        strip_dispatch<R, MIXED>(a, a.strips[k], ph, any_high);
-    if constexpr (MIXED) drain_hp(a);
+    stage_strips<R, MIXED>(a, blockIdx.x * STRIP_WARPS + (threadIdx.x >> 5), gridDim.x * STRIP_WARPS);
 }
 
 // Block-wide reduction helpers (warp shuffles, then one atomic per warp).
