@@ -244,10 +244,6 @@ struct Layout {
     int utr = 0;
     int uform = -1;
     int64_t nzones = 0;         // zones of the block set
-    int2* d_high = nullptr;     // mixed recovery: zones deferred to the dense FP64 pass
-    int64_t high_cap = 0;
-    int2* d_hp = nullptr;       // mixed stage: stored zones above the Lorentz-factor split (drain_hp)
-    int64_t hp_cap = 0;
     TmaMaps* d_tmaps = nullptr; // tensor maps per slot (tiles of `utr` rows), when every block allows them
     int tmaps_cap = 0;
     bool tma_ok = false;
@@ -314,8 +310,6 @@ void free_layout(Layout& l) {
     cudaFree(l.d_tiles);
     cudaFree(l.d_utiles);
     cudaFree(l.d_chunks);
-    cudaFree(l.d_high);
-    cudaFree(l.d_hp);
     cudaFree(l.d_strips);
     cudaFree(l.d_sstrips);
     cudaFree(l.d_tmaps);
@@ -397,6 +391,11 @@ struct knc_ctx {
     int ddt_step = 0;      // step of the fold being issued
     double w_split = 2.0;
     float* d_mlp = nullptr;
+    // stage lists shared by every layout (rebuild_table grows them)
+    int2* d_high = nullptr;     // mixed recovery: zones deferred to the dense FP64 pass
+    int64_t high_cap = 0;
+    int2* d_hp = nullptr;       // mixed stage: stored zones above the Lorentz-factor split (drain_hp)
+    int64_t hp_cap = 0;
     // the bounded-wait test (knc_set_wait_test): poll limit of the fused
     // stage's grid barriers (0: the default) and a barrier that cannot complete
     int32_t wait_polls = 0;
@@ -801,20 +800,26 @@ int rebuild_table(knc_ctx* c) {
     L(c).nstrips = (int)strips.size();
     L(c).uform = c->uform;
     L(c).nzones = zoff;
-    if (zoff > L(c).high_cap) {
-        cudaFree(L(c).d_high);
-        L(c).d_high = nullptr;
-        CK(dalloc(&L(c).d_high, (size_t)zoff));
-        L(c).high_cap = zoff;
+    // The stage lists are used one stage at a time, so every layout shares
+    // them; they grow here, while a fold is planned (before its capture), and
+    // never shrink. The deferred recovery lists at most every zone; the list
+    // of zones above the split at most every zone a P array holds (halo rows
+    // included).
+    if (zoff > c->high_cap) {
+        cudaFree(c->d_high);
+        c->d_high = nullptr;
+        c->high_cap = 0;
+        CK(dalloc(&c->d_high, (size_t)zoff));
+        c->high_cap = zoff;
     }
-    // every zone a P array holds, halo rows included: the most a stage can list
     int64_t padded = 0;
     for (const BlockH* b : order) padded += (b->nr + 4) * b->nq;
-    if (padded > L(c).hp_cap) {
-        cudaFree(L(c).d_hp);
-        L(c).d_hp = nullptr;
-        CK(dalloc(&L(c).d_hp, (size_t)padded));
-        L(c).hp_cap = padded;
+    if (padded > c->hp_cap) {
+        cudaFree(c->d_hp);
+        c->d_hp = nullptr;
+        c->hp_cap = 0;
+        CK(dalloc(&c->d_hp, (size_t)padded));
+        c->hp_cap = padded;
     }
     L(c).tma_ok = false;
     if (tma_ok) {
@@ -1103,15 +1108,15 @@ int prepare_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, 
     a.dt = dt;
     a.dt_f = (float)dt;
     a.avg_half = w1 == 0.5 && bf == 0.5 ? 1 : 0;
-    if (mixed(c) && L(c).d_hp) {
+    if (mixed(c) && c->d_hp) {
         // the list of stored zones above the Lorentz-factor split (written by
         // this stage's recovery, ghost and remap launches, read by its update)
-        a.hp_list = L(c).d_hp;
+        a.hp_list = c->d_hp;
         a.hp_count = &c->d_status->hp_count[stage & 1];
         a.hp_claim = &c->d_status->hp_claim[stage & 1];
         a.hp_count_next = &c->d_status->hp_count[(stage + 1) & 1];
         a.hp_claim_next = &c->d_status->hp_claim[(stage + 1) & 1];
-        a.hp_cap = (unsigned)L(c).hp_cap;
+        a.hp_cap = (unsigned)c->hp_cap;
         g.hp_list = a.hp_list;
         g.hp_count = a.hp_count;
         g.hp_cap = a.hp_cap;
@@ -1119,11 +1124,11 @@ int prepare_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, 
         g.edge_slot[1] = (int32_t)L(c).slot_index.size() - 1;
         g.uu_high_f = a.uu_high_f;
     }
-    if (mixed(c) && !c->fused && c->rform == KNC_RECOVERY_DEFERRED && L(c).d_high) {
-        a.high = L(c).d_high;
+    if (mixed(c) && !c->fused && c->rform == KNC_RECOVERY_DEFERRED && c->d_high) {
+        a.high = c->d_high;
         a.high_count = &c->d_status->high_count[stage & 1];
         a.high_count_next = &c->d_status->high_count[(stage + 1) & 1];
-        a.high_cap = (unsigned)L(c).high_cap;
+        a.high_cap = (unsigned)c->high_cap;
     }
     if (c->ddt) {
         a.dt_bits = &c->d_status->dt_bits;
@@ -1619,6 +1624,8 @@ void knc_destroy(knc_ctx* c) {
     cudaFree(c->d_host_prim);
     cudaFree(c->d_status);
     cudaFree(c->d_mlp);
+    cudaFree(c->d_high);
+    cudaFree(c->d_hp);
     cudaFree(c->d_stage);
     if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
     for (cudaEvent_t e : c->marks)
