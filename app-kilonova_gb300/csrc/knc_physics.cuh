@@ -491,9 +491,13 @@ __device__ __forceinline__ R lorentz_factor(const PhysT<R>& ph, const R* P) {
     return rsqrt_(R(1) + P[1] * P[1] + P[2] * P[2]);
 }
 
-// SRHD cons -> prim in the reference's Newton form (FP64, plain path):
-// Newton-Raphson on p, |f| < 1e-12 (D + tau), at most 50 iterations.
-// Returns HYDRO_* and the iteration count.
+// SRHD cons -> prim, FP64 (the plain path; the oracle runs the same
+// expressions in the same order): Newton-Raphson on p (Marti & Mueller 2003
+// section 6), |f| < 1e-12 (D + tau), at most 50 iterations, each with three
+// divisions and a square root: with 1 - v^2 = 1/W^2, rho e = X / W^2 for
+// X = tau + m (1 - W) + p (1 - W^2), rho h = m / W + rho e + p and
+// f / f' = f rho h / (v^2 gamma p - rho h). Returns HYDRO_* and the
+// iteration count.
 __device__ __forceinline__ int srhd_c2p_newton(double gm, const double* U, double guess, double* P,
                                                int& iterations, double& bad) {
     const double m = U[0];
@@ -508,16 +512,15 @@ __device__ __forceinline__ int srhd_c2p_newton(double gm, const double* U, doubl
     bool found = false;
     for (int n = 0; n < NEWTON_ITER_MAX; ++n) {
         const double et = tau + p + m;
-        const double b2 = fmin(ss / et / et, 1.0 - 1e-10);
-        const double w2 = 1.0 / (1.0 - b2);
+        const double inv = 1.0 / et;
+        const double b2 = fmin(ss * inv * inv, 1.0 - 1e-10);
+        const double omb = 1.0 - b2;
+        const double w2 = 1.0 / omb;
         const double w = sqrt(w2);
-        const double e = (tau + m * (1.0 - w) + p * (1.0 - w2)) / (m * w);
-        const double d = m / w;
-        const double h = 1.0 + e + p / d;
-        const double a2 = gm * p / (d * h);
-        const double f = d * e * (gm - 1.0) - p;
-        const double g = b2 * a2 - 1.0;
-        p -= f / g;
+        const double de = (tau + m * (1.0 - w) + p * (1.0 - w2)) * omb;
+        const double dh = m * omb * w + de + p;
+        const double f = de * (gm - 1.0) - p;
+        p -= f * dh / (b2 * gm * p - dh);
         iterations = n + 1;
         if (fabs(f) < tol) { w0 = w; found = true; break; }
     }

@@ -136,6 +136,11 @@ inline double lorentz_factor(const Phys& ph, const Prim& P) {
 // SRHD cons -> prim: Newton-Raphson on the pressure (Marti & Mueller 2003 §6),
 // f(p) = rho e (gamma-1) - p with rho, e, W recovered at the trial p; df/dp
 // approximated by v^2 c_s^2 - 1. Converged when |f| < 1e-12 (D + tau).
+// Each step takes three divisions and a square root: with 1 - v^2 = 1/W^2,
+// rho e = X / W^2 for X = tau + m (1 - W) + p (1 - W^2), rho h = m / W +
+// rho e + p and f / f' = f rho h (v^2 gamma p - rho h)^-1 (the same iteration
+// as the textbook form's seven divisions, rounded differently; which form the
+// reference's un-vendored crate uses is not known).
 // Plain guess p = 0 (the only guess the conserved state alone provides).
 // Returns KNC_HYDRO_NONE, NEGATIVE_PRESSURE (floored), or an error kind.
 int srhd_c2p(const Phys& ph, const Cons& U, double guess, Prim& P, int& iterations,
@@ -153,16 +158,15 @@ int srhd_c2p(const Phys& ph, const Cons& U, double guess, Prim& P, int& iteratio
     bool found = false;
     for (int n = 0; n < NEWTON_ITER_MAX; ++n) {
         const double et = tau + p + m;
-        const double b2 = std::min(ss / et / et, 1.0 - 1e-10);
-        const double w2 = 1.0 / (1.0 - b2);
+        const double inv = 1.0 / et;
+        const double b2 = std::min(ss * inv * inv, 1.0 - 1e-10);
+        const double omb = 1.0 - b2;
+        const double w2 = 1.0 / omb;
         const double w = std::sqrt(w2);
-        const double e = (tau + m * (1.0 - w) + p * (1.0 - w2)) / (m * w);
-        const double d = m / w;
-        const double h = 1.0 + e + p / d;
-        const double a2 = gm * p / (d * h);
-        const double f = d * e * (gm - 1.0) - p;
-        const double g = b2 * a2 - 1.0;
-        p -= f / g;
+        const double de = (tau + m * (1.0 - w) + p * (1.0 - w2)) * omb;
+        const double dh = m * omb * w + de + p;
+        const double f = de * (gm - 1.0) - p;
+        p -= f * dh / (b2 * gm * p - dh);
         iterations = n + 1;
         if (std::fabs(f) < tol) { w0 = w; found = true; break; }
     }
