@@ -233,15 +233,27 @@ def run_reference(args):
 PROFILE_OF = {"update": "update_strip_mixed_wind_4096x1024.md", "c2p": "c2p_mixed_wind_4096x1024.md"}
 
 
-def profiled_traffic(kernel: str):
-    """DRAM bytes (read + write) of one launch from the committed ncu summary."""
-    f = ROOT / "profiles" / PROFILE_OF.get(kernel, "")
+def profile_value(name: str, key: str):
+    """A `key = value` line of a committed ncu summary under profiles/."""
+    f = ROOT / "profiles" / name
     if not f.is_file():
         return None
     for line in f.read_text().splitlines():
-        if line.startswith("traffic_bytes_per_launch"):
-            return int(line.split("=")[1])
+        if line.startswith(key + " ") or line.startswith(key + "="):
+            return float(line.split("=")[1])
     return None
+
+
+def profiled_traffic(kernel: str, key: str = "traffic_bytes_per_launch"):
+    """DRAM bytes (read + write) of one launch from the committed ncu summary."""
+    v = profile_value(PROFILE_OF.get(kernel, ""), key)
+    return int(v) if v is not None else None
+
+
+# FP64 operations per launch of the plain FP64 stage's kernels on this
+# workload (DADD + DMUL + 2 DFMA, counted by ncu; data-dependent through the
+# Newton iterations, stable for the workload)
+FP64_PROFILE = "fp64_kernels_wind_4096x1024.md"
 
 
 def l1_density(a, b) -> float:
@@ -449,6 +461,23 @@ def run_knc(args):
     ms64 = max_over_ranks(pg, ms64)
     v64 = zones * args.steps * world / (ms64 * 1e-3)
     fp64_peak = knc.measure_fp64_peak()
+    # the FP64 kernels timed one after another (CUDA events), against the
+    # FP64 FMA rate measured above: this path's own roofline
+    p64 = make(False, False, False)
+    p64.set_tuning(**fp64.tuning())
+    p64.advance(2)
+    p64.set_profiling(True)
+    p64.advance(4)
+    kt64 = p64.kernel_times()
+    p64.close()
+    fp64_roof = {}
+    for kind, key in (("c2p", "flops_per_launch_c2p"), ("update", "flops_per_launch_update")):
+        flops = profile_value(FP64_PROFILE, key)
+        ms_k = kt64[kind][0] / max(kt64[kind][1], 1)
+        if flops and ms_k > 0:
+            fp64_roof[kind] = {"ms_per_launch": ms_k, "flops_per_launch": flops,
+                               "achieved_gflops": flops / (ms_k * 1e-3) / 1e9,
+                               "frac_of_fp64_peak": flops / (ms_k * 1e-3) / 1e9 / fp64_peak}
 
     # ---- headline: mixed + learned + graph
     clocks = ClockSampler(local)
@@ -501,6 +530,16 @@ def run_knc(args):
     alg_bytes = per_zone * zones
     achieved = alg_bytes / (dom_ms * 1e-3) / 1e9
     traffic = profiled_traffic(dom) if (dom != "update" or tuning.get("strip")) else None
+    # per stage, against that stage's algorithmic bytes (the update launch:
+    # stage 1 reads U and writes U1, 80 B per zone; stage 2 reads U1 and U0
+    # and writes the average, 120 B)
+    per_stage = None
+    if dom == "update" and tuning.get("strip"):
+        per_stage = {}
+        for k, alg in ((1, 80.0), (2, 120.0)):
+            t = profiled_traffic("update", f"traffic_bytes_stage{k}")
+            if t:
+                per_stage[f"stage{k}"] = {"alg_bytes": alg * zones, "traffic": t, "ratio": t / (alg * zones)}
 
     # ---- end to end through the C ABI with host buffers
     nb = w.num_blocks
@@ -611,7 +650,7 @@ def run_knc(args):
                        "parallelism": f"replicas x{world}", "tuning": tuning},
             "fp64": {"value": v64, "ms_per_step": ms64 / args.steps, "tuning": fp64.tuning(),
                      "newton_iters_per_zone": st64["iters_fp64"] / max(st64["zones"], 1),
-                     "fp64_peak_gflops": fp64_peak},
+                     "fp64_peak_gflops": fp64_peak, "fp64_roofline": fp64_roof},
             "speedup_vs_fp64": value / v64,
             "l1_density": l1,
             "errors_vs_fp64": errs,
@@ -624,6 +663,8 @@ def run_knc(args):
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                          "peak_source": peak_src, "avg_launch_ms": dom_ms,
+                         "traffic_ratio": traffic / alg_bytes if traffic else None,
+                         "traffic_per_stage": per_stage,
                          "kernel_ms": {k: v[0] / max(v[1], 1) for k, v in kt.items()},
                          "alg_bytes_per_zone_launch": per_zone,
                          "step": {"alg_bytes_per_zone_update": ALG_BYTES_PER_ZONE_UPDATE,
