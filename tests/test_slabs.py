@@ -1,6 +1,7 @@
 """Radial-slab decomposition (knc.slabs): ranks advance overlapping slabs with
-the minimum time step over the slabs and exchange owned blocks once per fold;
-every owned block must equal the single-domain run bit for bit.
+the minimum time step over the slabs and exchange their edge blocks with
+their neighbours once per fold; every owned block must equal the
+single-domain run bit for bit, and each rank sends only its overlap blocks.
 
 The CPU tests run the oracle as each rank's engine on gloo ranks
 (world_size 2); the GPU test runs two library contexts on one GPU in one
@@ -54,24 +55,21 @@ def _rank(rank, world, port, name, folds, q):
         dist.all_reduce(t, op=dist.ReduceOp.MIN)
         return float(t.item())
 
-    def allgather(obj):
-        out = [None] * world
-        dist.all_gather_object(out, obj)
-        return out
-
+    exchange = slabs.torch_neighbour_exchange(dist, rank, world)
     for f in folds:
-        slabs.advance_slabs([dom], f, allreduce_min, allgather)
-    q.put((rank, {i: (c.copy(), s.copy()) for i, (c, s) in dom.owned_blocks().items()}, eng.time()))
+        slabs.advance_slabs([dom], f, allreduce_min, exchange)
+    q.put((rank, {i: (c.copy(), s.copy()) for i, (c, s) in dom.owned_blocks().items()}, eng.time(),
+           dom.bytes_sent, len(dom.to_below()) * (rank > 0) + len(dom.to_above()) * (rank < world - 1)))
     dist.destroy_process_group()
 
 
-@pytest.mark.parametrize("name", ["wind", "sphere"])
-def test_two_cpu_ranks_match_single_domain(name):
+@pytest.mark.parametrize("name,world", [("wind", 2), ("sphere", 2), ("wind", 3)])
+def test_cpu_ranks_match_single_domain(name, world):
     folds = [6, 5]
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_rank, args=(r, 2, port, name, folds, q)) for r in range(2)]
+    procs = [ctx.Process(target=_rank, args=(r, world, port, name, folds, q)) for r in range(world)]
     for p in procs:
         p.start()
     out = [q.get(timeout=300) for _ in procs]
@@ -81,9 +79,12 @@ def test_two_cpu_ranks_match_single_domain(name):
     for f in folds:
         ref.advance(f)
     merged = {}
-    for _, blocks, t in out:
+    block_bytes = ref.nr * ref.nq * 5 * 8
+    for _, blocks, t, sent, edge_blocks in out:
         merged.update(blocks)
         assert t == ref.time()
+        # each fold a rank sends its edge blocks to its neighbours, nothing else
+        assert sent == len(folds) * edge_blocks * block_bytes
     assert sorted(merged) == ref.block_indexes()
     assert max(zone_relative_errors(merged, ref.state())) == 0.0
 
