@@ -6,11 +6,12 @@
 // by the solver's prim -> cons over a range of Lorentz factors and
 // temperatures (knc_generate_pairs).
 //
-// Training: each step draws a batch, runs the forward pass with the same
-// tensor-core layer as inference (bf16 weights and activations, FP32
-// accumulation), back-propagates in FP32 (straight-through for the bf16
-// rounding of weights and activations) into per-warp private gradient tiles in
-// shared memory, reduces them per CTA, and applies Adam.
+// Training: each step draws a batch and evaluates the loss gradient with one
+// launch of mlp_train_tc_kernel: the forward pass rounds weights and
+// activations to bf16 as inference does, and the back-propagation is FP32
+// (straight-through for those roundings), with its three dense contractions on
+// the fifth-generation tensor cores (tcgen05.mma, accumulators in tensor
+// memory). Adam then updates the FP32 master weights.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -21,189 +22,340 @@
 #include "knc_internal.h"
 #include "knc_mlp.cuh"
 #include "knc_physics.cuh"
+#include "knc_tc.cuh"
+#include "knc_tma.cuh"
 
 namespace knc {
 
-constexpr int TRAIN_WARPS = 4;
-constexpr int ZLD = 65;   // padded float rows of the per-warp z / dz tiles
+// ---- training kernel: one CTA of 128 threads per SM, a tile of 128 batch
+// rows at a time, thread t owning row t. The three 128 x 64 x K contractions
+// run on the tensor cores (tcgen05.mma, bf16 operands in shared memory, FP32
+// accumulators in tensor memory):
+//   Z2  = A1 . W2^T                    (K = 64 hidden units)
+//   dA1 = dZ2 . W2                     (K = 64)
+//   dW2 += [dZ2_hi; dZ2_lo]^T . A1     (K = 128 rows, accumulated over tiles)
+// A1 = bf16(silu(z1)) and W2 are bf16 already (the forward pass uses them so);
+// dZ2 is FP32 and enters as the sum of two bf16 parts, hi = bf16(dZ2) and
+// lo = bf16(dZ2 - hi), which carries 16 of its 24 significand bits. The
+// per-unit sums (b1, W1, b2, W3, b3) are warp-shuffle reductions in FP32.
+constexpr int TC_ROWS = 128;                       // batch rows per tile = MMA M
+constexpr int TC_THREADS = 128;
+constexpr uint32_t TC_TMEM_COLS = 256;             // Z2 at 0, dA1 at 64, dW2 at 128
+constexpr uint32_t TC_KLBO = 128, TC_KSBO = 1024;  // [rows][64] tiles: 8 K-chunks of 128 B per 8-row group
+constexpr uint32_t TC_TLBO = 144, TC_TSBO = 16 * 144;   // [n][128 rows] tiles: K-chunks 144 B apart
+constexpr uint32_t TC_IDESC = tc_idesc_bf16(128, 64);
+constexpr int TC_WAIT_POLLS = 1 << 22;
 
-struct TrainWarp {
-    __nv_bfloat16 act[MLP_ACT_ELEMS];   // a1 = bf16(silu(z1)) rows
-    float z[32 * ZLD];                  // z2, then dz2
-    float dz1[32 * ZLD];
-    float xn[32 * 3];
-    float dout[32];
-    float dw2[MLP_H * ZLD];             // private dW2 accumulator [u][v]
+struct TcTrainSmem {
+    unsigned char a1k[TC_ROWS * 64 * 2];      // A1 (M = row, K = unit)
+    unsigned char dzk[2][TC_ROWS * 64 * 2];   // dZ2 hi, lo (M = row, K = unit)
+    unsigned char w2k[64 * 64 * 2];           // W2 (N = output unit u, K = input unit v)
+    unsigned char w2t[64 * 64 * 2];           // W2^T (N = v, K = u)
+    unsigned char a1t[8 * TC_TSBO];           // A1^T (N = v, K = row)
+    unsigned char dzt[16 * TC_TSBO];          // [dZ2 hi; dZ2 lo]^T (M = 128: u, then 64 + u; K = row)
+    float w1[MLP_H * 3], b1[MLP_H], b2[MLP_H], w3[MLP_H];
+    float b3, xm[3], xs[3];
+    uint64_t bar[2];
+    uint32_t tmem_slot;
 };
 
-struct TrainSmem {
-    MlpWeights W;
-    TrainWarp warp[TRAIN_WARPS];
-};
+// Byte offsets in the two operand layouts.
+__device__ __forceinline__ uint32_t kbyte(int row, int k) {
+    return (uint32_t)(row >> 3) * TC_KSBO + (uint32_t)(k >> 3) * TC_KLBO + (uint32_t)(row & 7) * 16u +
+           (uint32_t)(k & 7) * 2u;
+}
+__device__ __forceinline__ uint32_t tbyte(int n, int row) {
+    return (uint32_t)(n >> 3) * TC_TSBO + (uint32_t)(row >> 3) * TC_TLBO + (uint32_t)(n & 7) * 16u +
+           (uint32_t)(row & 7) * 2u;
+}
 
 __device__ __forceinline__ float sigm(float z) { return 1.0f / (1.0f + expf(-z)); }
 
+__device__ __forceinline__ void st_bf16(unsigned char* base, uint32_t off, __nv_bfloat16 v) {
+    *reinterpret_cast<__nv_bfloat16*>(base + off) = v;
+}
+
+// Sum over the warp's 32 rows of 32 per-row values: a butterfly that halves
+// the set at each of 5 exchanges; lane l ends with the sum of column l.
+__device__ __forceinline__ float warp_colsum32(float (&v)[32]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int m = 16, h = 16; m > 0; m >>= 1, h >>= 1) {
+        const bool up = (lane & m) != 0;
+#pragma unroll
+        for (int k = 0; k < h; ++k) {
+            const float send = up ? v[k] : v[k + h];
+            const float keep = up ? v[k + h] : v[k];
+            v[k] = keep + __shfl_xor_sync(0xffffffffu, send, m);
+        }
+    }
+    return v[0];
+}
+
 // One launch = one gradient evaluation over `rows` rows. Row r reads data row
 // (seed ? hash(seed, r) % n_data : r). Gradients (of the mean loss) are added
-// into grad[]; the summed squared error into *loss_sum.
-__global__ void __launch_bounds__(TRAIN_WARPS * 32) mlp_fwd_bwd_kernel(const float* __restrict__ w,
-                                                                      const float* __restrict__ x,
-                                                                      const float* __restrict__ y, int64_t n_data,
-                                                                      int64_t rows, uint64_t seed, float inv_batch,
-                                                                      float* __restrict__ grad,
-                                                                      float* __restrict__ loss_sum,
-                                                                      float* __restrict__ pred) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    TrainSmem& S = *reinterpret_cast<TrainSmem*>(smem_raw);
-    const int lane = threadIdx.x & 31;
-    const int wid = threadIdx.x >> 5;
-    TrainWarp& T = S.warp[wid];
-    mlp_load(S.W, w);
-    for (int k = lane; k < MLP_H * ZLD; k += 32) T.dw2[k] = 0.0f;
+// into grad[]; the summed squared error into *loss_sum. A tensor-core wait
+// that gives up sets *err.
+__global__ void __launch_bounds__(TC_THREADS, 1) mlp_train_tc_kernel(const float* __restrict__ w,
+                                                                    const float* __restrict__ x,
+                                                                    const float* __restrict__ y, int64_t n_data,
+                                                                    int64_t rows, uint64_t seed, float inv_batch,
+                                                                    float* __restrict__ grad,
+                                                                    float* __restrict__ loss_sum,
+                                                                    float* __restrict__ pred, unsigned* err) {
+    extern __shared__ unsigned char smem_raw[];
+    TcTrainSmem& S =
+        *reinterpret_cast<TcTrainSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    for (int k = tid; k < MLP_H * MLP_H; k += TC_THREADS) {
+        const int u = k >> 6, v = k & 63;
+        const __nv_bfloat16 b = __float2bfloat16_rn(w[KNC_MLP_OFF_W2 + k]);
+        st_bf16(S.w2k, kbyte(u, v), b);
+        st_bf16(S.w2t, kbyte(v, u), b);
+    }
+    for (int k = tid; k < MLP_H * 3; k += TC_THREADS) S.w1[k] = bf16r(w[KNC_MLP_OFF_W1 + k]);
+    for (int k = tid; k < MLP_H; k += TC_THREADS) {
+        S.b1[k] = w[KNC_MLP_OFF_B1 + k];
+        S.b2[k] = w[KNC_MLP_OFF_B2 + k];
+        S.w3[k] = bf16r(w[KNC_MLP_OFF_W3 + k]);
+    }
+    if (tid == 0) {
+        S.b3 = w[KNC_MLP_OFF_B3];
+        for (int k = 0; k < 3; ++k) {
+            S.xm[k] = w[KNC_MLP_OFF_XMEAN + k];
+            S.xs[k] = w[KNC_MLP_OFF_XSCALE + k];
+        }
+        mbar_init(&S.bar[0], 1);
+        mbar_init(&S.bar[1], 1);
+        fence_barrier_init();
+    }
+    if (warp == 0) tc_alloc(smem_u32(&S.tmem_slot), TC_TMEM_COLS);
+    fence_proxy_async();
+    tc_fence_before();
     __syncthreads();
-    const MlpWeights& W = S.W;
+    tc_fence_after();
+    const uint32_t tmem = S.tmem_slot;
+    const uint32_t a1k = smem_u32(S.a1k), w2k = smem_u32(S.w2k), w2t = smem_u32(S.w2t);
+    const uint32_t dzk0 = smem_u32(S.dzk[0]), dzk1 = smem_u32(S.dzk[1]);
+    const uint32_t a1t = smem_u32(S.a1t), dzt = smem_u32(S.dzt);
 
-    // register accumulators of the small parameter groups (lane owns units lane, lane+32)
-    float g_w1[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-    float g_b1[2] = {0.f, 0.f}, g_b2[2] = {0.f, 0.f}, g_w3[2] = {0.f, 0.f};
+    // lane sums of columns lane and 32 + lane: W3, b2, b1, W1 (3)
+    float g_w3[2] = {0.f, 0.f}, g_b2[2] = {0.f, 0.f}, g_b1[2] = {0.f, 0.f};
+    float g_w1[3][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     float g_b3 = 0.f, l_sum = 0.f;
+    uint32_t phase = 0;
+    bool any_tile = false, failed = false;
 
-    const int64_t nchunks = (rows + 31) / 32;
-    const int64_t gwarp = (int64_t)blockIdx.x * TRAIN_WARPS + wid;
-    const int64_t nwarps = (int64_t)gridDim.x * TRAIN_WARPS;
-    for (int64_t chunk = gwarp; chunk < nchunks; chunk += nwarps) {
-        const int64_t r = chunk * 32 + lane;
+    const int64_t ntiles = (rows + TC_ROWS - 1) / TC_ROWS;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int64_t r = t * TC_ROWS + tid;
         const bool valid = r < rows;
         int64_t d = r;
         if (seed) d = (int64_t)(splitmix64(seed ^ splitmix64((uint64_t)r)) % (uint64_t)n_data);
-        float xr[3] = {0.f, 0.f, 0.f}, yr = 0.f;
+        float xr0 = 0.f, xr1 = 0.f, xr2 = 0.f, yr = 0.f;
         if (valid) {
-            xr[0] = x[d * 3];
-            xr[1] = x[d * 3 + 1];
-            xr[2] = x[d * 3 + 2];
+            xr0 = x[d * 3];
+            xr1 = x[d * 3 + 1];
+            xr2 = x[d * 3 + 2];
             yr = y[d];
         }
-        // ---- forward
-        mlp_layer1<false>(W, T.act, xr);
-        T.xn[lane * 3 + 0] = (xr[0] - W.xm[0]) * W.xs[0];
-        T.xn[lane * 3 + 1] = (xr[1] - W.xm[1]) * W.xs[1];
-        T.xn[lane * 3 + 2] = (xr[2] - W.xm[2]) * W.xs[2];
-        __syncwarp();
-        float acc[2][8][4];
-        mlp_layer2(W, T.act, acc);
-        {
-            const int g = lane >> 2, t = lane & 3;
+        const float xn0 = (xr0 - S.xm[0]) * S.xs[0];
+        const float xn1 = (xr1 - S.xm[1]) * S.xs[1];
+        const float xn2 = (xr2 - S.xm[2]) * S.xs[2];
+        auto z1_of = [&](int v) {
+            return __fmaf_rn(S.w1[v * 3 + 2], xn2, __fmaf_rn(S.w1[v * 3 + 1], xn1, __fmaf_rn(S.w1[v * 3], xn0, S.b1[v])));
+        };
+        // ---- layer 1: A1 row (K-major) and column (transposed tile)
 #pragma unroll
-            for (int mt = 0; mt < 2; ++mt)
+        for (int c = 0; c < 8; ++c) {
+            uint32_t pk[4];
 #pragma unroll
-                for (int nt = 0; nt < 8; ++nt) {
-                    const int c = nt * 8 + 2 * t;
-                    T.z[(mt * 16 + g) * ZLD + c] = acc[mt][nt][0];
-                    T.z[(mt * 16 + g) * ZLD + c + 1] = acc[mt][nt][1];
-                    T.z[(mt * 16 + g + 8) * ZLD + c] = acc[mt][nt][2];
-                    T.z[(mt * 16 + g + 8) * ZLD + c + 1] = acc[mt][nt][3];
-                }
+            for (int h = 0; h < 4; ++h) {
+                const int v = 8 * c + 2 * h;
+                const float za = z1_of(v), zb = z1_of(v + 1);
+                const __nv_bfloat16 ba = __float2bfloat16_rn(za / (1.0f + expf(-za)));
+                const __nv_bfloat16 bb = __float2bfloat16_rn(zb / (1.0f + expf(-zb)));
+                st_bf16(S.a1t, tbyte(v, tid), ba);
+                st_bf16(S.a1t, tbyte(v + 1, tid), bb);
+                __nv_bfloat162 p2;
+                p2.x = ba;
+                p2.y = bb;
+                pk[h] = *reinterpret_cast<const uint32_t*>(&p2);
+            }
+            *reinterpret_cast<uint4*>(S.a1k + kbyte(tid, 8 * c)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
         }
-        __syncwarp();
-        float out = W.b3;
-        for (int u = 0; u < MLP_H; ++u) {
-            const float z2 = T.z[lane * ZLD + u];
-            out = fmaf(z2 * sigm(z2), W.w3[u], out);
+        fence_proxy_async();
+        tc_fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks)
+                tc_mma_bf16(tmem, tc_desc(a1k + 256u * ks, TC_KLBO, TC_KSBO), tc_desc(w2k + 256u * ks, TC_KLBO, TC_KSBO),
+                            TC_IDESC, ks > 0);
+            tc_commit(smem_u32(&S.bar[0]));
+        }
+        if (__syncthreads_or(!mbar_wait_bounded(&S.bar[0], phase, TC_WAIT_POLLS))) {
+            failed = true;
+            break;
+        }
+        tc_fence_after();
+        // ---- layer 2 and the output
+        float z2[64], s2[64];
+        tc_ld64(tmem, 0, z2);
+        float out = S.b3;
+#pragma unroll
+        for (int u = 0; u < 64; ++u) {
+            z2[u] += S.b2[u];
+            s2[u] = sigm(z2[u]);
+            out = fmaf(z2[u] * s2[u], S.w3[u], out);
         }
         if (pred && valid && !seed) pred[r] = out;
         const float e = valid ? out - yr : 0.f;
         l_sum += e * e;
         const float dout = 2.0f * e * inv_batch;
-        T.dout[lane] = dout;
         g_b3 += dout;
-        __syncwarp();
-        // ---- backward, lane owns hidden units u = lane, lane + 32
+        // W3: dout h2 summed over rows
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int u = lane + 32 * h;
-            const float w3u = W.w3[u];
-            float gw3 = 0.f, gb2 = 0.f;
-            for (int row = 0; row < 32; ++row) {
-                const float z2 = T.z[row * ZLD + u];
-                const float s = sigm(z2);
-                const float dr = T.dout[row];
-                gw3 = fmaf(dr, z2 * s, gw3);
-                const float dz2 = dr * w3u * s * (1.0f + z2 * (1.0f - s));
-                T.z[row * ZLD + u] = dz2;
-                gb2 += dz2;
-            }
-            g_w3[h] += gw3;
-            g_b2[h] += gb2;
+        for (int hh = 0; hh < 2; ++hh) {
+            float q[32];
+#pragma unroll
+            for (int k = 0; k < 32; ++k) q[k] = dout * (z2[32 * hh + k] * s2[32 * hh + k]);
+            g_w3[hh] += warp_colsum32(q);
         }
-        __syncwarp();
+        // dZ2 in place of z2
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int u = lane + 32 * h;
-            for (int v = 0; v < MLP_H; ++v) {
-                float a = 0.f;
-                for (int row = 0; row < 32; ++row)
-                    a = fmaf(T.z[row * ZLD + u], __bfloat162float(T.act[row * MLP_LD + v]), a);
-                T.dw2[u * ZLD + v] += a;
-            }
+        for (int u = 0; u < 64; ++u) {
+            const float s = s2[u];
+            z2[u] = dout * S.w3[u] * s * (1.0f + z2[u] * (1.0f - s));
         }
-        // own row: da1 = dz2 W2, dz1 = da1 silu'(z1)
-        {
-            float z1[MLP_H];
-            const float xn0 = T.xn[lane * 3], xn1 = T.xn[lane * 3 + 1], xn2 = T.xn[lane * 3 + 2];
-            for (int v = 0; v < MLP_H; ++v)
-                z1[v] = __fmaf_rn(W.w1[v * 3 + 2], xn2, __fmaf_rn(W.w1[v * 3 + 1], xn1, __fmaf_rn(W.w1[v * 3], xn0, W.b1[v])));
-            for (int v = 0; v < MLP_H; ++v) {
-                float da = 0.f;
-                for (int u = 0; u < MLP_H; ++u)
-                    da = fmaf(T.z[lane * ZLD + u], __bfloat162float(W.w2[u * MLP_LD + v]), da);
-                const float s = sigm(z1[v]);
-                T.dz1[lane * ZLD + v] = da * s * (1.0f + z1[v] * (1.0f - s));
-            }
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+            float q[32];
+#pragma unroll
+            for (int k = 0; k < 32; ++k) q[k] = z2[32 * hh + k];
+            g_b2[hh] += warp_colsum32(q);
         }
-        __syncwarp();
+        // dZ2 = hi + lo into the row tiles (dA1) and the stacked transposed tile (dW2)
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int v = lane + 32 * h;
-            float gb = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f;
-            for (int row = 0; row < 32; ++row) {
-                const float dz = T.dz1[row * ZLD + v];
-                gb += dz;
-                g0 = fmaf(dz, T.xn[row * 3], g0);
-                g1 = fmaf(dz, T.xn[row * 3 + 1], g1);
-                g2 = fmaf(dz, T.xn[row * 3 + 2], g2);
+        for (int c = 0; c < 8; ++c) {
+            uint32_t ph[4], pl[4];
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                const int u = 8 * c + 2 * h;
+                const __nv_bfloat16 ha = __float2bfloat16_rn(z2[u]), hb = __float2bfloat16_rn(z2[u + 1]);
+                const __nv_bfloat16 la = __float2bfloat16_rn(z2[u] - __bfloat162float(ha));
+                const __nv_bfloat16 lb = __float2bfloat16_rn(z2[u + 1] - __bfloat162float(hb));
+                st_bf16(S.dzt, tbyte(u, tid), ha);
+                st_bf16(S.dzt, tbyte(u + 1, tid), hb);
+                st_bf16(S.dzt, tbyte(64 + u, tid), la);
+                st_bf16(S.dzt, tbyte(64 + u + 1, tid), lb);
+                __nv_bfloat162 p2;
+                p2.x = ha;
+                p2.y = hb;
+                ph[h] = *reinterpret_cast<const uint32_t*>(&p2);
+                p2.x = la;
+                p2.y = lb;
+                pl[h] = *reinterpret_cast<const uint32_t*>(&p2);
             }
-            g_b1[h] += gb;
-            g_w1[h][0] += g0;
-            g_w1[h][1] += g1;
-            g_w1[h][2] += g2;
+            *reinterpret_cast<uint4*>(S.dzk[0] + kbyte(tid, 8 * c)) = make_uint4(ph[0], ph[1], ph[2], ph[3]);
+            *reinterpret_cast<uint4*>(S.dzk[1] + kbyte(tid, 8 * c)) = make_uint4(pl[0], pl[1], pl[2], pl[3]);
         }
-        __syncwarp();
-    }
-    // ---- reduce: warp-private tiles and registers -> global
+        fence_proxy_async();
+        tc_fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        g_b3 += __shfl_xor_sync(0xffffffffu, g_b3, o);
-        l_sum += __shfl_xor_sync(0xffffffffu, l_sum, o);
-    }
-    if (lane == 0) {
-        atomicAdd(&grad[KNC_MLP_OFF_B3], g_b3);
-        atomicAdd(loss_sum, l_sum);
-    }
+            for (int ks = 0; ks < 4; ++ks)
+                tc_mma_bf16(tmem + 64u, tc_desc(dzk0 + 256u * ks, TC_KLBO, TC_KSBO),
+                            tc_desc(w2t + 256u * ks, TC_KLBO, TC_KSBO), TC_IDESC, ks > 0);
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int u = lane + 32 * h;
-        atomicAdd(&grad[KNC_MLP_OFF_B1 + u], g_b1[h]);
-        atomicAdd(&grad[KNC_MLP_OFF_B2 + u], g_b2[h]);
-        atomicAdd(&grad[KNC_MLP_OFF_W3 + u], g_w3[h]);
-        for (int k = 0; k < 3; ++k) atomicAdd(&grad[KNC_MLP_OFF_W1 + u * 3 + k], g_w1[h][k]);
+            for (int ks = 0; ks < 4; ++ks)
+                tc_mma_bf16(tmem + 64u, tc_desc(dzk1 + 256u * ks, TC_KLBO, TC_KSBO),
+                            tc_desc(w2t + 256u * ks, TC_KLBO, TC_KSBO), TC_IDESC, 1u);
+#pragma unroll
+            for (int ks = 0; ks < 8; ++ks)
+                tc_mma_bf16(tmem + 128u, tc_desc(dzt + 2u * TC_TLBO * ks, TC_TLBO, TC_TSBO),
+                            tc_desc(a1t + 2u * TC_TLBO * ks, TC_TLBO, TC_TSBO), TC_IDESC, (any_tile || ks > 0) ? 1u : 0u);
+            tc_commit(smem_u32(&S.bar[1]));
+        }
+        any_tile = true;
+        if (__syncthreads_or(!mbar_wait_bounded(&S.bar[1], phase, TC_WAIT_POLLS))) {
+            failed = true;
+            break;
+        }
+        tc_fence_after();
+        phase ^= 1u;
+        // ---- layer 1 backward: dz1 = dA1 silu'(z1), in place of dA1
+        float da[64];
+        tc_ld64(tmem, 64, da);
+#pragma unroll
+        for (int v = 0; v < 64; ++v) {
+            const float z = z1_of(v);
+            const float s = sigm(z);
+            da[v] = da[v] * s * (1.0f + z * (1.0f - s));
+        }
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+            float q[32];
+#pragma unroll
+            for (int k = 0; k < 32; ++k) q[k] = da[32 * hh + k];
+            g_b1[hh] += warp_colsum32(q);
+#pragma unroll
+            for (int k = 0; k < 32; ++k) q[k] = da[32 * hh + k] * xn0;
+            g_w1[0][hh] += warp_colsum32(q);
+#pragma unroll
+            for (int k = 0; k < 32; ++k) q[k] = da[32 * hh + k] * xn1;
+            g_w1[1][hh] += warp_colsum32(q);
+#pragma unroll
+            for (int k = 0; k < 32; ++k) q[k] = da[32 * hh + k] * xn2;
+            g_w1[2][hh] += warp_colsum32(q);
+        }
+        tc_fence_before();
     }
+    if (failed) {
+        if (tid == 0) atomicExch(err, 1u);
+        // the tensor core's work in flight, if any, gets one more bounded wait
+        mbar_wait_bounded(&S.bar[0], phase, TC_WAIT_POLLS);
+        mbar_wait_bounded(&S.bar[1], phase, TC_WAIT_POLLS);
+    } else if (any_tile) {
+        // ---- dW2: accumulator rows u (hi part) and 64 + u (lo part), summed
+        float acc[64];
+        tc_ld64(tmem, 128, acc);
+        __syncthreads();   // every MMA has completed; the row tiles are free
+        float* red = reinterpret_cast<float*>(S.a1k);   // [128][65] floats over a1k and dzk
+#pragma unroll
+        for (int v = 0; v < 64; ++v) red[tid * 65 + v] = acc[v];
+        __syncthreads();
+        for (int k = tid; k < MLP_H * MLP_H; k += TC_THREADS) {
+            const int u = k >> 6, v = k & 63;
+            atomicAdd(&grad[KNC_MLP_OFF_W2 + k], red[u * 65 + v] + red[(64 + u) * 65 + v]);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            g_b3 += __shfl_xor_sync(0xffffffffu, g_b3, o);
+            l_sum += __shfl_xor_sync(0xffffffffu, l_sum, o);
+        }
+        if (lane == 0) {
+            atomicAdd(&grad[KNC_MLP_OFF_B3], g_b3);
+            atomicAdd(loss_sum, l_sum);
+        }
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+            const int u = 32 * hh + lane;
+            atomicAdd(&grad[KNC_MLP_OFF_W3 + u], g_w3[hh]);
+            atomicAdd(&grad[KNC_MLP_OFF_B2 + u], g_b2[hh]);
+            atomicAdd(&grad[KNC_MLP_OFF_B1 + u], g_b1[hh]);
+            for (int k = 0; k < 3; ++k) atomicAdd(&grad[KNC_MLP_OFF_W1 + u * 3 + k], g_w1[k][hh]);
+        }
+    }
+    tc_fence_before();
     __syncthreads();
-    // sum the warps' dW2 tiles into warp 0's tile, then one atomic per entry
-    for (int k = threadIdx.x; k < MLP_H * MLP_H; k += blockDim.x) {
-        const int u = k / MLP_H, v = k - u * MLP_H;
-        float s = 0.f;
-        for (int q = 0; q < TRAIN_WARPS; ++q) s += S.warp[q].dw2[u * ZLD + v];
-        if (s != 0.f) atomicAdd(&grad[KNC_MLP_OFF_W2 + k], s);
+    if (warp == 0) {
+        tc_fence_after();
+        tc_dealloc(tmem, TC_TMEM_COLS);
     }
 }
 
@@ -305,25 +457,25 @@ cudaError_t launch_sample_pairs(const DevBlock* blocks, const int4* tiles, int n
 
 namespace {
 
-size_t train_smem_bytes() { return sizeof(TrainSmem); }
+size_t train_smem_bytes() { return sizeof(TcTrainSmem) + 1024; }   // + alignment of the operand tiles
 
 cudaError_t configure_train() {
     static bool done = false;
     if (done) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(mlp_fwd_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(mlp_train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)train_smem_bytes());
     if (e == cudaSuccess) done = true;
     return e;
 }
 
+// One CTA per 128-row tile up to one per SM (the kernel's shared memory
+// admits one CTA per SM, so its tensor-memory allocation never waits).
 int grid_for_rows(int64_t rows) {
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t chunks = (rows + 31) / 32;
-    // at least 4 chunks per warp so the per-CTA reduction amortises
-    const int64_t ctas = std::max<int64_t>(1, std::min<int64_t>(sms, (chunks + 4 * TRAIN_WARPS - 1) / (4 * TRAIN_WARPS)));
-    return (int)ctas;
+    const int64_t tiles = (rows + TC_ROWS - 1) / TC_ROWS;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(sms, tiles));
 }
 
 struct DevBuf {
@@ -377,7 +529,9 @@ int knc_mlp_forward_backward(const float* weights, const float* x, const float* 
                              float* loss, float* grad) {
     if (!weights || !x || !y || n <= 0) return KNC_ERR_INVALID_ARGUMENT;
     CKR(configure_train());
-    DevBuf dw, dx, dy, dg, dl, dp;
+    DevBuf dw, dx, dy, dg, dl, dp, de;
+    CKR(cudaMalloc(&de.p, 4));
+    CKR(cudaMemset(de.p, 0, 4));
     CKR(cudaMalloc(&dw.p, KNC_MLP_NUM_PARAMS * 4));
     CKR(cudaMalloc(&dx.p, (size_t)n * 12));
     CKR(cudaMalloc(&dy.p, (size_t)n * 4));
@@ -389,10 +543,13 @@ int knc_mlp_forward_backward(const float* weights, const float* x, const float* 
     CKR(cudaMemcpy(dy.p, y, (size_t)n * 4, cudaMemcpyHostToDevice));
     CKR(cudaMemset(dg.p, 0, KNC_MLP_NUM_PARAMS * 4));
     CKR(cudaMemset(dl.p, 0, 4));
-    mlp_fwd_bwd_kernel<<<grid_for_rows(n), TRAIN_WARPS * 32, train_smem_bytes()>>>(
+    mlp_train_tc_kernel<<<grid_for_rows(n), TC_THREADS, train_smem_bytes()>>>(
         (const float*)dw.p, (const float*)dx.p, (const float*)dy.p, n, n, 0ull, 1.0f / (float)n, (float*)dg.p,
-        (float*)dl.p, (float*)dp.p);
+        (float*)dl.p, (float*)dp.p, (unsigned*)de.p);
     CKR(cudaGetLastError());
+    unsigned err = 0;
+    CKR(cudaMemcpy(&err, de.p, 4, cudaMemcpyDeviceToHost));
+    if (err) return KNC_ERR_TIMEOUT;
     float lsum = 0.f;
     CKR(cudaMemcpy(&lsum, dl.p, 4, cudaMemcpyDeviceToHost));
     if (loss) *loss = lsum / (float)n;
@@ -405,7 +562,9 @@ int knc_mlp_train(const double* pairs, int64_t n, float* weights, const knc_mlp_
                   float* final_loss) {
     if (!pairs || n <= 0 || !weights || !tp || tp->batch <= 0 || tp->steps < 0) return KNC_ERR_INVALID_ARGUMENT;
     CKR(configure_train());
-    DevBuf dpairs, dx, dy, dw, dm, dv, dg, dl;
+    DevBuf dpairs, dx, dy, dw, dm, dv, dg, dl, de;
+    CKR(cudaMalloc(&de.p, 4));
+    CKR(cudaMemset(de.p, 0, 4));
     CKR(cudaMalloc(&dpairs.p, (size_t)n * 8 * sizeof(double)));
     CKR(cudaMalloc(&dx.p, (size_t)n * 12));
     CKR(cudaMalloc(&dy.p, (size_t)n * 4));
@@ -446,9 +605,9 @@ int knc_mlp_train(const double* pairs, int64_t n, float* weights, const knc_mlp_
     double p1 = 1.0, p2 = 1.0;
     for (int64_t step = 0; step < tp->steps; ++step) {
         const uint64_t seed = splitmix64((tp->seed ? tp->seed : 1ull) + (uint64_t)step * 0x9E3779B97F4A7C15ull) | 1ull;
-        mlp_fwd_bwd_kernel<<<grid, TRAIN_WARPS * 32, train_smem_bytes()>>>(
+        mlp_train_tc_kernel<<<grid, TC_THREADS, train_smem_bytes()>>>(
             (const float*)dw.p, (const float*)dx.p, (const float*)dy.p, n, batch, seed, 1.0f / (float)batch,
-            (float*)dg.p, (float*)dl.p, nullptr);
+            (float*)dg.p, (float*)dl.p, nullptr, (unsigned*)de.p);
         p1 *= b1;
         p2 *= b2;
         // learning-rate decay: cosine over the run to 5 % of the initial rate
@@ -462,10 +621,13 @@ int knc_mlp_train(const double* pairs, int64_t n, float* weights, const knc_mlp_
     // final loss over (up to) the first 1M rows
     const int64_t ev = std::min<int64_t>(n, 1 << 20);
     CKR(cudaMemset(dl.p, 0, 4));
-    mlp_fwd_bwd_kernel<<<grid_for_rows(ev), TRAIN_WARPS * 32, train_smem_bytes()>>>(
+    mlp_train_tc_kernel<<<grid_for_rows(ev), TC_THREADS, train_smem_bytes()>>>(
         (const float*)dw.p, (const float*)dx.p, (const float*)dy.p, n, ev, 0ull, 1.0f / (float)ev, (float*)dg.p,
-        (float*)dl.p, nullptr);
+        (float*)dl.p, nullptr, (unsigned*)de.p);
     CKR(cudaGetLastError());
+    unsigned err = 0;
+    CKR(cudaMemcpy(&err, de.p, 4, cudaMemcpyDeviceToHost));
+    if (err) return KNC_ERR_TIMEOUT;
     float lsum = 0.f;
     CKR(cudaMemcpy(&lsum, dl.p, 4, cudaMemcpyDeviceToHost));
     CKR(cudaMemcpy(weights, dw.p, KNC_MLP_NUM_PARAMS * 4, cudaMemcpyDeviceToHost));

@@ -420,7 +420,10 @@ def run_knc(args):
     probe.advance(2)
     run_pairs = learned.sample_pairs(probe, stride=16)
     probe.close()
-    weights, train_loss = learned.train(np.concatenate([pairs, run_pairs]), steps=args.train_steps, seed=11)
+    all_pairs = np.concatenate([pairs, run_pairs])
+    data_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    weights, train_loss = learned.train(all_pairs, steps=args.train_steps, seed=11)
     train_s = time.perf_counter() - t0
 
     def make(mixed: bool, guess: bool, graph: bool, workload=None, tune=False):
@@ -659,7 +662,8 @@ def run_knc(args):
             "l1_density_after_run": l1_run,
             "c2p": {"fp64_iters_per_zone": sth["iters_fp64"] / max(sth["zones"], 1),
                     "fp32_iters_per_zone": sth["iters_fp32"] / max(sth["zones"], 1),
-                    "fallbacks": sth["fallbacks"], "mlp_train_loss": train_loss, "mlp_train_s": train_s},
+                    "fallbacks": sth["fallbacks"], "mlp_train_loss": train_loss, "mlp_train_s": train_s,
+                    "mlp_train_steps": args.train_steps, "mlp_train_pairs": len(all_pairs), "mlp_data_s": data_s},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                          "peak_source": peak_src, "avg_launch_ms": dom_ms,
