@@ -1039,14 +1039,18 @@ int fused_grid(knc_ctx* c) {
     int per_sm = 1;
     const bool mlp = c->guess == KNC_GUESS_MLP && c->d_mlp;
     const bool strip_only = mixed(c) && c->uform == KNC_UPDATE_STRIP;
-    const cudaError_t e = strip_only ? fused_strip_max_ctas_mixed(mlp, &per_sm)
+    const bool deferred = strip_only && c->rform == KNC_RECOVERY_DEFERRED;
+    const int mb = c->ctas_per_sm >= 4 && c->ctas_per_sm <= 6 ? c->ctas_per_sm : 4;   // StageArgs::strip_ctas
+    const cudaError_t e = deferred     ? fused_deferred_max_ctas_mixed(mlp, mb, &per_sm)
+                          : strip_only ? fused_strip_max_ctas_mixed(mlp, &per_sm)
                           : mixed(c) ? fused_max_ctas_mixed(mlp, c->utr, &per_sm)
                                      : fused_max_ctas_f64(mlp && c->hp.system == KNC_SYSTEM_RELATIVISTIC, c->utr, &per_sm);
     if (e != cudaSuccess || per_sm < 1) per_sm = 1;
     if (c->ctas_per_sm > 0 && c->ctas_per_sm < per_sm) per_sm = c->ctas_per_sm;
     const Layout& l = L(c);
     const int nt = fused_threads(c);
-    const int need_a = (int)(2 * l.nq_edge[0] + nt - 1) / nt + (int)(2 * l.nq_edge[1] + nt - 1) / nt + l.nchunks;
+    const int need_a = (int)(2 * l.nq_edge[0] + nt - 1) / nt + (int)(2 * l.nq_edge[1] + nt - 1) / nt +
+                       (deferred ? (l.ntiles + nt / 32 - 1) / (nt / 32) : l.nchunks);
     const int need_b = (int)(((int64_t)l.nremap * 2 * l.max_nq + nt - 1) / nt);
     const int need_c = l.uform == KNC_UPDATE_STRIP ? (l.nstrips + nt / 32 - 1) / (nt / 32) : l.nutiles;
     const int need = std::max(std::max(need_a, need_b), std::max(need_c, 1));
@@ -1124,7 +1128,7 @@ int prepare_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, 
         g.edge_slot[1] = (int32_t)L(c).slot_index.size() - 1;
         g.uu_high_f = a.uu_high_f;
     }
-    if (mixed(c) && !c->fused && c->rform == KNC_RECOVERY_DEFERRED && c->d_high) {
+    if (mixed(c) && (!c->fused || c->uform == KNC_UPDATE_STRIP) && c->rform == KNC_RECOVERY_DEFERRED && c->d_high) {
         a.high = c->d_high;
         a.high_count = &c->d_status->high_count[stage & 1];
         a.high_count_next = &c->d_status->high_count[(stage + 1) & 1];
@@ -1159,7 +1163,9 @@ int run_stage(knc_ctx* c, int sel_in, int sel_out, int sel_base, double w1, doub
         f.spin_limit = c->wait_polls > 0 ? c->wait_polls : BARRIER_SPIN_LIMIT;
         f.bar_base = c->bar_epoch + (c->wait_unreachable ? 1u : 0u);
         const int grid = fused_grid(c);
-        c->bar_epoch += (unsigned long long)grid * (lay.nremap ? 2u : 1u);
+        // barrier arrivals per CTA: the deferring form always counts three
+        const bool deferred = mixed(c) && c->uform == KNC_UPDATE_STRIP && c->rform == KNC_RECOVERY_DEFERRED;
+        c->bar_epoch += (unsigned long long)grid * (deferred ? 3u : lay.nremap ? 2u : 1u);
         ProfScope ps(c, KNC_KERNEL_FUSED);
         CK(mixed(c) ? launch_stage_fused_mixed(a, g, f, grid, c->stream)
                     : launch_stage_fused_f64(a, g, f, grid, c->stream));
@@ -2732,6 +2738,13 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
                     : fused_max_ctas_f64(mlp && c->hp.system == KNC_SYSTEM_RELATIVISTIC, 8, &per_sm));
         for (int sr : {8, 16, 32})
             for (int k = 1; k <= per_sm && k <= 8; ++k) cands.push_back({sr, 1, k, KNC_UPDATE_STRIP});
+        if (mixed(c)) {
+            // with the deferring recovery (the separate form's five launches in one)
+            CK(fused_deferred_max_ctas_mixed(mlp, 5, &per_sm));
+            for (int sr : {8, 12, 16, 32})
+                for (int k = std::max(1, per_sm - 1); k <= per_sm && k <= 8; ++k)
+                    cands.push_back({sr, 1, k, KNC_UPDATE_STRIP, KNC_RECOVERY_DEFERRED});
+        }
     }
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));

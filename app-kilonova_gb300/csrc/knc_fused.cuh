@@ -53,6 +53,17 @@ __device__ __forceinline__ void grid_barrier(DevStatus* st, unsigned long long t
     __syncthreads();
 }
 
+// A barrier the CTA passes without waiting: it only counts its arrival, so the
+// barriers after it keep their targets. For a phase with no work (every CTA
+// knows it from the same device value), the next phase may start at once.
+__device__ __forceinline__ void grid_arrive(DevStatus* st) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(&st->bar_count, 1ull);
+    }
+}
+
 // Per-thread recovery statistics (summed into DevStatus at the end). 32-bit
 // per thread (a thread recovers far fewer than 2^28 zones of at most 16
 // iterations each), widened for the warp sums.

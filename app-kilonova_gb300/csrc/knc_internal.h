@@ -265,6 +265,9 @@ cudaError_t fused_max_ctas_f64(bool mlp, int utr, int* per_sm);
 cudaError_t fused_max_ctas_mixed(bool mlp, int utr, int* per_sm);
 // The mixed fused stage with warp strips only (CTAs of STRIP_WARPS warps).
 cudaError_t fused_strip_max_ctas_mixed(bool mlp, int* per_sm);
+// The mixed fused stage with the deferring recovery and warp strips, built
+// for mb (4 or 5) resident CTAs per SM.
+cudaError_t fused_deferred_max_ctas_mixed(bool mlp, int mb, int* per_sm);
 // Threads of a fused / update CTA for tile rows utr.
 inline int stage_threads(int utr) { return (utr + 1) * TILE_Q; }
 // Tile rows the fused kernel is instantiated for: utr when it is a tile

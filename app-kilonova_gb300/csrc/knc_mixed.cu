@@ -396,6 +396,41 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// One recovery tile t = {slot, i0, j0, -} walked by the calling warp: its
+// TILE_R rows of 32 zones, each lane's column of the next rows copied ahead
+// into the warp's staging slots sUw. Zones that need the FP64 recovery go to
+// the stage's list (a.high).
+template <int DT>
+__device__ __forceinline__ void recover_rows_tile(const StageArgs& a, const int4 t, double (*sUw)[NFIELD][32],
+                                                  MlpWeights& W, C2pStats& st) {
+    const int lane = threadIdx.x & 31;
+    const DevBlock& B = a.blocks[t.x];
+    const int j = t.z + lane;
+    const bool jin = j < B.nq;
+    const int rows = min(TILE_R, B.nr - t.y);
+    const int64_t n = (int64_t)B.nr * B.nq;
+    const double* Ub = B.buf[a.sel_in] + (int64_t)t.y * B.nq + j;
+    auto issue = [&](int r) {
+        if (jin && r < rows) {
+#pragma unroll
+            for (int q = 0; q < NFIELD; ++q) cp_async8(&sUw[r % C2P_DEPTH][q][lane], Ub + q * n + (int64_t)r * B.nq);
+        }
+        cp_async_commit();
+    };
+#pragma unroll
+    for (int r = 0; r < C2P_DEPTH - 1; ++r) issue(r);
+    for (int r = 0; r < rows; ++r) {
+        issue(r + C2P_DEPTH - 1);
+        cp_async_wait<C2P_DEPTH - 1>();
+        double U[5] = {1.0, 0.0, 0.0, 1.0, 0.0};
+        if (jin) {
+#pragma unroll
+            for (int q = 0; q < NFIELD; ++q) U[q] = sUw[r % C2P_DEPTH][q][lane];
+        }
+        MixedC2p<false, true>::zone_state<DT>(a, t.x, B, t.y + r, j, jin, U, W, nullptr, st);
+    }
+}
+
 template <int DT>
 __global__ void __launch_bounds__(TILE_THREADS, 3) c2p_rows_kernel(StageArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -406,38 +441,29 @@ __global__ void __launch_bounds__(TILE_THREADS, 3) c2p_rows_kernel(StageArgs a) 
     const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
     if (ek != NO_ERROR && (uint32_t)(ek >> 48) < (uint32_t)a.stage) return;
     MlpWeights& W = *reinterpret_cast<MlpWeights*>(smem_raw);   // unused without the learned guess
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int w = threadIdx.x >> 5;
     C2pStats st;
-    for (int tile = blockIdx.x * WPC + w; tile < a.ntiles; tile += gridDim.x * WPC) {
-        const int4 t = a.tiles[tile];
-        const DevBlock& B = a.blocks[t.x];
-        const int j = t.z + lane;
-        const bool jin = j < B.nq;
-        const int rows = min(TILE_R, B.nr - t.y);
-        const int64_t n = (int64_t)B.nr * B.nq;
-        const double* Ub = B.buf[a.sel_in] + (int64_t)t.y * B.nq + j;
-        auto issue = [&](int r) {
-            if (jin && r < rows) {
-#pragma unroll
-                for (int q = 0; q < NFIELD; ++q) cp_async8(&sU[w][r % C2P_DEPTH][q][lane], Ub + q * n + (int64_t)r * B.nq);
-            }
-            cp_async_commit();
-        };
-#pragma unroll
-        for (int r = 0; r < C2P_DEPTH - 1; ++r) issue(r);
-        for (int r = 0; r < rows; ++r) {
-            issue(r + C2P_DEPTH - 1);
-            cp_async_wait<C2P_DEPTH - 1>();
-            double U[5] = {1.0, 0.0, 0.0, 1.0, 0.0};
-            if (jin) {
-#pragma unroll
-                for (int q = 0; q < NFIELD; ++q) U[q] = sU[w][r % C2P_DEPTH][q][lane];
-            }
-            MixedC2p<false, true>::zone_state<DT>(a, t.x, B, t.y + r, j, jin, U, W, nullptr, st);
-        }
-    }
+    for (int tile = blockIdx.x * WPC + w; tile < a.ntiles; tile += gridDim.x * WPC)
+        recover_rows_tile<DT>(a, a.tiles[tile], sU[w], W, st);
     cp_async_wait<0>();
     warp_reduce_stats(a.status, st.zones, st.it64, st.it32, st.fbs, st.dtz, a.compute_dt != 0);
+}
+
+// The deferred zones (the first `count` of a.high), 32 per warp: warps
+// first, first + step, ... of the grid. Every lane of a warp calls it.
+template <bool MLP>
+__device__ __forceinline__ void recover_high_groups(const StageArgs& a, unsigned count, unsigned first,
+                                                    unsigned step, MlpWeights& W, __nv_bfloat16* act,
+                                                    C2pStats& st) {
+    const unsigned lane = threadIdx.x & 31;
+    for (unsigned base = first * 32; base < count; base += step * 32) {
+        const unsigned k = base + lane;
+        const bool active = k < count;
+        const int2 e = a.high[active ? k : base];
+        const DevBlock& B = a.blocks[e.x];
+        const int i = e.y / B.nq, j = e.y - i * B.nq;
+        MixedC2p<MLP>::zone(a, e.x, B, i, j, active, W, act, st);
+    }
 }
 
 // The deferred zones of this stage ({slot, z} in a.high, *a.high_count of
@@ -463,17 +489,8 @@ __global__ void __launch_bounds__(TILE_THREADS, 2) c2p_high_kernel(StageArgs a) 
         __syncthreads();
     }
     C2pStats st;
-    const unsigned warps = gridDim.x * (TILE_THREADS / 32);
-    const unsigned lane = threadIdx.x & 31;
-    for (unsigned base = (blockIdx.x * (TILE_THREADS / 32) + (threadIdx.x >> 5)) * 32; base < count;
-         base += warps * 32) {
-        const unsigned k = base + lane;
-        const bool active = k < count;
-        const int2 e = a.high[active ? k : base];
-        const DevBlock& B = a.blocks[e.x];
-        const int i = e.y / B.nq, j = e.y - i * B.nq;
-        MixedC2p<MLP>::zone(a, e.x, B, i, j, active, W, act, st);
-    }
+    recover_high_groups<MLP>(a, count, blockIdx.x * (TILE_THREADS / 32) + (threadIdx.x >> 5),
+                             gridDim.x * (TILE_THREADS / 32), W, act, st);
     warp_reduce_stats(a.status, st.zones, st.it64, st.it32, st.fbs, st.dtz, a.compute_dt != 0);
 }
 
@@ -714,6 +731,161 @@ __global__ void __launch_bounds__(STRIP_WARPS * 32, 5)
     stage_fused_body<float, true, 8, MixedC2p<MLP>, STRIP_WARPS * 32, true>(a, g, f);
 }
 
+// The fused stage with the deferring recovery and warp strips, the separate
+// form's five launches in one (CTAs of 4 warps, all resident):
+//   A  ghost rows of both mesh ends (CTA items), then the recovery tiles, one
+//      per warp, rows walked with the next rows copied ahead (recover_rows_tile;
+//      zones needing the FP64 recovery are listed);
+//   -- barrier --
+//   B  the listed zones densely (recover_high_groups, learned guess on the
+//      tensor cores); -- barrier, only waited on when the list holds a zone --
+//      then the halo remaps across polar-resolution changes (they copy a
+//      coarser neighbour's recovered primitives, so they follow the dense
+//      pass); -- barrier, only waited on with remaps --
+//   C  the warp strips of the update.
+// Every launch counts three barrier arrivals per CTA (the host advances its
+// barrier epoch by three grids); a barrier whose phase has no work is passed
+// with its arrival only. The phases call the functions of the separate
+// kernels, so the two forms give bit-identical states.
+// The phases of the fused deferring stage; each sums its recovery statistics
+// (and the time-step reduction) like its separate kernel does.
+__device__ __forceinline__ void fused_ghost_phase(const GhostArgs& g) {
+    constexpr int NT = STRIP_WARPS * 32;
+    const int ng0 = (2 * g.nq[0] + NT - 1) / NT, ng1 = (2 * g.nq[1] + NT - 1) / NT;
+    for (int item = blockIdx.x; item < ng0 + ng1; item += gridDim.x) {
+        if (item < ng0) ghost_zone(g, 0, item * NT + threadIdx.x);
+        else ghost_zone(g, 1, (item - ng0) * NT + threadIdx.x);
+    }
+}
+
+template <int DT>
+__device__ __forceinline__ void fused_recovery_phase(const StageArgs& a, double (*sUw)[NFIELD][32], MlpWeights& W) {
+    C2pStats st;
+    for (int tile = blockIdx.x * STRIP_WARPS + (int)(threadIdx.x >> 5); tile < a.ntiles; tile += gridDim.x * STRIP_WARPS)
+        recover_rows_tile<DT>(a, a.tiles[tile], sUw, W, st);
+    cp_async_wait<0>();
+    warp_reduce_stats(a.status, st.zones, st.it64, st.it32, st.fbs, st.dtz, a.compute_dt != 0);
+}
+
+template <bool MLP>
+__device__ __forceinline__ void fused_high_phase(const StageArgs& a, unsigned count, MlpWeights& W,
+                                                     __nv_bfloat16* act) {
+    C2pStats st;
+    recover_high_groups<MLP>(a, count, blockIdx.x * STRIP_WARPS + (threadIdx.x >> 5), gridDim.x * STRIP_WARPS, W,
+                             act, st);
+    warp_reduce_stats(a.status, st.zones, st.it64, st.it32, st.fbs, st.dtz, a.compute_dt != 0);
+}
+
+__device__ __forceinline__ void fused_remap_phase(const StageArgs& a, const FusedArgs& f) {
+    constexpr int NT = STRIP_WARPS * 32;
+    const int per = 2 * f.max_nq;
+    const int total = f.nremap * per;
+    for (int k = blockIdx.x * NT + threadIdx.x; k < total; k += gridDim.x * NT) {
+        const int item = k / per;
+        remap_zone<float, MixedRemapRecovery>(a, f.remap[item], k - item * per);
+    }
+}
+
+__device__ __forceinline__ void fused_update_phase(const StageArgs& a) {
+    stage_strips<float, true>(a, blockIdx.x * STRIP_WARPS + (int)(threadIdx.x >> 5), gridDim.x * STRIP_WARPS);
+}
+
+// The fused stage with the deferring recovery and warp strips, the separate
+// form's five launches in one (CTAs of 4 warps, all resident):
+//   A  ghost rows of both mesh ends (CTA items), then the recovery tiles, one
+//      per warp, rows walked with the next rows copied ahead (recover_rows_tile;
+//      zones needing the FP64 recovery are listed);
+//   -- barrier --
+//   B  the listed zones densely (recover_high_groups, learned guess on the
+//      tensor cores); -- barrier, only waited on when the list holds a zone --
+//      then the halo remaps across polar-resolution changes (they copy a
+//      coarser neighbour's recovered primitives, so they follow the dense
+//      pass); -- barrier, only waited on with remaps --
+//   C  the warp strips of the update.
+// Every launch counts three barrier arrivals per CTA (the host advances its
+// barrier epoch by three grids); a barrier whose phase has no work is passed
+// with its arrival only. The phases call the functions of the separate
+// kernels, so the two forms give bit-identical states.
+template <bool MLP, int MB>
+__global__ void __launch_bounds__(STRIP_WARPS * 32, MB)
+    stage_fused_deferred_kernel(const __grid_constant__ StageArgs a, const __grid_constant__ GhostArgs g,
+                                const __grid_constant__ FusedArgs f) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ __align__(16) double sU[STRIP_WARPS][C2P_DEPTH][NFIELD][32];
+    __shared__ int run_update;
+    constexpr int NT = STRIP_WARPS * 32;
+    MlpWeights& W = *reinterpret_cast<MlpWeights*>(smem_raw);
+    __nv_bfloat16* act = reinterpret_cast<__nv_bfloat16*>(smem_raw + sizeof(MlpWeights)) +
+                         (threadIdx.x >> 5) * MLP_ACT_ELEMS;
+    // a failure in an earlier stage stops the step; every CTA still arrives
+    // at every barrier
+    const unsigned long long ek = *(volatile unsigned long long*)&a.status->err_key;
+    const bool run = !(ek != NO_ERROR && (uint32_t)(ek >> 48) < (uint32_t)a.stage);
+
+    // ---- A
+    if (run) {
+        fused_ghost_phase(g);
+        if (a.compute_dt) fused_recovery_phase<1>(a, sU[threadIdx.x >> 5], W);
+        else fused_recovery_phase<0>(a, sU[threadIdx.x >> 5], W);
+    }
+    grid_barrier(a.status, f.bar_base + gridDim.x, f.spin_limit);
+
+    // ---- B: the listed zones, then the remaps
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.high_count_next = 0u;   // the next stage's list starts empty
+    const unsigned count = min(*(volatile unsigned*)a.high_count, a.high_cap);
+    if (run && count > 0u && (unsigned)blockIdx.x * NT < count) {
+        if (MLP) {
+            mlp_load(W, a.mlp);
+            __syncthreads();
+        }
+        fused_high_phase<MLP>(a, count, W, act);
+    }
+    if (count > 0u) grid_barrier(a.status, f.bar_base + 2ull * gridDim.x, f.spin_limit);
+    else grid_arrive(a.status);
+    if (f.nremap > 0) {
+        if (run) fused_remap_phase(a, f);
+        grid_barrier(a.status, f.bar_base + 3ull * gridDim.x, f.spin_limit);
+    } else {
+        grid_arrive(a.status);
+    }
+
+    // ---- C: the update's warp strips (skipped after any failure, like the separate kernel)
+    if (threadIdx.x == 0)
+        run_update = *(volatile unsigned long long*)&a.status->err_key == NO_ERROR &&
+                     *(volatile int32_t*)&a.status->bar_abort == 0;
+    __syncthreads();
+    if (run_update) fused_update_phase(a);
+}
+
+// MB: resident CTAs per SM the register allocation is sized for (4: no
+// spills; 5: more warps)
+template <bool MLP, int MB>
+static cudaError_t fused_deferred(const StageArgs& a, const GhostArgs& g, const FusedArgs& f, int grid,
+                                  cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(STRIP_WARPS * 32);
+    cfg.dynamicSmemBytes = fused_strip_smem_bytes<MLP>();
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, stage_fused_deferred_kernel<MLP, MB>, a, g, f);
+}
+
+template <bool MLP, int MB>
+static cudaError_t fused_deferred_ctas(int* n) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, stage_fused_deferred_kernel<MLP, MB>, STRIP_WARPS * 32,
+                                                         fused_strip_smem_bytes<MLP>());
+}
+
+cudaError_t fused_deferred_max_ctas_mixed(bool mlp, int mb, int* n) {
+    if (mb == 4) return mlp ? fused_deferred_ctas<true, 4>(n) : fused_deferred_ctas<false, 4>(n);
+    return mlp ? fused_deferred_ctas<true, 5>(n) : fused_deferred_ctas<false, 5>(n);
+}
+
 template <bool MLP>
 static cudaError_t fused_strip_mixed(const StageArgs& a, const GhostArgs& g, const FusedArgs& f, int grid,
                                      cudaStream_t s) {
@@ -740,6 +912,11 @@ cudaError_t fused_strip_max_ctas_mixed(bool mlp, int* n) {
 cudaError_t launch_stage_fused_mixed(const StageArgs& a, const GhostArgs& g, const FusedArgs& f, int grid,
                                      cudaStream_t s) {
     const bool mlp = a.mlp != nullptr;
+    if (a.strips && a.high) {
+        // built for 4 CTAs per SM (no spills) or 5 (more warps), like the strip kernels
+        if (a.strip_ctas == 4) return mlp ? fused_deferred<true, 4>(a, g, f, grid, s) : fused_deferred<false, 4>(a, g, f, grid, s);
+        return mlp ? fused_deferred<true, 5>(a, g, f, grid, s) : fused_deferred<false, 5>(a, g, f, grid, s);
+    }
     if (a.strips) return mlp ? fused_strip_mixed<true>(a, g, f, grid, s) : fused_strip_mixed<false>(a, g, f, grid, s);
     switch (fused_tr(a.utr)) {
     case 4: return mlp ? fused_mixed<4, true>(a, g, f, grid, s) : fused_mixed<4, false>(a, g, f, grid, s);

@@ -569,25 +569,58 @@ def run_knc(args):
         u64 = make(False, False, False, workload=wu, tune=True)
         ms_u64, _ = timed(u64, args.steps, args.fold)
         zu64 = timed.zone_updates
-        uh = make(True, True, True, workload=wu, tune=True)
-        ms_uh, launches_u = timed(uh, args.steps, args.fold)
-        zuh = timed.zone_updates
         ms_u64 = max_over_ranks(pg, ms_u64)
-        ms_uh = max_over_ranks(pg, ms_uh)
-        same_blocks = uh.block_indexes() == u64.block_indexes()
+
+        def run_c4(tuning=None):
+            """The mixed + learned + graph path on the uneven workload with the
+            autotuner's launch shape (tuning None) or the given one."""
+            s = make(True, True, True, workload=wu, tune=tuning is None)
+            if tuning is not None:
+                s.set_tuning(**tuning)
+            ms, launches = timed(s, args.steps, args.fold)
+            z = timed.zone_updates
+            ms = max_over_ranks(pg, ms)
+            r = {"value": z * world / (ms * 1e-3), "ms_per_step": ms / args.steps,
+                 "launches_per_stage": launches / (3 * args.steps), "tuning": s.tuning(),
+                 "blocks_end": len(s.block_indexes()),
+                 "block_range_end": [s.block_indexes()[0], s.block_indexes()[-1]],
+                 "speedup_vs_fp64": (z / ms) / (zu64 / ms_u64),
+                 "l1_density": l1_density(s, u64) if s.block_indexes() == u64.block_indexes() else None}
+            s.close()
+            return r
+
+        auto = run_c4()
+        t = auto["tuning"]
+        rows = t["tile_rows"] if t["strip"] else 16
+        # the autotuner times single stages launched from the host; the timed
+        # run replays captured folds, where launch gaps are hidden, so the
+        # other family of shapes is timed the same way too: the separate
+        # deferring launches, or every RK3 stage as one cooperative launch (the
+        # fused deferring form at 4 and 5 resident CTAs per SM)
+        fused = auto if t["fused"] else None
+        separate = None if t["fused"] else auto
+        if fused is None:
+            for k in (4, 5):
+                r = run_c4(dict(tile_rows=rows, fused=True, strip=True, ctas_per_sm=k, deferred=True))
+                if fused is None or r["ms_per_step"] < fused["ms_per_step"]:
+                    fused = r
+        else:
+            separate = run_c4(dict(tile_rows=rows, strip=True, ctas_per_sm=5, deferred=True))
+        best = fused if fused["ms_per_step"] < separate["ms_per_step"] else separate
         un = {"workload": f"{wu.name}: {wu.zones} zones at start, nr from 32..512 and nq from 64..256 "
                           "per block (seeded), RK3, both excision surfaces at 0.5c",
-              "zones_start": wu.zones, "blocks_end": len(uh.block_indexes()),
-              "block_range_end": [uh.block_indexes()[0], uh.block_indexes()[-1]],
-              "value": zuh * world / (ms_uh * 1e-3), "fp64_value": zu64 * world / (ms_u64 * 1e-3),
-              "speedup_vs_fp64": (zuh / ms_uh) / (zu64 / ms_u64),
-              "ms_per_step": ms_uh / args.steps, "fp64_ms_per_step": ms_u64 / args.steps,
-              "l1_density": l1_density(uh, u64) if same_blocks else None,
-              "tuning": uh.tuning(), "launches_per_stage": launches_u / (3 * args.steps),
-              "path": "mixed + learned guess + one CUDA graph per fold; each RK3 stage one launch when the "
-                      "autotuner picks the fused form"}
+              "zones_start": wu.zones, "blocks_end": best["blocks_end"],
+              "block_range_end": best["block_range_end"],
+              "value": best["value"], "fp64_value": zu64 * world / (ms_u64 * 1e-3),
+              "speedup_vs_fp64": best["speedup_vs_fp64"],
+              "ms_per_step": best["ms_per_step"], "fp64_ms_per_step": ms_u64 / args.steps,
+              "l1_density": best["l1_density"], "tuning": best["tuning"],
+              "launches_per_stage": best["launches_per_stage"],
+              "autotuned_tuning": t,
+              "separate_launches": separate, "one_launch_per_stage": fused,
+              "path": "mixed + learned guess + one CUDA graph per fold; the faster of the separate launches and "
+                      "the one-launch-per-stage form, both timed as captured folds"}
         u64.close()
-        uh.close()
 
     # ---- the learned guess inside the W = 100 jet (2048 x 512), against plain
     # Newton from the reference's guess: FP64 / FP32 iterations per zone and

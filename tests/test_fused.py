@@ -296,3 +296,53 @@ def test_mixed_deferred_recovery_matches_inline(learned):
     assert runs[1].c2p_stats()["iters_fp64"] > 0
     assert runs[0].c2p_stats() == runs[1].c2p_stats()
     assert _same(runs[0].state(), runs[1].state())
+
+
+def _mixed_strips(w, fused, deferred, batched, mlp=None, steps=6, rows=16):
+    import knc
+    g, _ = make_pair(w, gpu=True)
+    g.set_precision(knc.abi.KNC_PRECISION_MIXED)
+    if mlp is not None:
+        g.set_c2p_guess(knc.abi.KNC_GUESS_MLP, mlp)
+    g.set_tuning(tile_rows=rows, strip=True, fused=fused, deferred=deferred)
+    g.set_batched(batched)
+    for _ in range(steps // 3):
+        g.advance(3)
+    return g
+
+
+@pytest.mark.parametrize("name", ["uneven_small", "jet_small", "wind_small"])
+def test_mixed_fused_deferred_matches_separate(name):
+    """The fused stage with the deferring recovery (ghost rows, recovery,
+    dense FP64 pass, remaps and update in one cooperative launch) equals the
+    separate deferring launches bit for bit: on a moving uneven mesh (remaps
+    every stage), on the W = 100 jet with the learned guess (listed zones, so
+    the dense pass and its barrier run) and on the wind (neither)."""
+    from knc import learned, workloads
+    w = workloads.WORKLOADS[name]()
+    wts = None
+    if name == "jet_small":
+        wts = learned.init_weights(seed=3)
+        wts[-6:-3] = 0.0
+        wts[-3:] = 1.0
+    steps = 12 if name == "uneven_small" else 6
+    ref = _mixed_strips(w, False, True, False, mlp=wts, steps=steps)
+    g = _mixed_strips(w, True, True, True, mlp=wts, steps=steps)
+    assert g.block_indexes() == ref.block_indexes()
+    assert _same(g.state(), ref.state())
+    assert g.time() == ref.time()
+
+
+def test_fused_deferred_one_launch_per_stage():
+    import knc
+    from knc import workloads
+    w = workloads.uneven_small(order="RK3")
+    g, _ = make_pair(w, gpu=True)
+    g.set_precision(knc.abi.KNC_PRECISION_MIXED)
+    g.set_tuning(tile_rows=16, strip=True, fused=True, deferred=True)
+    # RK3: three stages per step, one launch each; an advance call may add
+    # one time-step pass
+    n0 = g.launch_count()
+    g.advance(4)
+    assert g.launch_count() - n0 in (4 * 3, 4 * 3 + 1)
+
