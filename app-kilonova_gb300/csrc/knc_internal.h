@@ -102,6 +102,10 @@ struct DevStatus {
     // the work items of that list the update has claimed
     unsigned hp_count[2];
     unsigned hp_claim[2];
+    // the fused deferring stage: phase A's work items (ghost-row groups, then
+    // recovery tiles) claimed by warps; zero between launches
+    unsigned item_claim;
+    unsigned pad3;
 };
 
 struct StageArgs {

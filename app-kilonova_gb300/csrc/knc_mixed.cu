@@ -733,9 +733,9 @@ __global__ void __launch_bounds__(STRIP_WARPS * 32, 5)
 
 // The fused stage with the deferring recovery and warp strips, the separate
 // form's five launches in one (CTAs of 4 warps, all resident):
-//   A  ghost rows of both mesh ends (CTA items), then the recovery tiles, one
-//      per warp, rows walked with the next rows copied ahead (recover_rows_tile;
-//      zones needing the FP64 recovery are listed);
+//   A  work items claimed by warps: ghost rows of both mesh ends in groups of
+//      32 zones, then the recovery tiles, rows walked with the next rows copied
+//      ahead (recover_rows_tile; zones needing the FP64 recovery are listed);
 //   -- barrier --
 //   B  the listed zones densely (recover_high_groups, learned guess on the
 //      tensor cores); -- barrier, only waited on when the list holds a zone --
@@ -749,20 +749,27 @@ __global__ void __launch_bounds__(STRIP_WARPS * 32, 5)
 // kernels, so the two forms give bit-identical states.
 // The phases of the fused deferring stage; each sums its recovery statistics
 // (and the time-step reduction) like its separate kernel does.
-__device__ __forceinline__ void fused_ghost_phase(const GhostArgs& g) {
-    constexpr int NT = STRIP_WARPS * 32;
-    const int ng0 = (2 * g.nq[0] + NT - 1) / NT, ng1 = (2 * g.nq[1] + NT - 1) / NT;
-    for (int item = blockIdx.x; item < ng0 + ng1; item += gridDim.x) {
-        if (item < ng0) ghost_zone(g, 0, item * NT + threadIdx.x);
-        else ghost_zone(g, 1, (item - ng0) * NT + threadIdx.x);
-    }
-}
-
+// Phase A of the fused deferring stage, per warp: work items claimed one at a
+// time (a.status->item_claim), first the ghost rows of both mesh ends in
+// groups of 32 zones, then the recovery tiles. The ghost rows are a long FP64
+// latency chain per zone (the separate form hides it on a second stream);
+// claimed first and dynamically, they delay no warp's share of the tiles.
 template <int DT>
-__device__ __forceinline__ void fused_recovery_phase(const StageArgs& a, double (*sUw)[NFIELD][32], MlpWeights& W) {
+__device__ __forceinline__ void fused_phase_a(const StageArgs& a, const GhostArgs& g, double (*sUw)[NFIELD][32],
+                                              MlpWeights& W) {
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned ng0 = (unsigned)(2 * g.nq[0] + 31) / 32, ng1 = (unsigned)(2 * g.nq[1] + 31) / 32;
+    const unsigned total = ng0 + ng1 + (unsigned)a.ntiles;
     C2pStats st;
-    for (int tile = blockIdx.x * STRIP_WARPS + (int)(threadIdx.x >> 5); tile < a.ntiles; tile += gridDim.x * STRIP_WARPS)
-        recover_rows_tile<DT>(a, a.tiles[tile], sUw, W, st);
+    for (;;) {
+        unsigned item = 0u;
+        if (lane == 0) item = atomicAdd(&a.status->item_claim, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= total) break;
+        if (item < ng0) ghost_zone(g, 0, (int)(item * 32 + lane));
+        else if (item < ng0 + ng1) ghost_zone(g, 1, (int)((item - ng0) * 32 + lane));
+        else recover_rows_tile<DT>(a, a.tiles[item - ng0 - ng1], sUw, W, st);
+    }
     cp_async_wait<0>();
     warp_reduce_stats(a.status, st.zones, st.it64, st.it32, st.fbs, st.dtz, a.compute_dt != 0);
 }
@@ -792,9 +799,9 @@ __device__ __forceinline__ void fused_update_phase(const StageArgs& a) {
 
 // The fused stage with the deferring recovery and warp strips, the separate
 // form's five launches in one (CTAs of 4 warps, all resident):
-//   A  ghost rows of both mesh ends (CTA items), then the recovery tiles, one
-//      per warp, rows walked with the next rows copied ahead (recover_rows_tile;
-//      zones needing the FP64 recovery are listed);
+//   A  work items claimed by warps: ghost rows of both mesh ends in groups of
+//      32 zones, then the recovery tiles, rows walked with the next rows copied
+//      ahead (recover_rows_tile; zones needing the FP64 recovery are listed);
 //   -- barrier --
 //   B  the listed zones densely (recover_high_groups, learned guess on the
 //      tensor cores); -- barrier, only waited on when the list holds a zone --
@@ -824,14 +831,16 @@ __global__ void __launch_bounds__(STRIP_WARPS * 32, MB)
 
     // ---- A
     if (run) {
-        fused_ghost_phase(g);
-        if (a.compute_dt) fused_recovery_phase<1>(a, sU[threadIdx.x >> 5], W);
-        else fused_recovery_phase<0>(a, sU[threadIdx.x >> 5], W);
+        if (a.compute_dt) fused_phase_a<1>(a, g, sU[threadIdx.x >> 5], W);
+        else fused_phase_a<0>(a, g, sU[threadIdx.x >> 5], W);
     }
     grid_barrier(a.status, f.bar_base + gridDim.x, f.spin_limit);
 
     // ---- B: the listed zones, then the remaps
-    if (blockIdx.x == 0 && threadIdx.x == 0) *a.high_count_next = 0u;   // the next stage's list starts empty
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *a.high_count_next = 0u;       // the next stage's list starts empty
+        a.status->item_claim = 0u;     // phase A's items are all claimed: zero for the next launch
+    }
     const unsigned count = min(*(volatile unsigned*)a.high_count, a.high_cap);
     if (run && count > 0u && (unsigned)blockIdx.x * NT < count) {
         if (MLP) {
