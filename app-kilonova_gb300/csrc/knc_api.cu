@@ -2738,8 +2738,12 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
                     : fused_max_ctas_f64(mlp && c->hp.system == KNC_SYSTEM_RELATIVISTIC, 8, &per_sm));
         for (int sr : {8, 16, 32})
             for (int k = 1; k <= per_sm && k <= 8; ++k) cands.push_back({sr, 1, k, KNC_UPDATE_STRIP});
-        if (mixed(c)) {
-            // with the deferring recovery (the separate form's five launches in one)
+        if (mixed(c) && !c->batched) {
+            // with the deferring recovery (the separate form's five launches in
+            // one). Only for stages launched from the host one by one: the
+            // candidates are timed that way, and inside a fold's captured
+            // graph, where the separate launches' gaps are hidden, the fused
+            // form measured 2-7% slower than the separate one
             CK(fused_deferred_max_ctas_mixed(mlp, 5, &per_sm));
             for (int sr : {8, 12, 16, 32})
                 for (int k = std::max(1, per_sm - 1); k <= per_sm && k <= 8; ++k)
