@@ -2718,11 +2718,17 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
         for (int sr : {4, 8, 10, 12, 16, 20, 24, 32, 64})
             for (int mb : {4, 5, 6})
                 if (mixed(c) || mb == 4) cands.push_back({sr, 0, mb, KNC_UPDATE_STRIP});
+    // The fused stages (one cooperative launch per stage) only for solvers
+    // that launch their stages from the host one by one, the way candidates
+    // are timed: inside a batched solver's captured folds, where the
+    // separate launches' gaps are hidden, every fused form measured slower
+    // than the separate launches (by 2-8% for the fused deferring stage)
+    const bool offer_fused = c->coop && !c->batched;
     for (int tr : {4, 8, 16}) {
         cands.push_back({tr, 0, 0, KNC_UPDATE_TILE});
         // tensor-copy staging (used where every block allows it)
         if (mixed(c)) cands.push_back({tr, 0, 0, KNC_UPDATE_TILE_TMA});
-        if (!c->coop) continue;
+        if (!offer_fused) continue;
         c->utr = tr;
         int per_sm = 1;
         const bool mlp = c->guess == KNC_GUESS_MLP && c->d_mlp;
@@ -2730,7 +2736,7 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
                     : fused_max_ctas_f64(mlp && c->hp.system == KNC_SYSTEM_RELATIVISTIC, tr, &per_sm));
         for (int k = 1; k <= per_sm && k <= 8; ++k) cands.push_back({tr, 1, k, KNC_UPDATE_TILE});
     }
-    if (c->coop && c->mesh.p.num_polar_zones > 1) {
+    if (offer_fused && c->mesh.p.num_polar_zones > 1) {
         // the fused stage with warp strips in its update phase (CTAs of 9 warps)
         int per_sm = 1;
         const bool mlp = c->guess == KNC_GUESS_MLP && c->d_mlp;
@@ -2738,12 +2744,8 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
                     : fused_max_ctas_f64(mlp && c->hp.system == KNC_SYSTEM_RELATIVISTIC, 8, &per_sm));
         for (int sr : {8, 16, 32})
             for (int k = 1; k <= per_sm && k <= 8; ++k) cands.push_back({sr, 1, k, KNC_UPDATE_STRIP});
-        if (mixed(c) && !c->batched) {
-            // with the deferring recovery (the separate form's five launches in
-            // one). Only for stages launched from the host one by one: the
-            // candidates are timed that way, and inside a fold's captured
-            // graph, where the separate launches' gaps are hidden, the fused
-            // form measured 2-7% slower than the separate one
+        if (mixed(c)) {
+            // with the deferring recovery (the separate form's five launches in one)
             CK(fused_deferred_max_ctas_mixed(mlp, 5, &per_sm));
             for (int sr : {8, 12, 16, 32})
                 for (int k = std::max(1, per_sm - 1); k <= per_sm && k <= 8; ++k)
