@@ -988,6 +988,7 @@ StageArgs base_args(knc_ctx* c) {
     a.strips = c->uform == KNC_UPDATE_STRIP ? L(c).d_strips : nullptr;
     a.nstrips = c->uform == KNC_UPDATE_STRIP ? L(c).nstrips : 0;
     a.strip_ctas = c->ctas_per_sm >= 4 && c->ctas_per_sm <= 6 ? c->ctas_per_sm : 4;
+    a.fused_wide = c->fused && c->ctas_per_sm == 1 ? 1 : 0;
     a.srhd = c->hp.system == KNC_SYSTEM_RELATIVISTIC;
     a.hllc = c->hp.riemann_solver == KNC_RIEMANN_HLLC;
     a.one_dimensional = c->mesh.p.num_polar_zones == 1;
@@ -1040,7 +1041,8 @@ int fused_grid(knc_ctx* c) {
     const bool mlp = c->guess == KNC_GUESS_MLP && c->d_mlp;
     const bool strip_only = mixed(c) && c->uform == KNC_UPDATE_STRIP;
     const bool deferred = strip_only && c->rform == KNC_RECOVERY_DEFERRED;
-    const int mb = c->ctas_per_sm >= 4 && c->ctas_per_sm <= 6 ? c->ctas_per_sm : 4;   // StageArgs::strip_ctas
+    // StageArgs::fused_wide / strip_ctas: the variant of the deferring form
+    const int mb = c->ctas_per_sm == 1 ? 1 : c->ctas_per_sm >= 4 && c->ctas_per_sm <= 6 ? c->ctas_per_sm : 4;
     const cudaError_t e = deferred     ? fused_deferred_max_ctas_mixed(mlp, mb, &per_sm)
                           : strip_only ? fused_strip_max_ctas_mixed(mlp, &per_sm)
                           : mixed(c) ? fused_max_ctas_mixed(mlp, c->utr, &per_sm)
@@ -1048,7 +1050,7 @@ int fused_grid(knc_ctx* c) {
     if (e != cudaSuccess || per_sm < 1) per_sm = 1;
     if (c->ctas_per_sm > 0 && c->ctas_per_sm < per_sm) per_sm = c->ctas_per_sm;
     const Layout& l = L(c);
-    const int nt = fused_threads(c);
+    const int nt = deferred ? fused_deferred_threads(mb) : fused_threads(c);
     const int need_a = (int)(2 * l.nq_edge[0] + nt - 1) / nt + (int)(2 * l.nq_edge[1] + nt - 1) / nt +
                        (deferred ? (l.ntiles + nt / 32 - 1) / (nt / 32) : l.nchunks);
     const int need_b = (int)(((int64_t)l.nremap * 2 * l.max_nq + nt - 1) / nt);
@@ -2747,9 +2749,12 @@ int knc_autotune(knc_ctx* c, int32_t reps, knc_tuning* best_out, double* ms_out)
         if (mixed(c)) {
             // with the deferring recovery (the separate form's five launches in one)
             CK(fused_deferred_max_ctas_mixed(mlp, 5, &per_sm));
-            for (int sr : {8, 12, 16, 32})
-                for (int k = std::max(1, per_sm - 1); k <= per_sm && k <= 8; ++k)
+            // (k = 1: one CTA of 20 warps per SM)
+            for (int sr : {8, 12, 16, 32}) {
+                cands.push_back({sr, 1, 1, KNC_UPDATE_STRIP, KNC_RECOVERY_DEFERRED});
+                for (int k = std::max(2, per_sm - 1); k <= per_sm && k <= 8; ++k)
                     cands.push_back({sr, 1, k, KNC_UPDATE_STRIP, KNC_RECOVERY_DEFERRED});
+            }
         }
     }
     cudaEvent_t e0, e1;

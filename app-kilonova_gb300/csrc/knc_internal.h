@@ -119,6 +119,7 @@ struct StageArgs {
     const int4* strips;     // {slot, i0, j0, rows}: warp strips of the strip form, or null
     int32_t nstrips;
     int32_t strip_ctas;     // strip form: CTAs per SM the kernel is built for (4, 5 or 6)
+    int32_t fused_wide;     // fused deferring stage: one CTA of 20 warps per SM
     // adaptive dt found on the device (the fold's first recovery reduces
     // dl / a_max into *dt_bits): dt = *dt_bits x cfl replaces dt / dt_f
     const unsigned long long* dt_bits;
@@ -270,8 +271,10 @@ cudaError_t fused_max_ctas_mixed(bool mlp, int utr, int* per_sm);
 // The mixed fused stage with warp strips only (CTAs of STRIP_WARPS warps).
 cudaError_t fused_strip_max_ctas_mixed(bool mlp, int* per_sm);
 // The mixed fused stage with the deferring recovery and warp strips, built
-// for mb (4 or 5) resident CTAs per SM.
+// for mb resident CTAs per SM: 4 or 5 CTAs of 4 warps, or (mb = 1) one CTA
+// of 20 warps; fused_deferred_threads(mb): its CTA size.
 cudaError_t fused_deferred_max_ctas_mixed(bool mlp, int mb, int* per_sm);
+int fused_deferred_threads(int mb);
 // Threads of a fused / update CTA for tile rows utr.
 inline int stage_threads(int utr) { return (utr + 1) * TILE_Q; }
 // Tile rows the fused kernel is instantiated for: utr when it is a tile

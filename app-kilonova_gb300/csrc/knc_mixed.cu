@@ -731,22 +731,6 @@ __global__ void __launch_bounds__(STRIP_WARPS * 32, 5)
     stage_fused_body<float, true, 8, MixedC2p<MLP>, STRIP_WARPS * 32, true>(a, g, f);
 }
 
-// The fused stage with the deferring recovery and warp strips, the separate
-// form's five launches in one (CTAs of 4 warps, all resident):
-//   A  work items claimed by warps: ghost rows of both mesh ends in groups of
-//      32 zones, then the recovery tiles, rows walked with the next rows copied
-//      ahead (recover_rows_tile; zones needing the FP64 recovery are listed);
-//   -- barrier --
-//   B  the listed zones densely (recover_high_groups, learned guess on the
-//      tensor cores); -- barrier, only waited on when the list holds a zone --
-//      then the halo remaps across polar-resolution changes (they copy a
-//      coarser neighbour's recovered primitives, so they follow the dense
-//      pass); -- barrier, only waited on with remaps --
-//   C  the warp strips of the update.
-// Every launch counts three barrier arrivals per CTA (the host advances its
-// barrier epoch by three grids); a barrier whose phase has no work is passed
-// with its arrival only. The phases call the functions of the separate
-// kernels, so the two forms give bit-identical states.
 // The phases of the fused deferring stage; each sums its recovery statistics
 // (and the time-step reduction) like its separate kernel does.
 // Phase A of the fused deferring stage, per warp: work items claimed one at a
@@ -774,17 +758,17 @@ __device__ __forceinline__ void fused_phase_a(const StageArgs& a, const GhostArg
     warp_reduce_stats(a.status, st.zones, st.it64, st.it32, st.fbs, st.dtz, a.compute_dt != 0);
 }
 
-template <bool MLP>
+template <bool MLP, int WARPS>
 __device__ __forceinline__ void fused_high_phase(const StageArgs& a, unsigned count, MlpWeights& W,
-                                                     __nv_bfloat16* act) {
+                                                 __nv_bfloat16* act) {
     C2pStats st;
-    recover_high_groups<MLP>(a, count, blockIdx.x * STRIP_WARPS + (threadIdx.x >> 5), gridDim.x * STRIP_WARPS, W,
-                             act, st);
+    recover_high_groups<MLP>(a, count, blockIdx.x * WARPS + (threadIdx.x >> 5), gridDim.x * WARPS, W, act, st);
     warp_reduce_stats(a.status, st.zones, st.it64, st.it32, st.fbs, st.dtz, a.compute_dt != 0);
 }
 
+template <int WARPS>
 __device__ __forceinline__ void fused_remap_phase(const StageArgs& a, const FusedArgs& f) {
-    constexpr int NT = STRIP_WARPS * 32;
+    constexpr int NT = WARPS * 32;
     const int per = 2 * f.max_nq;
     const int total = f.nremap * per;
     for (int k = blockIdx.x * NT + threadIdx.x; k < total; k += gridDim.x * NT) {
@@ -793,12 +777,13 @@ __device__ __forceinline__ void fused_remap_phase(const StageArgs& a, const Fuse
     }
 }
 
+template <int WARPS>
 __device__ __forceinline__ void fused_update_phase(const StageArgs& a) {
-    stage_strips<float, true>(a, blockIdx.x * STRIP_WARPS + (int)(threadIdx.x >> 5), gridDim.x * STRIP_WARPS);
+    stage_strips<float, true>(a, blockIdx.x * WARPS + (int)(threadIdx.x >> 5), gridDim.x * WARPS);
 }
 
 // The fused stage with the deferring recovery and warp strips, the separate
-// form's five launches in one (CTAs of 4 warps, all resident):
+// form's five launches in one (CTAs of WARPS warps, all resident):
 //   A  work items claimed by warps: ghost rows of both mesh ends in groups of
 //      32 zones, then the recovery tiles, rows walked with the next rows copied
 //      ahead (recover_rows_tile; zones needing the FP64 recovery are listed);
@@ -813,16 +798,26 @@ __device__ __forceinline__ void fused_update_phase(const StageArgs& a) {
 // barrier epoch by three grids); a barrier whose phase has no work is passed
 // with its arrival only. The phases call the functions of the separate
 // kernels, so the two forms give bit-identical states.
-template <bool MLP, int MB>
-__global__ void __launch_bounds__(STRIP_WARPS * 32, MB)
+// Shared memory (dynamic): each warp's staging slots of the recovery, then
+// (with the learned guess) the network and one activation tile per warp.
+template <bool MLP, int WARPS>
+constexpr size_t fused_deferred_smem_bytes() {
+    return sizeof(double) * WARPS * C2P_DEPTH * NFIELD * 32 +
+           (MLP ? sizeof(MlpWeights) + WARPS * MLP_ACT_ELEMS * sizeof(__nv_bfloat16) : 0);
+}
+
+template <bool MLP, int WARPS, int MB>
+__global__ void __launch_bounds__(WARPS * 32, MB)
     stage_fused_deferred_kernel(const __grid_constant__ StageArgs a, const __grid_constant__ GhostArgs g,
                                 const __grid_constant__ FusedArgs f) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ __align__(16) double sU[STRIP_WARPS][C2P_DEPTH][NFIELD][32];
     __shared__ int run_update;
-    constexpr int NT = STRIP_WARPS * 32;
-    MlpWeights& W = *reinterpret_cast<MlpWeights*>(smem_raw);
-    __nv_bfloat16* act = reinterpret_cast<__nv_bfloat16*>(smem_raw + sizeof(MlpWeights)) +
+    constexpr int NT = WARPS * 32;
+    typedef double Slots[C2P_DEPTH][NFIELD][32];
+    Slots* sU = reinterpret_cast<Slots*>(smem_raw);
+    unsigned char* mlp_area = smem_raw + sizeof(double) * WARPS * C2P_DEPTH * NFIELD * 32;
+    MlpWeights& W = *reinterpret_cast<MlpWeights*>(mlp_area);
+    __nv_bfloat16* act = reinterpret_cast<__nv_bfloat16*>(mlp_area + sizeof(MlpWeights)) +
                          (threadIdx.x >> 5) * MLP_ACT_ELEMS;
     // a failure in an earlier stage stops the step; every CTA still arrives
     // at every barrier
@@ -847,12 +842,12 @@ __global__ void __launch_bounds__(STRIP_WARPS * 32, MB)
             mlp_load(W, a.mlp);
             __syncthreads();
         }
-        fused_high_phase<MLP>(a, count, W, act);
+        fused_high_phase<MLP, WARPS>(a, count, W, act);
     }
     if (count > 0u) grid_barrier(a.status, f.bar_base + 2ull * gridDim.x, f.spin_limit);
     else grid_arrive(a.status);
     if (f.nremap > 0) {
-        if (run) fused_remap_phase(a, f);
+        if (run) fused_remap_phase<WARPS>(a, f);
         grid_barrier(a.status, f.bar_base + 3ull * gridDim.x, f.spin_limit);
     } else {
         grid_arrive(a.status);
@@ -863,37 +858,59 @@ __global__ void __launch_bounds__(STRIP_WARPS * 32, MB)
         run_update = *(volatile unsigned long long*)&a.status->err_key == NO_ERROR &&
                      *(volatile int32_t*)&a.status->bar_abort == 0;
     __syncthreads();
-    if (run_update) fused_update_phase(a);
+    if (run_update) fused_update_phase<WARPS>(a);
 }
 
-// MB: resident CTAs per SM the register allocation is sized for (4: no
-// spills; 5: more warps)
-template <bool MLP, int MB>
+// The variants: CTAs of 4 warps built for 4 (no spills) or 5 resident CTAs
+// per SM, or one CTA of FUSED_WIDE_WARPS warps per SM (fewer arrivals at each
+// grid barrier: one per SM instead of four or five).
+constexpr int FUSED_WIDE_WARPS = 20;
+
+template <bool MLP, int WARPS, int MB>
+static cudaError_t fused_deferred_configure() {
+    static bool done = false;   // per process: the library serves one device at a time
+    if (done) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(stage_fused_deferred_kernel<MLP, WARPS, MB>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)fused_deferred_smem_bytes<MLP, WARPS>());
+    if (e == cudaSuccess) done = true;
+    return e;
+}
+
+template <bool MLP, int WARPS, int MB>
 static cudaError_t fused_deferred(const StageArgs& a, const GhostArgs& g, const FusedArgs& f, int grid,
                                   cudaStream_t s) {
+    const cudaError_t e = fused_deferred_configure<MLP, WARPS, MB>();
+    if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(STRIP_WARPS * 32);
-    cfg.dynamicSmemBytes = fused_strip_smem_bytes<MLP>();
+    cfg.blockDim = dim3(WARPS * 32);
+    cfg.dynamicSmemBytes = fused_deferred_smem_bytes<MLP, WARPS>();
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, stage_fused_deferred_kernel<MLP, MB>, a, g, f);
+    return cudaLaunchKernelEx(&cfg, stage_fused_deferred_kernel<MLP, WARPS, MB>, a, g, f);
 }
 
-template <bool MLP, int MB>
+template <bool MLP, int WARPS, int MB>
 static cudaError_t fused_deferred_ctas(int* n) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, stage_fused_deferred_kernel<MLP, MB>, STRIP_WARPS * 32,
-                                                         fused_strip_smem_bytes<MLP>());
+    const cudaError_t e = fused_deferred_configure<MLP, WARPS, MB>();
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, stage_fused_deferred_kernel<MLP, WARPS, MB>, WARPS * 32,
+                                                         fused_deferred_smem_bytes<MLP, WARPS>());
 }
 
 cudaError_t fused_deferred_max_ctas_mixed(bool mlp, int mb, int* n) {
-    if (mb == 4) return mlp ? fused_deferred_ctas<true, 4>(n) : fused_deferred_ctas<false, 4>(n);
-    return mlp ? fused_deferred_ctas<true, 5>(n) : fused_deferred_ctas<false, 5>(n);
+    if (mb == 1)
+        return mlp ? fused_deferred_ctas<true, FUSED_WIDE_WARPS, 1>(n) : fused_deferred_ctas<false, FUSED_WIDE_WARPS, 1>(n);
+    if (mb == 4) return mlp ? fused_deferred_ctas<true, STRIP_WARPS, 4>(n) : fused_deferred_ctas<false, STRIP_WARPS, 4>(n);
+    return mlp ? fused_deferred_ctas<true, STRIP_WARPS, 5>(n) : fused_deferred_ctas<false, STRIP_WARPS, 5>(n);
 }
+
+int fused_deferred_threads(int mb) { return (mb == 1 ? FUSED_WIDE_WARPS : STRIP_WARPS) * 32; }
 
 template <bool MLP>
 static cudaError_t fused_strip_mixed(const StageArgs& a, const GhostArgs& g, const FusedArgs& f, int grid,
@@ -922,9 +939,15 @@ cudaError_t launch_stage_fused_mixed(const StageArgs& a, const GhostArgs& g, con
                                      cudaStream_t s) {
     const bool mlp = a.mlp != nullptr;
     if (a.strips && a.high) {
-        // built for 4 CTAs per SM (no spills) or 5 (more warps), like the strip kernels
-        if (a.strip_ctas == 4) return mlp ? fused_deferred<true, 4>(a, g, f, grid, s) : fused_deferred<false, 4>(a, g, f, grid, s);
-        return mlp ? fused_deferred<true, 5>(a, g, f, grid, s) : fused_deferred<false, 5>(a, g, f, grid, s);
+        // one wide CTA per SM, or 4-warp CTAs built for 4 per SM (no spills) or 5 (more warps)
+        if (a.fused_wide)
+            return mlp ? fused_deferred<true, FUSED_WIDE_WARPS, 1>(a, g, f, grid, s)
+                       : fused_deferred<false, FUSED_WIDE_WARPS, 1>(a, g, f, grid, s);
+        if (a.strip_ctas == 4)
+            return mlp ? fused_deferred<true, STRIP_WARPS, 4>(a, g, f, grid, s)
+                       : fused_deferred<false, STRIP_WARPS, 4>(a, g, f, grid, s);
+        return mlp ? fused_deferred<true, STRIP_WARPS, 5>(a, g, f, grid, s)
+                   : fused_deferred<false, STRIP_WARPS, 5>(a, g, f, grid, s);
     }
     if (a.strips) return mlp ? fused_strip_mixed<true>(a, g, f, grid, s) : fused_strip_mixed<false>(a, g, f, grid, s);
     switch (fused_tr(a.utr)) {

@@ -621,11 +621,12 @@ def run_knc(args):
         # run replays captured folds, where launch gaps are hidden, so the
         # other family of shapes is timed the same way too: the separate
         # deferring launches, or every RK3 stage as one cooperative launch (the
-        # fused deferring form at 4 and 5 resident CTAs per SM)
+        # fused deferring form with one 20-warp CTA per SM, or 4 or 5 4-warp
+        # CTAs per SM)
         fused = auto if t["fused"] else None
         separate = None if t["fused"] else auto
         if fused is None:
-            for k in (4, 5):
+            for k in (1, 4, 5):
                 r = run_c4(dict(tile_rows=rows, fused=True, strip=True, ctas_per_sm=k, deferred=True))
                 if fused is None or r["ms_per_step"] < fused["ms_per_step"]:
                     fused = r

@@ -298,26 +298,28 @@ def test_mixed_deferred_recovery_matches_inline(learned):
     assert _same(runs[0].state(), runs[1].state())
 
 
-def _mixed_strips(w, fused, deferred, batched, mlp=None, steps=6, rows=16):
+def _mixed_strips(w, fused, deferred, batched, mlp=None, steps=6, rows=16, ctas=0):
     import knc
     g, _ = make_pair(w, gpu=True)
     g.set_precision(knc.abi.KNC_PRECISION_MIXED)
     if mlp is not None:
         g.set_c2p_guess(knc.abi.KNC_GUESS_MLP, mlp)
-    g.set_tuning(tile_rows=rows, strip=True, fused=fused, deferred=deferred)
+    g.set_tuning(tile_rows=rows, strip=True, fused=fused, deferred=deferred, ctas_per_sm=ctas)
     g.set_batched(batched)
     for _ in range(steps // 3):
         g.advance(3)
     return g
 
 
+@pytest.mark.parametrize("ctas", [0, 1, 5])
 @pytest.mark.parametrize("name", ["uneven_small", "jet_small", "wind_small"])
-def test_mixed_fused_deferred_matches_separate(name):
+def test_mixed_fused_deferred_matches_separate(name, ctas):
     """The fused stage with the deferring recovery (ghost rows, recovery,
     dense FP64 pass, remaps and update in one cooperative launch) equals the
     separate deferring launches bit for bit: on a moving uneven mesh (remaps
     every stage), on the W = 100 jet with the learned guess (listed zones, so
-    the dense pass and its barrier run) and on the wind (neither)."""
+    the dense pass and its barrier run) and on the wind (neither); with
+    4-warp CTAs at 4 (ctas 0) or 5 per SM, and with one 20-warp CTA per SM."""
     from knc import learned, workloads
     w = workloads.WORKLOADS[name]()
     wts = None
@@ -327,7 +329,7 @@ def test_mixed_fused_deferred_matches_separate(name):
         wts[-3:] = 1.0
     steps = 12 if name == "uneven_small" else 6
     ref = _mixed_strips(w, False, True, False, mlp=wts, steps=steps)
-    g = _mixed_strips(w, True, True, True, mlp=wts, steps=steps)
+    g = _mixed_strips(w, True, True, True, mlp=wts, steps=steps, ctas=ctas)
     assert g.block_indexes() == ref.block_indexes()
     assert _same(g.state(), ref.state())
     assert g.time() == ref.time()
