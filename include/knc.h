@@ -266,12 +266,18 @@ int knc_set_batched(knc_ctx* ctx, int32_t graph);
  *                a tile runs on (tile_rows + 1) warps), or of a warp strip
  *                (4 to 64)
  *   fused        0: a stage is four launches (ghost rows, recovery, remaps,
- *                update); 1: one persistent cooperative launch whose phases
- *                are separated by bounded grid barriers (bit-identical result)
+ *                update; the deferring recovery adds its dense pass); 1: one
+ *                persistent cooperative launch whose phases are separated by
+ *                bounded grid barriers (bit-identical result). Mixed
+ *                precision with warp strips and KNC_RECOVERY_DEFERRED: the
+ *                deferring recovery, its dense pass, the remaps and the
+ *                update in that one launch
  *   ctas_per_sm  fused grid = ctas_per_sm x SMs CTAs (0: the occupancy bound;
  *                larger values are clamped to it); mixed warp strips: the
  *                CTAs per SM the strip kernel's registers are sized for
- *                (4, 5 or 6; other values: 4)
+ *                (4, 5 or 6; other values: 4); the fused deferring stage:
+ *                1 runs one CTA of 20 warps per SM, 5 five CTAs of 4 warps,
+ *                other values four CTAs of 4 warps
  *   update_form  separate form only: KNC_UPDATE_TILE, or KNC_UPDATE_TILE_TMA
  *                (mixed precision: each tile's primitives with halo, U_in and
  *                U_base staged by tensor copies into double-buffered shared
@@ -286,7 +292,7 @@ typedef struct knc_tuning {
     int32_t fused;
     int32_t ctas_per_sm;
     int32_t update_form;
-    int32_t recovery_form;   /* mixed, separate form: KNC_RECOVERY_* */
+    int32_t recovery_form;   /* mixed: KNC_RECOVERY_* (fused: with warp strips only) */
 } knc_tuning;
 /* KNC_RECOVERY_INLINE: each warp recovers its zones, the FP64 ones among
  * them in place; KNC_RECOVERY_DEFERRED: zones that need the FP64 recovery
@@ -299,7 +305,10 @@ int knc_get_tuning(const knc_ctx* ctx, knc_tuning* tuning);
  * per SM x update form) with `reps` first-stage launches each on the live state (they write
  * only the scratch buffer and primitives, so the state is unchanged), keeps
  * the fastest and returns it with its time per stage (either output may be
- * NULL). */
+ * NULL). The stages are launched from the host one by one, so the fused
+ * forms are candidates only when the context is not batched: inside a
+ * batched context's captured graphs the separate launches' gaps are hidden
+ * and they measured faster. */
 int knc_autotune(knc_ctx* ctx, int32_t reps, knc_tuning* best, double* ms_per_stage);
 
 /* Mixed precision: the Lorentz-factor split (default 2.0). Zones whose
