@@ -1371,6 +1371,9 @@ int reset_status(knc_ctx* c, bool keep_stats) {
         CK(cudaMemsetAsync(&d->bar_count, 0, sizeof(d->bar_count) + sizeof(d->bar_abort), c->stream));
         CK(cudaMemsetAsync(d->high_count, 0, sizeof(d->high_count), c->stream));
         CK(cudaMemsetAsync(d->hp_count, 0, sizeof(d->hp_count) + sizeof(d->hp_claim), c->stream));
+        // the fused deferring stage's item counter: a launch whose grid
+        // barrier gave up may leave it counting
+        CK(cudaMemsetAsync(&d->item_claim, 0, sizeof(d->item_claim), c->stream));
     } else {
         DevStatus s;
         std::memset(&s, 0, sizeof(s));

@@ -103,7 +103,9 @@ struct DevStatus {
     unsigned hp_count[2];
     unsigned hp_claim[2];
     // the fused deferring stage: phase A's work items (ghost-row groups, then
-    // recovery tiles) claimed by warps; zero between launches
+    // recovery tiles) claimed by warps; zero between launches (each launch
+    // zeroes it once its first barrier has passed, and every status reset
+    // does, for a launch whose barrier gave up)
     unsigned item_claim;
     unsigned pad3;
 };

@@ -868,20 +868,14 @@ constexpr int FUSED_WIDE_WARPS = 20;
 
 template <bool MLP, int WARPS, int MB>
 static cudaError_t fused_deferred_configure() {
-    static bool done = false;   // per process: the library serves one device at a time
-    if (done) return cudaSuccess;
-    const cudaError_t e = cudaFuncSetAttribute(stage_fused_deferred_kernel<MLP, WARPS, MB>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)fused_deferred_smem_bytes<MLP, WARPS>());
-    if (e == cudaSuccess) done = true;
-    return e;
+    return cudaFuncSetAttribute(stage_fused_deferred_kernel<MLP, WARPS, MB>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)fused_deferred_smem_bytes<MLP, WARPS>());
 }
 
 template <bool MLP, int WARPS, int MB>
 static cudaError_t fused_deferred(const StageArgs& a, const GhostArgs& g, const FusedArgs& f, int grid,
                                   cudaStream_t s) {
-    const cudaError_t e = fused_deferred_configure<MLP, WARPS, MB>();
-    if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(WARPS * 32);
@@ -897,8 +891,6 @@ static cudaError_t fused_deferred(const StageArgs& a, const GhostArgs& g, const 
 
 template <bool MLP, int WARPS, int MB>
 static cudaError_t fused_deferred_ctas(int* n) {
-    const cudaError_t e = fused_deferred_configure<MLP, WARPS, MB>();
-    if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, stage_fused_deferred_kernel<MLP, WARPS, MB>, WARPS * 32,
                                                          fused_deferred_smem_bytes<MLP, WARPS>());
 }
@@ -979,9 +971,13 @@ static cudaError_t configure_fused_mixed() {
 
 cudaError_t configure_f64();
 
+// Kernel attributes (shared memory above the default limit), once per device.
 cudaError_t configure_kernels() {
-    static cudaError_t result = cudaErrorNotReady;
-    if (result == cudaSuccess) return result;
+    constexpr int MAX_DEVICES = 64;
+    static bool done[MAX_DEVICES] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) dev = 0;
+    if (done[dev]) return cudaSuccess;
     cudaError_t e = configure_f64();
     if (e == cudaSuccess) e = configure_update_mixed<4>();
     if (e == cudaSuccess) e = configure_update_mixed<8>();
@@ -1001,7 +997,13 @@ cudaError_t configure_kernels() {
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(c2p_mixed_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(sizeof(MlpWeights) + 8 * MLP_ACT_ELEMS * sizeof(__nv_bfloat16)));
-    result = e;
+    if (e == cudaSuccess) e = fused_deferred_configure<false, STRIP_WARPS, 4>();
+    if (e == cudaSuccess) e = fused_deferred_configure<true, STRIP_WARPS, 4>();
+    if (e == cudaSuccess) e = fused_deferred_configure<false, STRIP_WARPS, 5>();
+    if (e == cudaSuccess) e = fused_deferred_configure<true, STRIP_WARPS, 5>();
+    if (e == cudaSuccess) e = fused_deferred_configure<false, FUSED_WIDE_WARPS, 1>();
+    if (e == cudaSuccess) e = fused_deferred_configure<true, FUSED_WIDE_WARPS, 1>();
+    done[dev] = e == cudaSuccess;
     return e;
 }
 

@@ -459,13 +459,11 @@ namespace {
 
 size_t train_smem_bytes() { return sizeof(TcTrainSmem) + 1024; }   // + alignment of the operand tiles
 
+// The training kernel's shared memory, on the current device (every call:
+// the library may serve several devices).
 cudaError_t configure_train() {
-    static bool done = false;
-    if (done) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(mlp_train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)train_smem_bytes());
-    if (e == cudaSuccess) done = true;
-    return e;
+    return cudaFuncSetAttribute(mlp_train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)train_smem_bytes());
 }
 
 // One CTA per 128-row tile up to one per SM (the kernel's shared memory

@@ -17,17 +17,24 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_deferred", "mixed_deferred_wide"])
 def test_fused_barrier_gives_up_and_reports_timeout(precision):
+    """mixed_deferred: the fused stage with the deferring recovery (its
+    first barrier follows phase A's claimed items); _wide: one 20-warp CTA
+    per SM."""
     import knc
     from knc import abi, workloads
     w = workloads.wind_small()
     s = knc.build_solver(w)
     ref = knc.build_solver(w)
     for g in (s, ref):
-        if precision == "mixed":
+        if precision != "fp64":
             g.set_precision(abi.KNC_PRECISION_MIXED)
-        g.set_tuning(tile_rows=8, fused=True)
+        if precision.startswith("mixed_deferred"):
+            g.set_tuning(tile_rows=16, fused=True, strip=True, deferred=True,
+                         ctas_per_sm=1 if precision.endswith("wide") else 0)
+        else:
+            g.set_tuning(tile_rows=8, fused=True)
         g.advance(1)
     zones = sum(int(np.prod(s.shape_of(i))) for i in s.block_indexes())
     cons, scal = np.empty((zones, 4)), np.empty(zones)
