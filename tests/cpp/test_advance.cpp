@@ -10,6 +10,8 @@
 //   hydro_error_at_position       a negative density in one zone: advance
 //                                 throws knc::HydroError with the oracle's
 //                                 kind, block, zone, centroid and value
+//   mixed_precision_within_gate   the mixed-precision stage, 100 steps: lab-frame
+//                                 density L1 against the oracle at most 1e-6
 //   state_round_trip              load then state() returns the same blocks
 //
 // Exit status 0 when every test passes; one line per test on stdout.
@@ -155,6 +157,38 @@ bool hydro_error_at_position(std::string& why) {
     return why = "no HydroError thrown", false;
 }
 
+bool mixed_precision_within_gate(std::string& why) {
+    // the mixed-precision stage (FP32 fluxes, FP64 state and recovery above
+    // the Lorentz-factor split) through the same surface: lab-frame density L1
+    // against the FP64 oracle at most 1e-6 after 100 steps
+    const auto hydro = wind_hydro();
+    const auto mesh = wind_mesh();
+    knc::Engine engine(hydro, mesh);
+    engine.set_model(wind_model());
+    engine.set_precision(KNC_PRECISION_MIXED);
+    knc::State state = engine.from_model(0.0);
+    Oracle oracle(hydro, mesh);
+    const knc_model_params model = wind_model();
+    oracle_set_model(oracle.ctx, &model);
+    oracle.load(state);
+    state = knc::advance(std::move(state), engine, 100);
+    oracle_advance(oracle.ctx, 100);
+    const knc::State ref = oracle.state();
+    if (state.time != ref.time) return why = "time differs", false;
+    double num = 0.0, den = 0.0;
+    for (const auto& kv : ref.solution) {
+        const knc::BlockState& b = kv.second;
+        const knc::BlockState& g = state.solution.at(kv.first);
+        for (size_t z = 0; z < b.conserved.size(); z += 4) {
+            num += std::fabs(g.conserved[z] - b.conserved[z]);
+            den += std::fabs(b.conserved[z]);
+        }
+    }
+    const double l1 = num / den;
+    if (!(l1 <= 1e-6)) return why = "density L1 " + std::to_string(l1), false;
+    return true;
+}
+
 bool state_round_trip(std::string& why) {
     const auto hydro = wind_hydro();
     const auto mesh = wind_mesh();
@@ -176,6 +210,7 @@ int main() {
     };
     const Case cases[] = {{"advance_matches_oracle", advance_matches_oracle},
                           {"hydro_error_at_position", hydro_error_at_position},
+                          {"mixed_precision_within_gate", mixed_precision_within_gate},
                           {"state_round_trip", state_round_trip}};
     int failed = 0;
     for (const Case& c : cases) {
