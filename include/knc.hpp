@@ -166,6 +166,23 @@ public:
     void set_model(const knc_model_params& model) { check(knc_set_model(ctx_, &model), "knc_set_model"); }
     void set_precision(int32_t precision) { check(knc_set_precision(ctx_, precision), "knc_set_precision"); }
     void set_batched(bool graph) { check(knc_set_batched(ctx_, graph ? 1 : 0), "knc_set_batched"); }
+    // KNC_GUESS_PLAIN (weights unused) or KNC_GUESS_MLP with a packed weight
+    // vector of knc_mlp_num_params() floats
+    void set_c2p_guess(int32_t guess, const std::vector<float>& weights = {}) {
+        check(knc_set_c2p_guess(ctx_, guess, weights.empty() ? nullptr : weights.data(), weights.size()),
+              "knc_set_c2p_guess");
+    }
+    // uneven blocks: (nr, nq) of block indexes first .. first + nr.size() - 1
+    void set_block_shapes(int32_t first, const std::vector<int32_t>& nr, const std::vector<int32_t>& nq) {
+        if (nr.size() != nq.size()) throw Error(KNC_ERR_INVALID_ARGUMENT, "set_block_shapes: nr and nq differ in length");
+        check(knc_set_block_shapes(ctx_, first, (int32_t)nr.size(), nr.data(), nq.data()), "knc_set_block_shapes");
+    }
+    void set_tuning(const knc_tuning& t) { check(knc_set_tuning(ctx_, &t), "knc_set_tuning"); }
+    knc_tuning autotune(int32_t reps = 3) {
+        knc_tuning t{};
+        check(knc_autotune(ctx_, reps, &t, nullptr), "knc_autotune");
+        return t;
+    }
 
     // State::from_model at time t (src/state.rs:55-69, 128-130)
     State from_model(double time) {
