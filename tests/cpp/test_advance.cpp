@@ -12,6 +12,8 @@
 //                                 kind, block, zone, centroid and value
 //   mixed_precision_within_gate   the mixed-precision stage, 100 steps: lab-frame
 //                                 density L1 against the oracle at most 1e-6
+//   newtonian_sphere_matches_oracle  NewtonianHydro, HLLC, adaptive time step,
+//                                 the over-dense sphere: 40 steps bit for bit
 //   state_round_trip              load then state() returns the same blocks
 //
 // Exit status 0 when every test passes; one line per test on stdout.
@@ -61,7 +63,8 @@ knc_model_params wind_model() {
 // The oracle behind the same surface: a State in, a State out.
 struct Oracle {
     oracle_ctx* ctx = nullptr;
-    Oracle(const knc::RelativisticHydro& h, const knc::Mesh& m) {
+    template <class Hydro>
+    Oracle(const Hydro& h, const knc::Mesh& m) {
         const knc_hydro_params hp = h.to_c();
         const knc_mesh_params mp = m.to_c();
         if (oracle_create(&hp, &mp, 8, &ctx) != KNC_OK) throw std::runtime_error("oracle_create");
@@ -189,6 +192,34 @@ bool mixed_precision_within_gate(std::string& why) {
     return true;
 }
 
+bool newtonian_sphere_matches_oracle(std::string& why) {
+    // NewtonianHydro (gamma 5/3, HLLC, RK2, always an adaptive time step) on
+    // the seeded over-dense sphere at rest: 40 steps in folds of 10, bit for bit
+    knc::NewtonianHydro hydro;
+    hydro.gamma_law_index = 5.0 / 3.0;
+    hydro.riemann_solver = knc::RiemannSolver::HLLC;
+    const auto mesh = wind_mesh();
+    knc_model_params sphere{};
+    sphere.kind = KNC_MODEL_SPHERE;
+    sphere.seed = 1;
+    sphere.p[0] = 10.0;   // rho inside
+    sphere.p[1] = 1.0;    // rho outside
+    sphere.p[2] = 2.0;    // sphere radius
+    sphere.p[3] = 1e-2;   // pressure
+    sphere.p[4] = 0.01;   // noise amplitude
+    knc::Engine engine(hydro, mesh);
+    engine.set_model(sphere);
+    knc::State state = engine.from_model(0.0);
+    Oracle oracle(hydro, mesh);
+    oracle_set_model(oracle.ctx, &sphere);
+    oracle.load(state);
+    for (int k = 0; k < 4; ++k) {
+        state = knc::advance(std::move(state), engine, 10);
+        oracle_advance(oracle.ctx, 10);
+    }
+    return same_state(state, oracle.state(), why);
+}
+
 bool state_round_trip(std::string& why) {
     const auto hydro = wind_hydro();
     const auto mesh = wind_mesh();
@@ -211,6 +242,7 @@ int main() {
     const Case cases[] = {{"advance_matches_oracle", advance_matches_oracle},
                           {"hydro_error_at_position", hydro_error_at_position},
                           {"mixed_precision_within_gate", mixed_precision_within_gate},
+                          {"newtonian_sphere_matches_oracle", newtonian_sphere_matches_oracle},
                           {"state_round_trip", state_round_trip}};
     int failed = 0;
     for (const Case& c : cases) {

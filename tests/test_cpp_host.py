@@ -44,4 +44,4 @@ def test_cpp_host_matches_oracle(tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert r.stdout.count("ok  ") == 4, r.stdout
+    assert r.stdout.count("ok  ") == 5, r.stdout
